@@ -1,0 +1,142 @@
+/*
+ * flowreg_gb300.h -- C ABI of the GB300 (sm_103a) backend for pyflowreg's
+ * variational optical-flow path.
+ *
+ * Plain C: device pointers are `float*` to CUDA device memory, streams are
+ * passed as `void*` (a cudaStream_t; NULL = legacy default stream).  Arrays
+ * use numpy's C order unless stated.  All work is enqueued on the stream;
+ * nothing synchronises the host except where a function says so.  Functions
+ * return FRG_OK or an error code; frg_last_error() then describes it
+ * (thread-local).
+ *
+ * Reference interfaces (pyflowreg, paths relative to src/pyflowreg/):
+ *   frg_plan_create / frg_set_reference / frg_get_displacement
+ *       replace get_displacement(fixed, moving, ...)     core/optical_flow.py:773-929
+ *       called once per frame by the executors          motion_correction/parallelization/sequential.py:296-298
+ *   frg_level_solve  replaces compute_flow via the level_solver_backend seam
+ *                                                        core/optical_flow.py:348-411, 584-606
+ *                                                        core/level_solver.py:158-369
+ *   frg_imregister   replaces imregister_wrapper          core/warping.py:160-234
+ *   frg_resize       replaces imresize_fused_gauss_cubic  util/resize_util.py:232-254
+ *   frg_motion_tensor replaces get_motion_tensor_gc/_gray core/optical_flow.py:73-228
+ *   frg_median5      replaces median_filter(size=(5,5), mode="mirror")
+ *                                                        core/optical_flow.py:607-609
+ */
+#ifndef FLOWREG_GB300_H
+#define FLOWREG_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FRG_OK 0
+#define FRG_EINVAL 1          /* bad argument (shape, pointer, option) */
+#define FRG_ENOMEM 2          /* device or host allocation failed */
+#define FRG_ECUDA 3           /* a CUDA call failed */
+#define FRG_EUNSUPPORTED 4    /* option not implemented by this backend */
+
+#define FRG_MAX_CHANNELS 8
+#define FRG_ABI_VERSION 1
+
+/* Optical-flow options, the subset of OFOptions.to_dict()
+ * (motion_correction/OF_options.py:1084-1101) that get_displacement uses. */
+typedef struct frg_params {
+    double alpha_x, alpha_y;              /* smoothness weights (OFOptions.alpha) */
+    double eta;                           /* pyramid factor, 0 < eta <= 1 */
+    int levels;                           /* maximum number of pyramid levels */
+    int min_level;                        /* finest level computed (effective value, >= 0) */
+    int iterations;                       /* SOR iterations per level */
+    int update_lag;                       /* iterations between nonlinearity updates */
+    double a_smooth;                      /* smoothness Charbonnier exponent (1.0 only) */
+    double a_data[FRG_MAX_CHANNELS];      /* data-term exponent per channel */
+    int const_assumption;                 /* 0: gradient constancy "gc", 1: gray value "gray" */
+    double omega;                         /* SOR relaxation factor (reference: 1.95) */
+} frg_params;
+
+typedef struct frg_plan frg_plan;
+
+int frg_version(void);
+const char* frg_last_error(void);
+
+/* Host-only helpers (no GPU needed), exposing the plan's schedule for tests:
+ *   frg_schedule: pyramid levels, coarsest first, as _solve_displacement_stage
+ *     iterates them (core/optical_flow.py:494-518, 572-577): sizes and the
+ *     scaled alpha.  Returns the number of levels (writes at most max_levels),
+ *     or a negative error code.
+ *   frg_resize_tables: tap indices/weights (out_len, P) of the fused
+ *     Gauss-cubic resize (util/resize_util.py:194-229).  Returns P; writes
+ *     nothing if P > max_taps.
+ *   frg_iteration_passes: how the SOR iterations are cut into wavefront
+ *     passes at the nonlinearity ticks ((t+1) % update_lag == 0,
+ *     core/level_solver.py:230).  G[i] iterations per pass; fold_mode[i] = -1
+ *     when the pass reuses the previous coefficients, else bit 0 = first
+ *     pass (du = dv = 0), bit 1 = psi recomputed.  Returns the pass count. */
+int frg_schedule(const frg_params* params, int height, int width, int max_levels, int* h, int* w,
+                 double* alpha_x, double* alpha_y);
+int frg_resize_tables(int in_len, int out_len, double sigma, int max_taps, int* idx, float* wt);
+int frg_iteration_passes(int iterations, int update_lag, int max_passes, int* G, int* fold_mode);
+
+/* A plan fixes the frame shape (height x width x channels), the options and
+ * the largest batch.  It owns all device memory it needs (tables, the
+ * reference pyramid and the per-batch workspace); frg_plan_device_bytes
+ * reports the total.  A plan is not thread-safe: use one per stream. */
+int frg_plan_create(const frg_params* params, int height, int width, int channels, int max_frames,
+                    frg_plan** out);
+void frg_plan_destroy(frg_plan* plan);
+size_t frg_plan_device_bytes(const frg_plan* plan);
+int frg_plan_num_levels(const frg_plan* plan);
+/* level 0 is the coarsest level actually solved */
+int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double* alpha_x,
+                        double* alpha_y);
+
+/* Reference (fixed) frame (height, width, channels) float32 and the per-pixel
+ * channel weight (height, width, channels) float32 (NULL: 1/channels), as
+ * get_displacement receives them after its input normalisation
+ * (core/optical_flow.py:846-879).  Builds the reference and weight pyramids. */
+int frg_set_reference(frg_plan* plan, const float* fixed, const float* weight, void* stream);
+
+/* Flow of n_frames moving frames (n_frames, height, width, channels) against
+ * the reference: flow_out (n_frames, height, width, 2) with [..., 0] = u
+ * (columns) and [..., 1] = v (rows).  uv_init (height, width, 2) or NULL is
+ * the initial field shared by all frames (the executors' w_init). */
+int frg_get_displacement(frg_plan* plan, int n_frames, const float* moving, const float* uv_init,
+                         float* flow_out, void* stream);
+
+/* Backward warp of frames (n_frames, height, width, channels) by flow
+ * (n_frames, height, width, 2); out-of-bounds pixels take reference
+ * (height, width, channels).  cubic = 1 bicubic, 0 bilinear. */
+int frg_imregister(int n_frames, int height, int width, int channels, const float* frames,
+                   const float* flow, const float* reference, int cubic, float* out, void* stream);
+
+/* One pyramid level of the lagged-nonlinearity SOR in the reference's exact
+ * (column-major lexicographic) update order.  J is six arrays (m, n, K) back
+ * to back in the order J11, J22, J33, J12, J13, J23; weight (m, n, K); u, v,
+ * du, dv (m, n); m, n include the one-pixel ring.  hx scales column
+ * differences, hy row differences.  du/dv rings are set to the adjacent
+ * interior values.  Allocates its scratch with cudaMallocAsync on `stream`. */
+int frg_level_solve(int m, int n, int K, const float* J, const float* weight, const float* u,
+                    const float* v, double alpha_x, double alpha_y, int iterations, int update_lag,
+                    const double* a_data, double a_smooth, double hx, double hy, double omega,
+                    float* du, float* dv, void* stream);
+
+/* Fused Gauss-cubic resize of n_planes planes (n_planes, ih, iw) to
+ * (n_planes, oh, ow), sigma = 0.6 / min(oh/ih, ow/iw) when that is < 1. */
+int frg_resize(int n_planes, int ih, int iw, const float* src, int oh, int ow, float* dst,
+               void* stream);
+
+/* Motion tensor of one channel: f1, f2 (h, w); out six planes (h+2, w+2)
+ * back to back (J11, J22, J33, J12, J13, J23) with a zero ring.
+ * gray = 0: gradient constancy, 1: gray-value constancy. */
+int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy, double hx, int gray,
+                      float* out, void* stream);
+
+/* 5x5 median with mirror boundary of one plane (h, w), h, w >= 3. */
+int frg_median5(int h, int w, const float* src, float* dst, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOWREG_GB300_H */

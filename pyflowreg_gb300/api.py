@@ -1,0 +1,482 @@
+"""Reference-facing API of the GB300 backend.
+
+Each public function mirrors a pyflowreg function on the optical-flow path --
+same name, arguments, argument meaning, return type and error behaviour -- and
+runs on the GPU through the C ABI (``include/flowreg_gb300.h``):
+
+* ``get_displacement``      core/optical_flow.py:773-929
+* ``imregister_wrapper``    core/warping.py:160-234
+* ``level_solver``          core/optical_flow.py:348-411 (the ``level_solver_backend`` seam)
+* ``imresize_fused_gauss_cubic`` util/resize_util.py:232-254
+* ``get_motion_tensor_gc`` / ``get_motion_tensor_gray`` core/optical_flow.py:73-228
+
+plus batched/device entry points (``get_displacement_batch``,
+``get_displacement_device``, ``imregister_device``) that register many frames
+in one call.  There is no CPU fallback: without a CUDA device these raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+
+try:  # torch provides device memory and streams
+    import torch
+except ImportError:  # pragma: no cover - torch is a hard dependency of the package
+    torch = None
+
+_CONST = {"gc": 0, "gradient": 0, "gray": 1, "brightness": 1, "cs": 2, "census": 2}
+
+
+def _require_cuda():
+    if torch is None or not torch.cuda.is_available():
+        raise RuntimeError("pyflowreg_gb300 needs a CUDA GPU (sm_103a); there is no CPU fallback")
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr())
+
+
+# --------------------------------------------------------------------------
+# Option handling (core/optical_flow.py:414-473, 842-885)
+# --------------------------------------------------------------------------
+def resolve_const_assumption(const_assumption) -> int:
+    if hasattr(const_assumption, "value"):
+        const_assumption = const_assumption.value
+    key = str(const_assumption).strip().lower()
+    if key not in _CONST:
+        supported = "', '".join(sorted(_CONST))
+        raise ValueError(
+            f"Unknown constancy assumption: '{const_assumption}'. Supported values are: '{supported}'."
+        )
+    if _CONST[key] == 2:
+        raise NotImplementedError("the census data term ('cs') is not implemented by the GB300 backend")
+    return _CONST[key]
+
+
+def normalize_gnc_schedule(gnc_schedule):
+    """Validation of core/optical_flow.py:414-432 (the backend then rejects GNC)."""
+    if gnc_schedule is None:
+        return None
+    schedule = np.asarray(gnc_schedule, dtype=np.float64)
+    if schedule.ndim != 1:
+        raise ValueError("gnc_schedule must be a 1D sequence of stage weights")
+    if schedule.size < 2:
+        raise ValueError("gnc_schedule must contain at least two stages")
+    if np.any(schedule < 0.0) or np.any(schedule > 1.0):
+        raise ValueError("gnc_schedule entries must lie in [0, 1]")
+    if not np.all(np.diff(schedule) >= 0.0):
+        raise ValueError("gnc_schedule must be monotone nondecreasing")
+    if not np.isclose(schedule[0], 0.0):
+        raise ValueError("gnc_schedule must start at 0.0")
+    if not np.isclose(schedule[-1], 1.0):
+        raise ValueError("gnc_schedule must end at 1.0")
+    return schedule
+
+
+def normalize_warping_steps(warping_steps):
+    if warping_steps is None:
+        return None
+    steps = int(warping_steps)
+    if steps < 1:
+        raise ValueError("warping_steps must be a positive integer")
+    return steps
+
+
+def normalize_weight(weight, m: int, n: int, K: int) -> np.ndarray:
+    """(m, n, K) float64 weight exactly as get_displacement builds it (:856-879)."""
+    if weight is None:
+        return np.ones((m, n, K), dtype=np.float64) / K
+    weight = np.asarray(weight).astype(np.float64)
+    if weight.ndim < 3:
+        if weight.ndim == 1:
+            if len(weight) < K:
+                ex = np.full(K, 1.0 / K, dtype=np.float64)
+                ex[: len(weight)] = weight
+                weight = ex
+            elif len(weight) > K:
+                weight = weight[:K]
+            weight = weight / weight.sum()
+            weight = np.ones((m, n, K), dtype=np.float64) * weight.reshape(1, 1, -1)
+        else:
+            weight = np.ones((m, n, K), dtype=np.float64) * weight[..., np.newaxis]
+    return weight
+
+
+def normalize_a_data(a_data, K: int) -> np.ndarray:
+    if not isinstance(a_data, np.ndarray):
+        return np.full(K, a_data, dtype=np.float64)
+    return np.ascontiguousarray(a_data, dtype=np.float64)
+
+
+def alpha_pair(alpha):
+    if np.isscalar(alpha):
+        return float(alpha), float(alpha)
+    alpha = list(alpha)
+    return float(alpha[0]), float(alpha[1] if len(alpha) > 1 else alpha[0])
+
+
+def make_params(alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
+                a_smooth=1.0, a_data=0.45, const_assumption="gc", K=1, omega=1.95) -> "_lib.FrgParams":
+    if K > _lib.FRG_MAX_CHANNELS:
+        raise ValueError(f"at most {_lib.FRG_MAX_CHANNELS} channels are supported")
+    p = _lib.FrgParams()
+    p.alpha_x, p.alpha_y = alpha_pair(alpha)
+    p.eta = float(eta)
+    p.levels = int(levels)
+    p.min_level = int(min_level)
+    p.iterations = int(iterations)
+    p.update_lag = int(update_lag)
+    p.a_smooth = float(a_smooth)
+    ad = normalize_a_data(a_data, K)
+    if ad.shape != (K,):
+        raise ValueError(f"a_data must have one entry per channel ({K})")
+    for k in range(K):
+        p.a_data[k] = float(ad[k])
+    p.const_assumption = resolve_const_assumption(const_assumption)
+    p.omega = float(omega)
+    return p
+
+
+def _params_key(p) -> tuple:
+    return (p.alpha_x, p.alpha_y, p.eta, p.levels, p.min_level, p.iterations, p.update_lag, p.a_smooth,
+            tuple(p.a_data), p.const_assumption, p.omega)
+
+
+# --------------------------------------------------------------------------
+# Plans
+# --------------------------------------------------------------------------
+class Plan:
+    """Owns one frg_plan: fixed frame shape, options and maximum batch."""
+
+    def __init__(self, params, H: int, W: int, K: int, max_frames: int):
+        _require_cuda()
+        self.lib = _lib.load()
+        self.H, self.W, self.K, self.max_frames = H, W, K, max_frames
+        self.params = params
+        self.device = torch.cuda.current_device()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.frg_plan_create(ctypes.byref(params), H, W, K, max_frames, ctypes.byref(h)),
+                   "frg_plan_create")
+        self.handle = h
+        self._ref_key = None
+
+    def levels(self):
+        out = []
+        for i in range(self.lib.frg_plan_num_levels(self.handle)):
+            h, w = ctypes.c_int(), ctypes.c_int()
+            ax, ay = ctypes.c_double(), ctypes.c_double()
+            _lib.check(self.lib.frg_plan_level_info(self.handle, i, ctypes.byref(h), ctypes.byref(w),
+                                                    ctypes.byref(ax), ctypes.byref(ay)))
+            out.append((h.value, w.value, ax.value, ay.value))
+        return out
+
+    def device_bytes(self) -> int:
+        return int(self.lib.frg_plan_device_bytes(self.handle))
+
+    def set_reference(self, fixed_t, weight_t=None, stream=None, key=None):
+        """fixed_t (H, W, K) float32 CUDA tensor; weight_t the same shape or None."""
+        if key is not None and key == self._ref_key:
+            return
+        self._check(fixed_t, (self.H, self.W, self.K))
+        if weight_t is not None:
+            self._check(weight_t, (self.H, self.W, self.K))
+        _lib.check(self.lib.frg_set_reference(self.handle, _ptr(fixed_t),
+                                              None if weight_t is None else _ptr(weight_t),
+                                              _stream_ptr(stream)), "frg_set_reference")
+        self._ref_key = key
+
+    def displacement(self, moving_t, uv_t=None, out_t=None, stream=None):
+        """moving_t (T, H, W, K) float32 CUDA tensor -> flow (T, H, W, 2) float32."""
+        T = moving_t.shape[0]
+        self._check(moving_t, (T, self.H, self.W, self.K))
+        if uv_t is not None:
+            self._check(uv_t, (self.H, self.W, 2))
+        if out_t is None:
+            out_t = torch.empty((T, self.H, self.W, 2), dtype=torch.float32, device=moving_t.device)
+        self._check(out_t, (T, self.H, self.W, 2))
+        for t0 in range(0, T, self.max_frames):
+            t1 = min(T, t0 + self.max_frames)
+            _lib.check(self.lib.frg_get_displacement(self.handle, t1 - t0, _ptr(moving_t[t0:t1]),
+                                                     None if uv_t is None else _ptr(uv_t),
+                                                     _ptr(out_t[t0:t1]), _stream_ptr(stream)),
+                       "frg_get_displacement")
+        return out_t
+
+    @staticmethod
+    def _check(t, shape):
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+            raise ValueError("expected a contiguous float32 CUDA tensor")
+        if tuple(t.shape) != tuple(shape):
+            raise ValueError(f"expected shape {tuple(shape)}, got {tuple(t.shape)}")
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.frg_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_plans: dict = {}
+_plans_lock = threading.Lock()
+
+
+def get_plan(params, H: int, W: int, K: int, n_frames: int, max_frames: Optional[int] = None) -> Plan:
+    """Cached plan for (shape, options, device); grown when a larger batch arrives."""
+    _require_cuda()
+    key = (H, W, K, _params_key(params), torch.cuda.current_device())
+    want = max(1, int(max_frames or n_frames))
+    with _plans_lock:
+        plan = _plans.get(key)
+        if plan is None or plan.max_frames < want:
+            if plan is not None:
+                plan.close()
+            plan = Plan(params, H, W, K, want)
+            _plans[key] = plan
+        return plan
+
+
+def clear_plans():
+    with _plans_lock:
+        for p in _plans.values():
+            p.close()
+        _plans.clear()
+
+
+# --------------------------------------------------------------------------
+# get_displacement (core/optical_flow.py:773-929)
+# --------------------------------------------------------------------------
+def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_level, levels, eta, a_smooth,
+             const_assumption, gnc_schedule, warping_steps, level_solver_backend):
+    const = resolve_const_assumption(const_assumption)
+    if normalize_gnc_schedule(gnc_schedule) is not None:
+        raise NotImplementedError("graduated non-convexity (gnc_schedule) is not implemented by the GB300 backend")
+    normalize_warping_steps(warping_steps)
+    if level_solver_backend is not None:
+        raise NotImplementedError("the GB300 backend runs its own level solver; level_solver_backend must be None")
+    fixed = np.asarray(fixed)
+    moving = np.asarray(moving)
+    K = fixed.shape[2] if fixed.ndim == 3 else 1
+    m, n = fixed.shape[:2]
+    w = normalize_weight(weight, m, n, K)
+    params = make_params(alpha, update_lag, iterations, min_level, levels, eta, a_smooth, a_data,
+                         ["gc", "gray"][const], K)
+    return fixed, moving, w, params, m, n, K
+
+
+def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
+                     a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None, weight=None,
+                     level_solver_backend=None, gnc_schedule=None, warping_steps=None):
+    """Drop-in for pyflowreg.core.optical_flow.get_displacement on the GPU.
+
+    Returns the (H, W, 2) float64 displacement, [..., 0] = u (columns),
+    [..., 1] = v (rows), like the reference.
+    """
+    assert fixed.ndim == moving.ndim, (
+        f"Fixed and moving must have same dimensions: fixed.shape={fixed.shape}, moving.shape={moving.shape}"
+    )
+    fixed, moving, w, params, m, n, K = _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations,
+                                                 min_level, levels, eta, a_smooth, const_assumption, gnc_schedule,
+                                                 warping_steps, level_solver_backend)
+    flow = _run_host(params, fixed.reshape(m, n, K), moving.reshape(1, m, n, K), w, uv)
+    return flow[0].astype(np.float64)
+
+
+def get_displacement_batch(fixed, moving_frames, alpha=(2, 2), update_lag=5, iterations=50, min_level=0,
+                           levels=50, eta=0.8, a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None,
+                           weight=None, gnc_schedule=None, warping_steps=None, max_frames=None):
+    """Many moving frames (T, H, W[, K]) against one fixed frame in one device
+    pass; returns (T, H, W, 2) float32 (the dtype the executors store)."""
+    moving_frames = np.asarray(moving_frames)
+    fixed, _, w, params, m, n, K = _prepare(fixed, moving_frames[0], weight, a_data, alpha, update_lag,
+                                            iterations, min_level, levels, eta, a_smooth, const_assumption,
+                                            gnc_schedule, warping_steps, None)
+    T = moving_frames.shape[0]
+    return _run_host(params, fixed.reshape(m, n, K), moving_frames.reshape(T, m, n, K), w, uv, max_frames)
+
+
+def _run_host(params, fixed, moving, weight, uv, max_frames=None):
+    _require_cuda()
+    T, m, n, K = moving.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    plan = get_plan(params, m, n, K, T, max_frames)
+    fixed32 = np.ascontiguousarray(fixed, dtype=np.float32)
+    w32 = np.ascontiguousarray(weight, dtype=np.float32)
+    key = (fixed32.tobytes().__hash__(), w32.tobytes().__hash__())
+    fixed_t = torch.from_numpy(fixed32).to(dev)
+    w_t = torch.from_numpy(w32).to(dev)
+    plan.set_reference(fixed_t, w_t, key=key)
+    mov_t = torch.from_numpy(np.ascontiguousarray(moving, dtype=np.float32)).to(dev)
+    uv_t = None
+    if uv is not None:
+        uv_t = torch.from_numpy(np.ascontiguousarray(np.asarray(uv)[:, :, :2], dtype=np.float32)).to(dev)
+    out = plan.displacement(mov_t, uv_t)
+    torch.cuda.current_stream().synchronize()
+    return out.cpu().numpy()
+
+
+def get_displacement_device(fixed_t, moving_t, uv_t=None, weight_t=None, out_t=None, stream=None,
+                            max_frames=None, **options):
+    """Device-resident form: fixed_t (H, W, K), moving_t (T, H, W, K) and
+    optional uv_t (H, W, 2) / weight_t (H, W, K) are float32 CUDA tensors;
+    returns flow (T, H, W, 2) float32 on the device, enqueued on `stream`."""
+    _require_cuda()
+    T, H, W, K = moving_t.shape
+    params = make_params(K=K, **options)
+    plan = get_plan(params, H, W, K, T, max_frames)
+    key = ("device", fixed_t.data_ptr(), fixed_t._version,
+           None if weight_t is None else (weight_t.data_ptr(), weight_t._version))
+    plan.set_reference(fixed_t, weight_t, stream=stream, key=key)
+    return plan.displacement(moving_t, uv_t, out_t, stream=stream)
+
+
+# --------------------------------------------------------------------------
+# imregister_wrapper (core/warping.py:160-234)
+# --------------------------------------------------------------------------
+def imregister_device(frames_t, flow_t, reference_t, interpolation_method="cubic", out_t=None, stream=None):
+    """frames_t (T, H, W, K), flow_t (T, H, W, 2), reference_t (H, W, K): float32 CUDA."""
+    _require_cuda()
+    method = str(interpolation_method).lower()
+    if method not in ("cubic", "linear"):
+        raise ValueError("Unsupported interpolation method. Use 'linear' or 'cubic'.")
+    T, H, W, K = frames_t.shape
+    for t, shp in ((frames_t, (T, H, W, K)), (flow_t, (T, H, W, 2)), (reference_t, (H, W, K))):
+        Plan._check(t, shp)
+    if out_t is None:
+        out_t = torch.empty_like(frames_t)
+    lib = _lib.load()
+    _lib.check(lib.frg_imregister(T, H, W, K, _ptr(frames_t), _ptr(flow_t), _ptr(reference_t),
+                                  1 if method == "cubic" else 0, _ptr(out_t), _stream_ptr(stream)),
+               "frg_imregister")
+    return out_t
+
+
+def imregister_wrapper(f2_level, u, v, f1_level, interpolation_method="cubic"):
+    """Drop-in for pyflowreg.core.warping.imregister_wrapper (float32 result,
+    channel axis squeezed when single-channel, like the reference)."""
+    _require_cuda()
+    f2 = np.asarray(f2_level)
+    f1 = np.asarray(f1_level)
+    if f2.ndim == 2:
+        f2 = f2[:, :, None]
+        f1 = f1[:, :, None]
+    H, W, C = f2.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    fr = torch.from_numpy(np.ascontiguousarray(f2, dtype=np.float32)[None]).to(dev)
+    ref = torch.from_numpy(np.ascontiguousarray(f1, dtype=np.float32)).to(dev)
+    fl = torch.from_numpy(np.ascontiguousarray(np.stack([u, v], axis=-1), dtype=np.float32)[None]).to(dev)
+    out = imregister_device(fr, fl, ref, interpolation_method)[0].cpu().numpy()
+    return out[:, :, 0] if out.shape[2] == 1 else out
+
+
+# --------------------------------------------------------------------------
+# level_solver seam (core/optical_flow.py:348-411)
+# --------------------------------------------------------------------------
+def level_solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag, verbose, a_data,
+                 a_smooth, hx, hy, gnc_beta=None):
+    """GPU level solver with the positional signature of ``level_solver_backend``.
+
+    Runs compute_flow's exact update order on the device in float32 and
+    returns (du, dv) as float64 (m, n) arrays.
+    """
+    _require_cuda()
+    if gnc_beta is not None:
+        raise NotImplementedError("GNC stages are not implemented by the GB300 backend")
+    J = np.stack([np.asarray(a, dtype=np.float32) for a in (J11, J22, J33, J12, J13, J23)])
+    if J.ndim == 3:
+        J = J[..., None]
+    _, m, n, K = J.shape
+    wgt = np.asarray(weight, dtype=np.float32)
+    if wgt.ndim == 2:
+        wgt = wgt[..., None]
+    wgt = np.ascontiguousarray(np.broadcast_to(wgt, (m, n, K)))
+    ad = np.ascontiguousarray(normalize_a_data(a_data, K))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    Jt = torch.from_numpy(np.ascontiguousarray(J)).to(dev)
+    Wt = torch.from_numpy(wgt).to(dev)
+    ut = torch.from_numpy(np.ascontiguousarray(u, dtype=np.float32)).to(dev)
+    vt = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).to(dev)
+    du = torch.empty((m, n), dtype=torch.float32, device=dev)
+    dv = torch.empty((m, n), dtype=torch.float32, device=dev)
+    ax, ay = alpha_pair(alpha)
+    lib = _lib.load()
+    _lib.check(lib.frg_level_solve(m, n, K, _ptr(Jt), _ptr(Wt), _ptr(ut), _ptr(vt), ax, ay, int(iterations),
+                                   int(update_lag), ad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   float(a_smooth), float(hx), float(hy), 1.95, _ptr(du), _ptr(dv),
+                                   _stream_ptr()), "frg_level_solve")
+    torch.cuda.current_stream().synchronize()
+    return du.cpu().numpy().astype(np.float64), dv.cpu().numpy().astype(np.float64)
+
+
+# --------------------------------------------------------------------------
+# Building blocks with the reference's signatures
+# --------------------------------------------------------------------------
+def imresize_fused_gauss_cubic(img, size, sigma_coeff=0.6, per_axis=False):
+    """Drop-in for util/resize_util.py:232-254 (sigma_coeff 0.6, per_axis False)."""
+    _require_cuda()
+    if sigma_coeff != 0.6 or per_axis:
+        raise NotImplementedError("only sigma_coeff=0.6, per_axis=False are implemented")
+    x = np.asarray(img)
+    oh, ow = int(size[0]), int(size[1])
+    planes = x[None] if x.ndim == 2 else np.moveaxis(x, 2, 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    src = torch.from_numpy(np.ascontiguousarray(planes, dtype=np.float32)).to(dev)
+    dst = torch.empty((planes.shape[0], oh, ow), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    _lib.check(lib.frg_resize(planes.shape[0], planes.shape[1], planes.shape[2], _ptr(src), oh, ow, _ptr(dst),
+                              _stream_ptr()), "frg_resize")
+    y = dst.cpu().numpy()
+    y = y[0] if x.ndim == 2 else np.moveaxis(y, 0, 2)
+    return y.astype(x.dtype, copy=False)
+
+
+def _tensor(f1, f2, hy, hx, gray):
+    _require_cuda()
+    f1 = np.asarray(f1, dtype=np.float32)
+    f2 = np.asarray(f2, dtype=np.float32)
+    h, w = f1.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    a = torch.from_numpy(np.ascontiguousarray(f1)).to(dev)
+    b = torch.from_numpy(np.ascontiguousarray(f2)).to(dev)
+    out = torch.empty((6, h + 2, w + 2), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    _lib.check(lib.frg_motion_tensor(h, w, _ptr(a), _ptr(b), float(hy), float(hx), int(gray), _ptr(out),
+                                     _stream_ptr()), "frg_motion_tensor")
+    o = out.cpu().numpy().astype(np.float64)
+    return tuple(o[i] for i in range(6))
+
+
+def get_motion_tensor_gc(f1, f2, hy, hx):
+    return _tensor(f1, f2, hy, hx, 0)
+
+
+def get_motion_tensor_gray(f1, f2, hy, hx):
+    return _tensor(f1, f2, hy, hx, 1)
+
+
+def median_filter5(a):
+    """scipy.ndimage.median_filter(a, size=(5, 5), mode='mirror') of a 2-D array."""
+    _require_cuda()
+    a = np.asarray(a, dtype=np.float32)
+    h, w = a.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    src = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    dst = torch.empty_like(src)
+    lib = _lib.load()
+    _lib.check(lib.frg_median5(h, w, _ptr(src), _ptr(dst), _stream_ptr()), "frg_median5")
+    return dst.cpu().numpy()

@@ -1,0 +1,822 @@
+// C ABI and host orchestration of the GB300 optical-flow path.
+//
+// The plan mirrors the level loop of pyflowreg's _solve_displacement_stage
+// (src/pyflowreg/core/optical_flow.py:476-617): the pyramid schedule
+// (warpingDepth, core/warping.py:237-277), the resize tap tables
+// (util/resize_util.py:182-229) and the alpha scaling are computed on the host
+// once per plan; every level then runs a fixed sequence of kernels over the
+// whole batch of frames.
+#include "frg_internal.h"
+#include "../../include/flowreg_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace frg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define FRG_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(FRG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Host-side schedule and tables.
+// ---------------------------------------------------------------------------
+
+// warpingDepth (core/warping.py:237-277); Python round() is round-half-even.
+int warping_depth(double eta, int levels, int m, int n)
+{
+    double min_dim = std::min(m, n);
+    int depth = 0;
+    for (int i = 0; i < levels; ++i) {
+        ++depth;
+        min_dim *= eta;
+        if (std::nearbyint(min_dim) < 10) break;
+    }
+    return depth;
+}
+
+// Keys cubic with A = -0.75 (util/resize_util.py:68-76), double precision.
+double keys(double x)
+{
+    const double A = -0.75;
+    const double ax = std::fabs(x);
+    if (ax < 1.0) return (A + 2.0) * std::pow(ax, 3.0) - (A + 3.0) * ax * ax + 1.0;
+    if (ax < 2.0) return A * std::pow(ax, 3.0) - 5.0 * A * ax * ax + 8.0 * A * ax - 4.0 * A;
+    return 0.0;
+}
+
+int reflect_idx(int j, int n)
+{
+    if (n <= 1) return 0;
+    while (j < 0 || j >= n) j = j < 0 ? -j - 1 : 2 * n - 1 - j;
+    return j;
+}
+
+// numpy's float32 sum of a small contiguous array (add.reduce: first element,
+// then the pairwise block of the rest with eight partial sums).
+float np_sum_f32(const std::vector<float>& a)
+{
+    if (a.empty()) return 0.0f;
+    const float* p = a.data() + 1;
+    const long n = (long)a.size() - 1;
+    float rest = 0.0f;
+    if (n < 8) {
+        for (long i = 0; i < n; ++i) rest += p[i];
+    } else {
+        float r[8];
+        for (int j = 0; j < 8; ++j) r[j] = p[j];
+        long i = 8;
+        for (; i < n - (n % 8); i += 8)
+            for (int j = 0; j < 8; ++j) r[j] += p[i + j];
+        rest = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+        for (; i < n; ++i) rest += p[i];
+    }
+    return a[0] + rest;
+}
+
+struct HostTables {
+    int P = 0;
+    std::vector<int32_t> idx;
+    std::vector<float> wt;
+};
+
+// _precompute_fused_gauss_cubic + _fill_tables_fused_gauss_cubic_reflect
+// (util/resize_util.py:194-229) with numba's typing: float32 Gaussian taps,
+// float64 accumulation and normalisation, float32 stores.
+HostTables make_tables(int in_len, int out_len, double sigma)
+{
+    HostTables t;
+    const double scale = (double)out_len / (double)in_len;
+    int R = 0;
+    std::vector<float> g;
+    if (sigma <= 0.0) {
+        g.push_back(1.0f);
+    } else {
+        R = (int)std::ceil(2.0 * sigma);
+        const float sf = (float)sigma;
+        for (int u = -R; u <= R; ++u) {
+            volatile float q = (float)u / sf;
+            volatile float q2 = q * q;
+            volatile float e = -0.5f * q2;
+            g.push_back(std::exp(e));
+        }
+        const float s = np_sum_f32(g);
+        for (float& x : g) x = x / s;
+    }
+    t.P = 2 * R + 4;
+    t.idx.resize((size_t)out_len * t.P);
+    t.wt.resize((size_t)out_len * t.P);
+    std::vector<double> acc(t.P);
+    for (int i = 0; i < out_len; ++i) {
+        const double x = (i + 0.5) / scale - 0.5;
+        const int left = (int)std::floor(x - 2.0) - R;
+        double ssum = 0.0;
+        for (int p = 0; p < t.P; ++p) {
+            const int j = left + p;
+            t.idx[(size_t)i * t.P + p] = reflect_idx(j, in_len);
+            const double d = x - j;
+            double a = 0.0;
+            for (int u = -R; u <= R; ++u) a += (double)g[u + R] * keys(d - u);
+            t.wt[(size_t)i * t.P + p] = (float)a;
+            ssum += a;
+        }
+        const double inv = 1.0 / ssum;
+        for (int p = 0; p < t.P; ++p)
+            t.wt[(size_t)i * t.P + p] = (float)((double)t.wt[(size_t)i * t.P + p] * inv);
+    }
+    return t;
+}
+
+// sigma of imresize_fused_gauss_cubic (util/resize_util.py:235-242)
+double resize_sigma(int ih, int iw, int oh, int ow)
+{
+    const double sy = (double)oh / ih, sx = (double)ow / iw;
+    const double s = sy < sx ? sy : sx;
+    return s < 1.0 ? 0.6 / s : 0.0;
+}
+
+// cv2.remap weights at the 32 sub-pixel positions, restated from the
+// documented Keys (A = -0.75) and bilinear kernels, single precision with a
+// fixed operation order.
+void remap_tables(float* cub, float* lin)
+{
+    for (int k = 0; k < 32; ++k) {
+        volatile float t = (float)k / 32.0f;
+        const float A = -0.75f;
+        auto inner = [&](float x) {
+            volatile float a = (A + 2.0f) * x;
+            volatile float b = a - (A + 3.0f);
+            volatile float xx = x * x;
+            volatile float c = b * xx;
+            return (float)(c + 1.0f);
+        };
+        auto outer = [&](float x) {
+            volatile float a = A * x;
+            volatile float b = a - 5.0f * A;
+            volatile float c = b * x;
+            volatile float d = c + 8.0f * A;
+            volatile float e = d * x;
+            return (float)(e - 4.0f * A);
+        };
+        const float w0 = outer(1.0f + t);
+        const float w1 = inner(t);
+        const float w2 = inner(1.0f - t);
+        volatile float r = 1.0f - w0;
+        r = r - w1;
+        r = r - w2;
+        cub[k * 4 + 0] = w0;
+        cub[k * 4 + 1] = w1;
+        cub[k * 4 + 2] = w2;
+        cub[k * 4 + 3] = r;
+        lin[k * 2 + 0] = 1.0f - t;
+        lin[k * 2 + 1] = t;
+    }
+}
+
+int ensure_remap_tables()
+{
+    static bool done = false;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(FRG_ECUDA, "no CUDA device");
+    static int done_dev = -1;
+    if (done && done_dev == dev) return FRG_OK;
+    float cub[128], lin[64];
+    remap_tables(cub, lin);
+    FRG_CUDA(upload_cubic_table(cub, lin));
+    done = true;
+    done_dev = dev;
+    return FRG_OK;
+}
+
+DiagGeom make_geom(int h, int w)
+{
+    DiagGeom g;
+    g.h = h;
+    g.w = w;
+    g.D = h + w - 1;
+    g.P = (h + 31) / 32 * 32;
+    return g;
+}
+
+struct DevTables {
+    int P = 0;
+    int32_t* ix = nullptr;
+    float* wx = nullptr;
+    int32_t* iy = nullptr;
+    float* wy = nullptr;
+};
+
+struct LevelPlan {
+    int i = 0;         // pyramid index (coarsest = largest)
+    int h = 0, w = 0;  // level size
+    bool top = false;
+    double h_row = 1, h_col = 1, alpha_x = 0, alpha_y = 0;
+    float wx = 0, wy = 0;  // alpha_x / h_col^2, alpha_y / h_row^2
+    DiagGeom g{};
+    int fh = 0, fw = 0;   // flow source size (previous level; full size at the top)
+    DevTables img, flow;  // full-res -> level, flow source -> level
+    float* ref = nullptr;    // (K, h, w) reference level
+    float* wdiag = nullptr;  // (K, D*P) weight level, diagonal-major
+};
+
+// Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
+// core/level_solver.py:230), split into wavefront passes of <= kGMax.
+struct Pass {
+    int G;
+    int fold_mode;  // -1: no fold; else bit0 zero-init, bit1 psi from (du, dv)
+};
+
+std::vector<Pass> make_passes(int iterations, int update_lag)
+{
+    std::vector<Pass> out;
+    int t = 0;
+    while (t < iterations) {
+        const bool tick = ((t + 1) % update_lag) == 0;
+        int end = t + 1;
+        while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
+        int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
+        for (int s = t; s < end; s += kGMax) {
+            Pass p;
+            p.G = std::min(kGMax, end - s);
+            p.fold_mode = (s == t) ? mode : -1;
+            out.push_back(p);
+        }
+        t = end;
+    }
+    return out;
+}
+
+}  // namespace
+
+struct frg_plan {
+    frg_params p{};
+    int H = 0, W = 0, K = 0, max_T = 0;
+    int min_level = 0;
+    std::vector<LevelPlan> levels;
+    std::vector<Pass> passes;
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    bool has_ref = false;
+    // per-batch workspace
+    float* tmp = nullptr;     // horizontal resize pass
+    float* f2 = nullptr;      // (T, K, h, w)
+    float* warped = nullptr;  // (T, K, h, w)
+    float* J = nullptr;       // (T, 6, K, D*P)
+    float* lap = nullptr;     // (T, 2, D*P)
+    float* coef = nullptr;    // (T, 5, D*P)
+    float* du = nullptr;      // (T, D*P)
+    float* dv = nullptr;      // (T, D*P)
+    float* uvpad = nullptr;   // (T, 2, h+2, w+2)
+    float* uacc[2] = {nullptr, nullptr};  // (T, 2, h, w)
+    float* ones = nullptr;    // (H, W, K) default weight
+    float a_data[kMaxK] = {0};
+};
+
+namespace {
+
+template <typename T>
+int dev_alloc(frg_plan* pl, T** out, size_t count)
+{
+    void* p = nullptr;
+    const size_t b = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) return fail(FRG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    pl->allocs.push_back(p);
+    pl->bytes += b;
+    *out = (T*)p;
+    return FRG_OK;
+}
+
+int upload_tables(frg_plan* pl, const HostTables& t, int n_out_x, const HostTables& ty, int n_out_y,
+                  DevTables* d)
+{
+    (void)n_out_x;
+    (void)n_out_y;
+    d->P = t.P;
+    int rc;
+    if ((rc = dev_alloc(pl, &d->ix, t.idx.size()))) return rc;
+    if ((rc = dev_alloc(pl, &d->wx, t.wt.size()))) return rc;
+    if ((rc = dev_alloc(pl, &d->iy, ty.idx.size()))) return rc;
+    if ((rc = dev_alloc(pl, &d->wy, ty.wt.size()))) return rc;
+    FRG_CUDA(cudaMemcpy(d->ix, t.idx.data(), t.idx.size() * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d->wx, t.wt.data(), t.wt.size() * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d->iy, ty.idx.data(), ty.idx.size() * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d->wy, ty.wt.data(), ty.wt.size() * 4, cudaMemcpyHostToDevice));
+    return FRG_OK;
+}
+
+View view(const float* p, long long fs, long long ps, long long rs, long long cs)
+{
+    View v;
+    v.p = p;
+    v.fs = fs;
+    v.ps = ps;
+    v.rs = rs;
+    v.cs = cs;
+    return v;
+}
+
+ViewW vieww(float* p, long long fs, long long ps, long long rs, long long cs)
+{
+    ViewW v;
+    v.p = p;
+    v.fs = fs;
+    v.ps = ps;
+    v.rs = rs;
+    v.cs = cs;
+    return v;
+}
+
+// Runs the passes of one level: fold at ticks, wavefront SOR passes.
+int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs, const float* W,
+                long long W_fs, const float* lap, long long lap_fs, float* du, float* dv,
+                long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
+                const float* a_data, float wx, float wy, float omega, cudaStream_t st)
+{
+    for (const Pass& ps : passes) {
+        if (ps.fold_mode >= 0)
+            FRG_CUDA(launch_fold(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, T, K, g,
+                                 a_data, ps.fold_mode, wx, wy, st));
+        // thread index runs along rows: rows are the a-direction (weight wy)
+        FRG_CUDA(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+    }
+    return FRG_OK;
+}
+
+int check_params(const frg_params* p, int K)
+{
+    if (!p) return fail(FRG_EINVAL, "params is NULL");
+    if (!(p->eta > 0.0 && p->eta <= 1.0)) return fail(FRG_EINVAL, "eta must be in (0, 1]");
+    if (p->levels < 1) return fail(FRG_EINVAL, "levels must be >= 1");
+    if (p->iterations < 1) return fail(FRG_EINVAL, "iterations must be >= 1");
+    if (p->update_lag < 1) return fail(FRG_EINVAL, "update_lag must be >= 1");
+    if (p->min_level < 0) return fail(FRG_EINVAL, "min_level must be >= 0");
+    if (p->a_smooth != 1.0)
+        return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
+    if (p->const_assumption != 0 && p->const_assumption != 1)
+        return fail(FRG_EUNSUPPORTED, "only the 'gc' and 'gray' constancy assumptions are supported");
+    for (int k = 0; k < K; ++k)
+        if (!(p->a_data[k] > 0.0)) return fail(FRG_EINVAL, "a_data must be > 0");
+    return FRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int frg_version(void) { return FRG_ABI_VERSION; }
+
+const char* frg_last_error(void) { return g_last_error.c_str(); }
+
+void frg_plan_destroy(frg_plan* plan)
+{
+    if (!plan) return;
+    for (void* p : plan->allocs) cudaFree(p);
+    delete plan;
+}
+
+int frg_plan_create(const frg_params* params, int height, int width, int channels, int max_frames,
+                    frg_plan** out)
+{
+    if (!out) return fail(FRG_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (height < 2 || width < 2) return fail(FRG_EINVAL, "frame must be at least 2 x 2");
+    if (channels < 1 || channels > kMaxK) return fail(FRG_EINVAL, "channels must be in [1, 8]");
+    if (max_frames < 1 || max_frames > 65535 / channels)
+        return fail(FRG_EINVAL, "max_frames out of range");
+    int rc = check_params(params, channels);
+    if (rc) return rc;
+    if ((rc = ensure_remap_tables())) return rc;
+
+    frg_plan* pl = new frg_plan();
+    pl->p = *params;
+    pl->H = height;
+    pl->W = width;
+    pl->K = channels;
+    pl->max_T = max_frames;
+    for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
+
+    // schedule: core/optical_flow.py:494-518
+    const int m = height, n = width;
+    const double eta = params->eta;
+    int mly = warping_depth(eta, params->levels, m, m);
+    int mlx = warping_depth(eta, params->levels, n, n);
+    const int max_level = std::min(mlx, mly) * 4;
+    mly = std::min(mly, max_level);
+    mlx = std::min(mlx, max_level);
+    const int top = std::max(mlx, mly);
+    int min_level = params->min_level;
+    if (top <= min_level) min_level = top - 1;
+    if (min_level < 0) min_level = 0;
+    pl->min_level = min_level;
+    if (min_level > 0) {
+        frg_plan_destroy(pl);
+        return fail(FRG_EUNSUPPORTED, "min_level > 0 (final cubic upsampling) is not supported yet");
+    }
+    int ph = 0, pw = 0;
+    size_t max_dp = 0, max_hw = 0, max_pad = 0;
+    for (int i = top; i >= min_level; --i) {
+        LevelPlan L;
+        L.i = i;
+        L.h = (int)std::nearbyint(m * std::pow(eta, (double)std::min(i, mly)));
+        L.w = (int)std::nearbyint(n * std::pow(eta, (double)std::min(i, mlx)));
+        if (L.h < 1 || L.w < 1) {
+            frg_plan_destroy(pl);
+            return fail(FRG_EINVAL, "degenerate pyramid level");
+        }
+        if ((L.h + 31) / 32 * 32 > kMaxLane) {
+            frg_plan_destroy(pl);
+            return fail(FRG_EUNSUPPORTED, "frames taller than 512 rows are not supported yet");
+        }
+        L.top = (i == top);
+        L.h_row = (double)m / L.h;
+        L.h_col = (double)n / L.w;
+        const double sc = (i == min_level) ? 1.0 : std::pow(eta, -0.5 * i);
+        L.alpha_x = sc * params->alpha_x;
+        L.alpha_y = sc * params->alpha_y;
+        L.wx = (float)(L.alpha_x / (L.h_col * L.h_col));
+        L.wy = (float)(L.alpha_y / (L.h_row * L.h_row));
+        L.g = make_geom(L.h, L.w);
+        const double sig = resize_sigma(m, n, L.h, L.w);
+        HostTables tx = make_tables(n, L.w, sig), ty = make_tables(m, L.h, sig);
+        if ((rc = upload_tables(pl, tx, L.w, ty, L.h, &L.img))) { frg_plan_destroy(pl); return rc; }
+        L.fh = L.top ? m : ph;
+        L.fw = L.top ? n : pw;
+        const double sigf = resize_sigma(L.fh, L.fw, L.h, L.w);
+        HostTables fx = make_tables(L.fw, L.w, sigf), fy = make_tables(L.fh, L.h, sigf);
+        if ((rc = upload_tables(pl, fx, L.w, fy, L.h, &L.flow))) { frg_plan_destroy(pl); return rc; }
+        if ((rc = dev_alloc(pl, &L.ref, (size_t)channels * L.h * L.w))) { frg_plan_destroy(pl); return rc; }
+        if ((rc = dev_alloc(pl, &L.wdiag, (size_t)channels * L.g.D * L.g.P))) { frg_plan_destroy(pl); return rc; }
+        max_dp = std::max(max_dp, (size_t)L.g.D * L.g.P);
+        max_hw = std::max(max_hw, (size_t)L.h * L.w);
+        max_pad = std::max(max_pad, (size_t)(L.h + 2) * (L.w + 2));
+        ph = L.h;
+        pw = L.w;
+        pl->levels.push_back(L);
+    }
+    pl->passes = make_passes(params->iterations, params->update_lag);
+
+    const size_t T = (size_t)max_frames, K = (size_t)channels;
+    const size_t tmp_elems = T * std::max<size_t>(K, 2) * (size_t)height * width;
+    if ((rc = dev_alloc(pl, &pl->tmp, tmp_elems)) || (rc = dev_alloc(pl, &pl->f2, T * K * max_hw)) ||
+        (rc = dev_alloc(pl, &pl->warped, T * K * max_hw)) ||
+        (rc = dev_alloc(pl, &pl->J, T * 6 * K * max_dp)) || (rc = dev_alloc(pl, &pl->lap, T * 2 * max_dp)) ||
+        (rc = dev_alloc(pl, &pl->coef, T * 5 * max_dp)) || (rc = dev_alloc(pl, &pl->du, T * max_dp)) ||
+        (rc = dev_alloc(pl, &pl->dv, T * max_dp)) || (rc = dev_alloc(pl, &pl->uvpad, T * 2 * max_pad)) ||
+        (rc = dev_alloc(pl, &pl->uacc[0], T * 2 * max_hw)) || (rc = dev_alloc(pl, &pl->uacc[1], T * 2 * max_hw)) ||
+        (rc = dev_alloc(pl, &pl->ones, K * (size_t)height * width))) {
+        frg_plan_destroy(pl);
+        return rc;
+    }
+    {
+        std::vector<float> ones(K * (size_t)height * width, 1.0f / (float)channels);
+        cudaError_t e = cudaMemcpy(pl->ones, ones.data(), ones.size() * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            frg_plan_destroy(pl);
+            return fail(FRG_ECUDA, cudaGetErrorString(e));
+        }
+    }
+    *out = pl;
+    return FRG_OK;
+}
+
+size_t frg_plan_device_bytes(const frg_plan* plan) { return plan ? plan->bytes : 0; }
+
+int frg_schedule(const frg_params* params, int height, int width, int max_levels, int* h, int* w,
+                 double* alpha_x, double* alpha_y)
+{
+    if (!params || height < 2 || width < 2) return -fail(FRG_EINVAL, "bad argument");
+    const int m = height, n = width;
+    const double eta = params->eta;
+    if (!(eta > 0.0 && eta <= 1.0) || params->levels < 1) return -fail(FRG_EINVAL, "bad eta/levels");
+    int mly = warping_depth(eta, params->levels, m, m);
+    int mlx = warping_depth(eta, params->levels, n, n);
+    const int max_level = std::min(mlx, mly) * 4;
+    mly = std::min(mly, max_level);
+    mlx = std::min(mlx, max_level);
+    const int top = std::max(mlx, mly);
+    int min_level = params->min_level;
+    if (top <= min_level) min_level = top - 1;
+    if (min_level < 0) min_level = 0;
+    int count = 0;
+    for (int i = top; i >= min_level; --i, ++count) {
+        if (count >= max_levels) continue;
+        if (h) h[count] = (int)std::nearbyint(m * std::pow(eta, (double)std::min(i, mly)));
+        if (w) w[count] = (int)std::nearbyint(n * std::pow(eta, (double)std::min(i, mlx)));
+        const double sc = (i == min_level) ? 1.0 : std::pow(eta, -0.5 * i);
+        if (alpha_x) alpha_x[count] = sc * params->alpha_x;
+        if (alpha_y) alpha_y[count] = sc * params->alpha_y;
+    }
+    return count;
+}
+
+int frg_resize_tables(int in_len, int out_len, double sigma, int max_taps, int* idx, float* wt)
+{
+    if (in_len < 1 || out_len < 1) return -fail(FRG_EINVAL, "bad length");
+    HostTables t = make_tables(in_len, out_len, sigma);
+    if (t.P > max_taps) return t.P;
+    if (idx) for (size_t i = 0; i < t.idx.size(); ++i) idx[i] = t.idx[i];
+    if (wt) for (size_t i = 0; i < t.wt.size(); ++i) wt[i] = t.wt[i];
+    return t.P;
+}
+
+int frg_iteration_passes(int iterations, int update_lag, int max_passes, int* G, int* fold_mode)
+{
+    if (iterations < 1 || update_lag < 1) return -fail(FRG_EINVAL, "bad iterations/update_lag");
+    std::vector<Pass> ps = make_passes(iterations, update_lag);
+    for (size_t i = 0; i < ps.size() && (int)i < max_passes; ++i) {
+        if (G) G[i] = ps[i].G;
+        if (fold_mode) fold_mode[i] = ps[i].fold_mode;
+    }
+    return (int)ps.size();
+}
+
+int frg_plan_num_levels(const frg_plan* plan) { return plan ? (int)plan->levels.size() : 0; }
+
+int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double* alpha_x, double* alpha_y)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    const LevelPlan& L = plan->levels[level];
+    if (h) *h = L.h;
+    if (w) *w = L.w;
+    if (alpha_x) *alpha_x = L.alpha_x;
+    if (alpha_y) *alpha_y = L.alpha_y;
+    return FRG_OK;
+}
+
+int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, void* stream)
+{
+    if (!pl || !fixed) return fail(FRG_EINVAL, "plan or fixed is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int H = pl->H, W = pl->W, K = pl->K;
+    const float* wsrc = weight ? weight : pl->ones;
+    for (LevelPlan& L : pl->levels) {
+        // reference level: resize(fixed) (core/optical_flow.py:519)
+        View src = view(fixed, 0, 1, (long long)W * K, K);
+        FRG_CUDA(launch_resize_h(src, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
+        FRG_CUDA(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(L.ref, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
+                                 L.img.iy, L.img.wy, L.img.P, st));
+        // weight level: resize(weight) (core/optical_flow.py:565-570), diagonal-major
+        View wv = view(wsrc, 0, 1, (long long)W * K, K);
+        FRG_CUDA(launch_resize_h(wv, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
+        FRG_CUDA(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(pl->f2, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
+                                 L.img.iy, L.img.wy, L.img.P, st));
+        FRG_CUDA(launch_to_diag(view(pl->f2, 0, (long long)L.h * L.w, L.w, 1), 1, K, L.h, L.w, L.wdiag, 0, L.g,
+                                st));
+    }
+    pl->has_ref = true;
+    return FRG_OK;
+}
+
+int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* uv_init, float* flow_out,
+                         void* stream)
+{
+    if (!pl || !moving || !flow_out) return fail(FRG_EINVAL, "NULL argument");
+    if (!pl->has_ref) return fail(FRG_EINVAL, "frg_set_reference has not been called");
+    if (T < 1 || T > pl->max_T) return fail(FRG_EINVAL, "n_frames out of range for this plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int H = pl->H, W = pl->W, K = pl->K;
+    const long long fsz = (long long)H * W * K;
+    int cur = 0;
+    const LevelPlan* prev = nullptr;
+    for (size_t li = 0; li < pl->levels.size(); ++li) {
+        const LevelPlan& L = pl->levels[li];
+        const int h = L.h, w = L.w;
+        const long long hw = (long long)h * w, pad = (long long)(h + 2) * (w + 2);
+        const long long dp = (long long)L.g.D * L.g.P;
+        // 1. moving level images from full resolution (core/optical_flow.py:520)
+        FRG_CUDA(launch_resize_h(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->tmp, w, L.img.ix,
+                                 L.img.wx, L.img.P, st));
+        FRG_CUDA(launch_resize_v(pl->tmp, T, K, H, w, vieww(pl->f2, K * hw, hw, w, 1), h, 0, L.img.iy, L.img.wy,
+                                 L.img.P, st));
+        // 2. flow at this level with an edge ring (core/optical_flow.py:530-536)
+        long long uv_fs;
+        if (L.top) {
+            uv_fs = 0;  // one field shared by every frame
+            if (uv_init) {
+                FRG_CUDA(launch_resize_h(view(uv_init, 0, 1, (long long)W * 2, 2), 1, 2, H, W, pl->tmp, w,
+                                         L.flow.ix, L.flow.wx, L.flow.P, st));
+                FRG_CUDA(launch_resize_v(pl->tmp, 1, 2, H, w, vieww(pl->uvpad, 0, pad, w + 2, 1), h, 1, L.flow.iy,
+                                         L.flow.wy, L.flow.P, st));
+            } else {
+                FRG_CUDA(cudaMemsetAsync(pl->uvpad, 0, sizeof(float) * 2 * pad, st));
+            }
+        } else {
+            uv_fs = 2 * pad;
+            const long long phw = (long long)prev->h * prev->w;
+            FRG_CUDA(launch_resize_h(view(pl->uacc[cur], 2 * phw, phw, prev->w, 1), T, 2, prev->h, prev->w,
+                                     pl->tmp, w, L.flow.ix, L.flow.wx, L.flow.P, st));
+            FRG_CUDA(launch_resize_v(pl->tmp, T, 2, prev->h, w, vieww(pl->uvpad, 2 * pad, pad, w + 2, 1), h, 1,
+                                     L.flow.iy, L.flow.wy, L.flow.P, st));
+        }
+        View up = view(pl->uvpad, uv_fs, 0, w + 2, 1);
+        View vp = view(pl->uvpad + pad, uv_fs, 0, w + 2, 1);
+        View f1v = view(L.ref, 0, hw, w, 1);
+        View f2v = view(pl->f2, K * hw, hw, w, 1);
+        // 3. warp of the moving level by the current flow (core/optical_flow.py:537-542)
+        View img2 = f2v;
+        if (!L.top) {
+            View ui = view(pl->uvpad + (w + 2) + 1, uv_fs, 0, w + 2, 1);
+            View vi = view(pl->uvpad + pad + (w + 2) + 1, uv_fs, 0, w + 2, 1);
+            FRG_CUDA(launch_warp(f2v, f1v, ui, vi, T, K, h, w, (float)L.h_col, (float)L.h_row, 1,
+                                 vieww(pl->warped, K * hw, hw, w, 1), st));
+            img2 = view(pl->warped, K * hw, hw, w, 1);
+        }
+        // 4. motion tensor and smoothness constants (core/optical_flow.py:547-563)
+        const long long J_fs = 6LL * K * dp;
+        FRG_CUDA(launch_tensor(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
+                               pl->J, J_fs, L.g, st));
+        FRG_CUDA(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
+        // 5. level solve (core/optical_flow.py:584-606)
+        int rc = solve_level(pl->passes, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du, pl->dv, dp, pl->coef,
+                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st);
+        if (rc) return rc;
+        // 6. median + accumulate (core/optical_flow.py:607-611)
+        const int do_median = std::min(h, w) > 5 ? 1 : 0;
+        const bool last = (li + 1 == pl->levels.size());
+        ViewW ou, ov;
+        if (last) {
+            ou = vieww(flow_out, (long long)H * W * 2, 0, (long long)W * 2, 2);
+            ov = vieww(flow_out + 1, (long long)H * W * 2, 0, (long long)W * 2, 2);
+        } else {
+            const int nxt = cur ^ 1;
+            ou = vieww(pl->uacc[nxt], 2 * hw, 0, w, 1);
+            ov = vieww(pl->uacc[nxt] + hw, 2 * hw, 0, w, 1);
+            cur = nxt;
+        }
+        FRG_CUDA(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
+        prev = &L;
+    }
+    return FRG_OK;
+}
+
+int frg_imregister(int n_frames, int height, int width, int channels, const float* frames, const float* flow,
+                   const float* reference, int cubic, float* out, void* stream)
+{
+    if (!frames || !flow || !reference || !out) return fail(FRG_EINVAL, "NULL argument");
+    if (n_frames < 1 || n_frames > 65535 || height < 1 || width < 1 || channels < 1)
+        return fail(FRG_EINVAL, "bad shape");
+    int rc = ensure_remap_tables();
+    if (rc) return rc;
+    const long long H = height, W = width, K = channels;
+    View f2 = view(frames, H * W * K, 1, W * K, K);
+    View f1 = view(reference, 0, 1, W * K, K);
+    View u = view(flow, H * W * 2, 0, W * 2, 2);
+    View v = view(flow + 1, H * W * 2, 0, W * 2, 2);
+    ViewW o = vieww(out, H * W * K, 1, W * K, K);
+    FRG_CUDA(launch_warp(f2, f1, u, v, n_frames, channels, height, width, 1.0f, 1.0f, cubic ? 1 : 0, o,
+                         (cudaStream_t)stream));
+    return FRG_OK;
+}
+
+int frg_level_solve(int m, int n, int K, const float* J, const float* weight, const float* u, const float* v,
+                    double alpha_x, double alpha_y, int iterations, int update_lag, const double* a_data,
+                    double a_smooth, double hx, double hy, double omega, float* du, float* dv, void* stream)
+{
+    if (!J || !weight || !u || !v || !a_data || !du || !dv) return fail(FRG_EINVAL, "NULL argument");
+    if (m < 3 || n < 3 || K < 1 || K > kMaxK) return fail(FRG_EINVAL, "bad shape");
+    if (iterations < 1 || update_lag < 1) return fail(FRG_EINVAL, "iterations and update_lag must be >= 1");
+    if (a_smooth != 1.0) return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
+    const int h = m - 2, w = n - 2;
+    DiagGeom g = make_geom(h, w);
+    if (g.P > kMaxLane) return fail(FRG_EUNSUPPORTED, "levels taller than 512 rows are not supported yet");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long dp = (long long)g.D * g.P;
+    const long long mn = (long long)m * n;
+    float* scratch = nullptr;
+    const size_t elems = (size_t)(6 * K + K + 2 + 5 + 2) * dp;
+    FRG_CUDA(cudaMallocAsync((void**)&scratch, elems * sizeof(float), st));
+    float* Jd = scratch;
+    float* Wd = Jd + 6LL * K * dp;
+    float* lap = Wd + (long long)K * dp;
+    float* coef = lap + 2 * dp;
+    float* dud = coef + 5 * dp;
+    float* dvd = dud + dp;
+    int rc = FRG_OK;
+    float ad[kMaxK];
+    for (int k = 0; k < K; ++k) ad[k] = (float)a_data[k];
+    const float wx = (float)(alpha_x / (hx * hx)), wy = (float)(alpha_y / (hy * hy));
+    auto run = [&]() -> int {
+        // J arrays (m, n, K) channel-last; interior starts at (1, 1)
+        for (int q = 0; q < 6; ++q)
+            FRG_CUDA(launch_to_diag(view(J + q * mn * K + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K,
+                                    h, w, Jd + q * K * dp, 0, g, st));
+        FRG_CUDA(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd,
+                                0, g, st));
+        FRG_CUDA(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
+        std::vector<Pass> passes = make_passes(iterations, update_lag);
+        int r = solve_level(passes, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy, (float)omega,
+                            st);
+        if (r) return r;
+        FRG_CUDA(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
+        FRG_CUDA(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
+        return FRG_OK;
+    };
+    rc = run();
+    cudaError_t e = cudaFreeAsync(scratch, st);
+    if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
+    return rc;
+}
+
+int frg_resize(int n_planes, int ih, int iw, const float* src, int oh, int ow, float* dst, void* stream)
+{
+    if (!src || !dst || n_planes < 1 || ih < 1 || iw < 1 || oh < 1 || ow < 1) return fail(FRG_EINVAL, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double sig = resize_sigma(ih, iw, oh, ow);
+    HostTables tx = make_tables(iw, ow, sig), ty = make_tables(ih, oh, sig);
+    const size_t tb = (tx.idx.size() + tx.wt.size() + ty.idx.size() + ty.wt.size()) * 4;
+    const size_t tmpb = (size_t)n_planes * ih * ow * 4;
+    char* buf = nullptr;
+    FRG_CUDA(cudaMallocAsync((void**)&buf, tb + tmpb, st));
+    int32_t* ix = (int32_t*)buf;
+    float* wx = (float*)(ix + tx.idx.size());
+    int32_t* iy = (int32_t*)(wx + tx.wt.size());
+    float* wy = (float*)(iy + ty.idx.size());
+    float* tmp = wy + ty.wt.size();
+    auto run = [&]() -> int {
+        FRG_CUDA(cudaMemcpyAsync(ix, tx.idx.data(), tx.idx.size() * 4, cudaMemcpyHostToDevice, st));
+        FRG_CUDA(cudaMemcpyAsync(wx, tx.wt.data(), tx.wt.size() * 4, cudaMemcpyHostToDevice, st));
+        FRG_CUDA(cudaMemcpyAsync(iy, ty.idx.data(), ty.idx.size() * 4, cudaMemcpyHostToDevice, st));
+        FRG_CUDA(cudaMemcpyAsync(wy, ty.wt.data(), ty.wt.size() * 4, cudaMemcpyHostToDevice, st));
+        FRG_CUDA(launch_resize_h(view(src, 0, (long long)ih * iw, iw, 1), 1, n_planes, ih, iw, tmp, ow, ix, wx, tx.P,
+                                 st));
+        FRG_CUDA(launch_resize_v(tmp, 1, n_planes, ih, ow, vieww(dst, 0, (long long)oh * ow, ow, 1), oh, 0, iy, wy,
+                                 ty.P, st));
+        // the host vectors must outlive the asynchronous copies
+        FRG_CUDA(cudaStreamSynchronize(st));
+        return FRG_OK;
+    };
+    int rc = run();
+    cudaError_t e = cudaFreeAsync(buf, st);
+    if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
+    return rc;
+}
+
+int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy, double hx, int gray, float* out,
+                      void* stream)
+{
+    if (!f1 || !f2 || !out || h < 1 || w < 1) return fail(FRG_EINVAL, "bad argument");
+    if (h > 4096 || w > 4096) return fail(FRG_EINVAL, "plane too large");
+    cudaStream_t st = (cudaStream_t)stream;
+    DiagGeom g = make_geom(h, w);
+    const long long dp = (long long)g.D * g.P;
+    float* Jd = nullptr;
+    FRG_CUDA(cudaMallocAsync((void**)&Jd, 6 * dp * sizeof(float), st));
+    auto run = [&]() -> int {
+        FRG_CUDA(launch_tensor(view(f1, 0, 0, w, 1), view(f2, 0, 0, w, 1), 1, 1, h, w, (float)hy, (float)hx,
+                               gray ? 1 : 0, Jd, 0, g, st));
+        const long long pad = (long long)(h + 2) * (w + 2);
+        FRG_CUDA(launch_from_diag(Jd, 0, 1, 6, g, vieww(out, 0, pad, w + 2, 1), 1, 1, st));
+        return FRG_OK;
+    };
+    int rc = run();
+    cudaError_t e = cudaFreeAsync(Jd, st);
+    if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
+    return rc;
+}
+
+int frg_median5(int h, int w, const float* src, float* dst, void* stream)
+{
+    if (!src || !dst || h < 3 || w < 3) return fail(FRG_EINVAL, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    DiagGeom g = make_geom(h, w);
+    const long long dp = (long long)g.D * g.P;
+    const long long pad = (long long)(h + 2) * (w + 2);
+    float* buf = nullptr;
+    FRG_CUDA(cudaMallocAsync((void**)&buf, (2 * dp + pad) * sizeof(float), st));
+    float* d1 = buf;
+    float* zeros = buf + 2 * dp;
+    auto run = [&]() -> int {
+        FRG_CUDA(cudaMemsetAsync(zeros, 0, pad * sizeof(float), st));
+        FRG_CUDA(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1, 0, g, st));
+        FRG_CUDA(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1 + dp, 0, g, st));
+        View z = view(zeros, 0, 0, w + 2, 1);
+        // the v output duplicates u; write it to the same destination
+        FRG_CUDA(launch_median_accum(d1, d1 + dp, 0, z, z, 1, g, 1, vieww(dst, 0, 0, w, 1),
+                                     vieww(dst, 0, 0, w, 1), st));
+        return FRG_OK;
+    };
+    int rc = run();
+    cudaError_t e = cudaFreeAsync(buf, st);
+    if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// Internal declarations shared by the CUDA kernels and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace frg {
+
+constexpr int kMaxK = 8;        // channels per frame handled by one plan
+constexpr int kGMax = 5;        // SOR iterations pipelined per wavefront pass
+constexpr int kMaxLane = 512;   // longest diagonal (rows of the level) per CTA
+constexpr int kRing = 2 * kGMax + 2;
+constexpr int kPrefetch = 4;    // diagonals loaded ahead into registers
+
+// 2-D strided view of a stack of planes: element (frame, plane, y, x) at
+// base + frame*fs + plane*ps + y*rs + x*cs (all in elements).
+struct View {
+    const float* p;
+    long long fs, ps, rs, cs;
+};
+struct ViewW {
+    float* p;
+    long long fs, ps, rs, cs;
+};
+
+// Diagonal-major layout of an h x w level interior: pixel (r, c) lives at
+// (r + c) * P + r, P = h rounded up to 32.  One diagonal is contiguous, so a
+// warp reading consecutive rows of one diagonal issues one 128-byte access.
+struct DiagGeom {
+    int h, w, D, P;
+};
+
+__host__ __device__ inline long long diag_index(const DiagGeom& g, int r, int c)
+{
+    return (long long)(r + c) * g.P + r;
+}
+
+// Kernel launchers (frg_kernels.cu).  All enqueue on `st` and return the
+// launch status; none synchronises.
+cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
+                            const int32_t* ix, const float* wx, int P, cudaStream_t st);
+cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih, int ow, ViewW dst,
+                            int oh, int pad, const int32_t* iy, const float* wy, int P, cudaStream_t st);
+cudaError_t launch_warp(View f2, View f1, View u, View v, int n_frames, int K, int h, int w,
+                        float h_col, float h_row, int cubic, ViewW out, cudaStream_t st);
+cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
+                          int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st);
+cudaError_t launch_lap(View u, View v, int n_frames, int h, int w, float wx, float wy, float* lap,
+                       long long lap_fs, DiagGeom g, cudaStream_t st);
+cudaError_t launch_to_diag(View src, int n_frames, int n_planes, int h, int w, float* dst,
+                           long long dst_fs, DiagGeom g, cudaStream_t st);
+cudaError_t launch_from_diag(const float* src, long long src_fs, int n_frames, int n_planes, DiagGeom g,
+                             ViewW dst, int ring, int ring_mode, cudaStream_t st);
+cudaError_t launch_fold(const float* J, long long J_fs, const float* W, long long W_fs,
+                        const float* lap, long long lap_fs, float* du, float* dv,
+                        long long st_fs, float* coef, long long coef_fs, int n_frames, int K,
+                        DiagGeom g, const float* a_data, int mode, float wx, float wy,
+                        cudaStream_t st);
+cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                       int n_frames, DiagGeom g, int G, float wa, float wb, float omega,
+                       cudaStream_t st);
+cudaError_t launch_median_accum(const float* du, const float* dv, long long st_fs, View u, View v,
+                                int n_frames, DiagGeom g, int do_median, ViewW out_u, ViewW out_v,
+                                cudaStream_t st);
+cudaError_t upload_cubic_table(const float* tab128, const float* lin64);
+
+}  // namespace frg

@@ -1,0 +1,621 @@
+// CUDA kernels of the GB300 optical-flow path (sm_103a, FP32, no tensor cores).
+//
+// Every kernel follows one step of pyflowreg's get_displacement
+// (src/pyflowreg/core/optical_flow.py:476-617); the reference line each one
+// restates is given above it.  All kernels are bounded loops without
+// inter-CTA waits, so none of them can hang.
+#include "frg_internal.h"
+
+#include <math.h>
+
+namespace frg {
+
+__constant__ float c_cubic[32 * 4];
+__constant__ float c_linear[32 * 2];
+
+cudaError_t upload_cubic_table(const float* tab128, const float* lin64)
+{
+    cudaError_t e = cudaMemcpyToSymbol(c_cubic, tab128, sizeof(float) * 128);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_linear, lin64, sizeof(float) * 64);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// ---------------------------------------------------------------------------
+// Separable fused Gauss-cubic resize (util/resize_util.py:116-141, 232-254).
+// Horizontal pass: dst[(f*n_planes + plane), y, x] = sum_p src[y, ix[x,p]] * wx[x,p]
+// ---------------------------------------------------------------------------
+__global__ void k_resize_h(View src, int n_planes, int ih, int iw, float* __restrict__ dst, int ow,
+                           const int32_t* __restrict__ ix, const float* __restrict__ wx, int P)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int fp = blockIdx.z;
+    if (x >= ow) return;
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    const float* row = src.p + f * src.fs + pl * src.ps + (long long)y * src.rs;
+    const int32_t* ixr = ix + (long long)x * P;
+    const float* wxr = wx + (long long)x * P;
+    float s = 0.0f;
+    for (int p = 0; p < P; ++p) s = fmaf(__ldg(row + (long long)ixr[p] * src.cs), wxr[p], s);
+    dst[((long long)fp * ih + y) * ow + x] = s;
+    (void)iw;
+}
+
+// Vertical pass; with pad = 1 the output is the level array with a one-pixel
+// edge-replicated ring (add_boundary, core/optical_flow.py:48-70).
+__global__ void k_resize_v(const float* __restrict__ src, int n_planes, int ih, int ow, ViewW dst, int oh,
+                           int pad, const int32_t* __restrict__ iy, const float* __restrict__ wy, int P)
+{
+    const int xo = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yo = blockIdx.y;
+    const int fp = blockIdx.z;
+    if (xo >= ow + 2 * pad) return;
+    const int x = clampi(xo - pad, 0, ow - 1);
+    const int y = clampi(yo - pad, 0, oh - 1);
+    const float* col = src + (long long)fp * ih * ow + x;
+    const int32_t* iyr = iy + (long long)y * P;
+    const float* wyr = wy + (long long)y * P;
+    float s = 0.0f;
+    for (int p = 0; p < P; ++p) s = fmaf(__ldg(col + (long long)iyr[p] * ow), wyr[p], s);
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    dst.p[f * dst.fs + pl * dst.ps + (long long)yo * dst.rs + (long long)xo * dst.cs] = s;
+}
+
+cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
+                            const int32_t* ix, const float* wx, int P, cudaStream_t st)
+{
+    dim3 blk(128), grd((ow + 127) / 128, ih, n_frames * n_planes);
+    k_resize_h<<<grd, blk, 0, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih, int ow, ViewW dst,
+                            int oh, int pad, const int32_t* iy, const float* wy, int P, cudaStream_t st)
+{
+    dim3 blk(128), grd((ow + 2 * pad + 127) / 128, oh + 2 * pad, n_frames * n_planes);
+    k_resize_v<<<grd, blk, 0, st>>>(src, n_planes, ih, ow, dst, oh, pad, iy, wy, P);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Backward warp with out-of-bounds fill (core/warping.py:160-234): the map is
+// x + u / h_col, y + v / h_row in float32; points outside [0, W) x [0, H)
+// take the reference level value; the rest is clamped and sampled on the
+// 1/32-pixel grid of cv2.remap (round half to even) with Keys A = -0.75
+// bicubic or bilinear weights and replicated borders.
+// ---------------------------------------------------------------------------
+__global__ void k_warp(View f2, View f1, View u, View v, int K, int h, int w, float h_col, float h_row,
+                       int cubic, ViewW out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const float uu = u.p[f * u.fs + (long long)y * u.rs + (long long)x * u.cs];
+    const float vv = v.p[f * v.fs + (long long)y * v.rs + (long long)x * v.cs];
+    const float mx = __fadd_rn((float)x, __fdiv_rn(uu, h_col));
+    const float my = __fadd_rn((float)y, __fdiv_rn(vv, h_row));
+    const bool oob = (mx < 0.0f) || (mx >= (float)w) || (my < 0.0f) || (my >= (float)h);
+    if (oob) {
+        for (int k = 0; k < K; ++k)
+            out.p[f * out.fs + k * out.ps + (long long)y * out.rs + (long long)x * out.cs] =
+                f1.p[f * f1.fs + k * f1.ps + (long long)y * f1.rs + (long long)x * f1.cs];
+        return;
+    }
+    const float cx = fminf(fmaxf(mx, 0.0f), (float)(w - 1));
+    const float cy = fminf(fmaxf(my, 0.0f), (float)(h - 1));
+    const int X = __float2int_rn(cx * 32.0f);
+    const int Y = __float2int_rn(cy * 32.0f);
+    const int ix = X >> 5, fx = X & 31;
+    const int iy = Y >> 5, fy = Y & 31;
+    for (int k = 0; k < K; ++k) {
+        const float* src = f2.p + f * f2.fs + k * f2.ps;
+        float acc = 0.0f;
+        if (cubic) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float* row = src + (long long)clampi(iy - 1 + i, 0, h - 1) * f2.rs;
+                const float wyi = c_cubic[fy * 4 + i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float w2 = __fmul_rn(wyi, c_cubic[fx * 4 + j]);
+                    acc = fmaf(row[(long long)clampi(ix - 1 + j, 0, w - 1) * f2.cs], w2, acc);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const float* row = src + (long long)clampi(iy + i, 0, h - 1) * f2.rs;
+                const float wyi = c_linear[fy * 2 + i];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const float w2 = __fmul_rn(wyi, c_linear[fx * 2 + j]);
+                    acc = fmaf(row[(long long)clampi(ix + j, 0, w - 1) * f2.cs], w2, acc);
+                }
+            }
+        }
+        out.p[f * out.fs + k * out.ps + (long long)y * out.rs + (long long)x * out.cs] = acc;
+    }
+}
+
+cudaError_t launch_warp(View f2, View f1, View u, View v, int n_frames, int K, int h, int w,
+                        float h_col, float h_row, int cubic, ViewW out, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    k_warp<<<grd, blk, 0, st>>>(f2, f1, u, v, K, h, w, h_col, h_row, cubic, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Motion tensor (core/optical_flow.py:73-160 gradient constancy, 163-228
+// gray-value constancy).  Derivatives use the reference's one-pixel symmetric
+// padding: every neighbour index is clamped into the level.  Output is
+// diagonal-major, per frame [6][K][D*P] in the order J11, J22, J33, J12, J13, J23.
+// ---------------------------------------------------------------------------
+__global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float hx, int gray,
+                         float* __restrict__ J, long long J_fs, DiagGeom g)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const int xm = max(x - 1, 0), xp = min(x + 1, w - 1);
+    const int ym = max(y - 1, 0), yp = min(y + 1, h - 1);
+    const long long di = diag_index(g, y, x);
+    const long long plane = (long long)g.D * g.P;
+    float* Jf = J + f * J_fs;
+    const float h2x = 2.0f * hx, h2y = 2.0f * hy;
+    const float hxx = hx * hx, hyy = hy * hy;
+    for (int k = 0; k < K; ++k) {
+        const float* a = f1.p + f * f1.fs + k * f1.ps;
+        const float* b = f2.p + f * f2.fs + k * f2.ps;
+#define A_(r, c) a[(long long)(r) * f1.rs + (long long)(c) * f1.cs]
+#define B_(r, c) b[(long long)(r) * f2.rs + (long long)(c) * f2.cs]
+        float j11, j22, j33, j12, j13, j23;
+        if (gray) {
+            const float fxv = 0.5f * ((A_(y, xp) - A_(y, xm)) / h2x + (B_(y, xp) - B_(y, xm)) / h2x);
+            const float fyv = 0.5f * ((A_(yp, x) - A_(ym, x)) / h2y + (B_(yp, x) - B_(ym, x)) / h2y);
+            const float ftv = B_(y, x) - A_(y, x);
+            j11 = fxv * fxv; j22 = fyv * fyv; j33 = ftv * ftv;
+            j12 = fxv * fyv; j13 = fxv * ftv; j23 = fyv * ftv;
+        } else {
+            const float fx_m = 0.5f * ((A_(ym, xp) - A_(ym, xm)) / h2x + (B_(ym, xp) - B_(ym, xm)) / h2x);
+            const float fx_p = 0.5f * ((A_(yp, xp) - A_(yp, xm)) / h2x + (B_(yp, xp) - B_(yp, xm)) / h2x);
+            const float fxy = (fx_p - fx_m) / h2y;
+            const float ft_l = B_(y, xm) - A_(y, xm), ft_r = B_(y, xp) - A_(y, xp);
+            const float ft_u = B_(ym, x) - A_(ym, x), ft_d = B_(yp, x) - A_(yp, x);
+            const float fxt = (ft_r - ft_l) / h2x;
+            const float fyt = (ft_d - ft_u) / h2y;
+            const float a0 = A_(y, x), b0 = B_(y, x);
+            const float fxx = 0.5f * (((A_(y, xm) - a0) + (A_(y, xp) - a0)) / hxx +
+                                      ((B_(y, xm) - b0) + (B_(y, xp) - b0)) / hxx);
+            const float fyy = 0.5f * (((A_(ym, x) - a0) + (A_(yp, x) - a0)) / hyy +
+                                      ((B_(ym, x) - b0) + (B_(yp, x) - b0)) / hyy);
+            const float reg_x = 1.0f / (fxx * fxx + fxy * fxy + 1e-6f);
+            const float reg_y = 1.0f / (fxy * fxy + fyy * fyy + 1e-6f);
+            j11 = reg_x * fxx * fxx + reg_y * fxy * fxy;
+            j22 = reg_x * fxy * fxy + reg_y * fyy * fyy;
+            j33 = reg_x * fxt * fxt + reg_y * fyt * fyt;
+            j12 = reg_x * fxx * fxy + reg_y * fxy * fyy;
+            j13 = reg_x * fxx * fxt + reg_y * fxy * fyt;
+            j23 = reg_x * fxy * fxt + reg_y * fyy * fyt;
+        }
+#undef A_
+#undef B_
+        const long long kb = (long long)k * plane + di;
+        const long long qs = (long long)K * plane;
+        Jf[0 * qs + kb] = j11;
+        Jf[1 * qs + kb] = j22;
+        Jf[2 * qs + kb] = j33;
+        Jf[3 * qs + kb] = j12;
+        Jf[4 * qs + kb] = j13;
+        Jf[5 * qs + kb] = j23;
+    }
+}
+
+cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
+                          int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    k_tensor<<<grd, blk, 0, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Constant part of the smoothness numerator for a level (u, v fixed during
+// the solve; core/level_solver.py:317-340):
+//   lap_u = wx*((uL-uc)+(uR-uc)) + wy*((uU-uc)+(uD-uc)), lap_v likewise,
+// from the edge-padded (h+2) x (w+2) u, v; diagonal-major output [2][D*P].
+// ---------------------------------------------------------------------------
+__global__ void k_lap(View u, View v, int h, int w, float wx, float wy, float* __restrict__ lap,
+                      long long lap_fs, DiagGeom g)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const float* up = u.p + f * u.fs;
+    const float* vp = v.p + f * v.fs;
+#define U_(r, c) up[(long long)(r) * u.rs + (long long)(c) * u.cs]
+#define V_(r, c) vp[(long long)(r) * v.rs + (long long)(c) * v.cs]
+    const float uc = U_(y + 1, x + 1), vc = V_(y + 1, x + 1);
+    const float lu = wx * ((U_(y + 1, x) - uc) + (U_(y + 1, x + 2) - uc)) +
+                     wy * ((U_(y, x + 1) - uc) + (U_(y + 2, x + 1) - uc));
+    const float lv = wx * ((V_(y + 1, x) - vc) + (V_(y + 1, x + 2) - vc)) +
+                     wy * ((V_(y, x + 1) - vc) + (V_(y + 2, x + 1) - vc));
+#undef U_
+#undef V_
+    const long long di = diag_index(g, y, x);
+    const long long plane = (long long)g.D * g.P;
+    lap[f * lap_fs + di] = lu;
+    lap[f * lap_fs + plane + di] = lv;
+    (void)h;
+}
+
+cudaError_t launch_lap(View u, View v, int n_frames, int h, int w, float wx, float wy, float* lap,
+                       long long lap_fs, DiagGeom g, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    k_lap<<<grd, blk, 0, st>>>(u, v, h, w, wx, wy, lap, lap_fs, g);
+    return cudaGetLastError();
+}
+
+// Row-major planes -> diagonal-major planes: dst[f][plane][D*P].
+__global__ void k_to_diag(View src, int n_planes, int h, int w, float* __restrict__ dst,
+                          long long dst_fs, DiagGeom g)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int fp = blockIdx.z;
+    if (x >= w) return;
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    const float val = src.p[f * src.fs + pl * src.ps + (long long)y * src.rs + (long long)x * src.cs];
+    dst[f * dst_fs + (long long)pl * g.D * g.P + diag_index(g, y, x)] = val;
+    (void)h;
+}
+
+cudaError_t launch_to_diag(View src, int n_frames, int n_planes, int h, int w, float* dst,
+                           long long dst_fs, DiagGeom g, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames * n_planes);
+    k_to_diag<<<grd, blk, 0, st>>>(src, n_planes, h, w, dst, dst_fs, g);
+    return cudaGetLastError();
+}
+
+// Diagonal-major planes -> row-major planes with a `ring`-pixel border:
+// ring_mode 0 leaves the border untouched, 1 zeroes it, 2 copies the nearest
+// interior value (the Neumann copy of set_boundary_2d).
+__global__ void k_from_diag(const float* __restrict__ src, long long src_fs, int n_planes, DiagGeom g,
+                            ViewW dst, int ring, int ring_mode)
+{
+    const int xo = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yo = blockIdx.y;
+    const int fp = blockIdx.z;
+    const int W2 = g.w + 2 * ring, H2 = g.h + 2 * ring;
+    if (xo >= W2) return;
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    const int x = xo - ring, y = yo - ring;
+    const bool inside = x >= 0 && x < g.w && y >= 0 && y < g.h;
+    if (!inside && ring_mode == 0) return;
+    float val = 0.0f;
+    if (inside || ring_mode == 2) {
+        const int xc = clampi(x, 0, g.w - 1), yc = clampi(y, 0, g.h - 1);
+        val = src[f * src_fs + (long long)pl * g.D * g.P + diag_index(g, yc, xc)];
+    }
+    dst.p[f * dst.fs + pl * dst.ps + (long long)yo * dst.rs + (long long)xo * dst.cs] = val;
+    (void)H2;
+}
+
+cudaError_t launch_from_diag(const float* src, long long src_fs, int n_frames, int n_planes, DiagGeom g,
+                             ViewW dst, int ring, int ring_mode, cudaStream_t st)
+{
+    dim3 blk(128), grd((g.w + 2 * ring + 127) / 128, g.h + 2 * ring, n_frames * n_planes);
+    k_from_diag<<<grd, blk, 0, st>>>(src, src_fs, n_planes, g, dst, ring, ring_mode);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Coefficient fold at a lagged-nonlinearity tick (core/level_solver.py:229-255,
+// 342-364).  mode 0: first group, psi = 1 and du = dv = 0; mode 1: psi from the
+// current (du, dv).  Writes, per pixel, the five coefficients the SOR update
+// needs: A12 = sum_k W psi J12, BU = lap_u - sum_k W psi J13,
+// BV = lap_v - sum_k W psi J23, 1/den_u, 1/den_v (0 where the denominator is 0).
+// ---------------------------------------------------------------------------
+struct AData { float a[kMaxK]; };
+
+__global__ void k_fold(const float* __restrict__ J, long long J_fs, const float* __restrict__ W,
+                       long long W_fs, const float* __restrict__ lap, long long lap_fs,
+                       float* __restrict__ du, float* __restrict__ dv, long long st_fs,
+                       float* __restrict__ coef, long long coef_fs, int K, DiagGeom g, AData ad,
+                       int mode, float wx, float wy)
+{
+    const long long plane = (long long)g.D * g.P;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= plane) return;
+    const int d = (int)(i / g.P);
+    const int r = (int)(i - (long long)d * g.P);
+    const int c = d - r;
+    if (r >= g.h || c < 0 || c >= g.w) return;
+    float* duf = du + f * st_fs;
+    float* dvf = dv + f * st_fs;
+    float a = 0.0f, b = 0.0f;
+    if (mode == 0) {
+        duf[i] = 0.0f;
+        dvf[i] = 0.0f;
+    } else {
+        a = duf[i];
+        b = dvf[i];
+    }
+    const float* Jf = J + f * J_fs;
+    const float* Wf = W + f * W_fs;
+    const long long qs = (long long)K * plane;
+    float A11 = 0.f, A22 = 0.f, A12 = 0.f, C13 = 0.f, C23 = 0.f;
+    for (int k = 0; k < K; ++k) {
+        const long long o = (long long)k * plane + i;
+        const float j11 = Jf[o], j22 = Jf[qs + o], j33 = Jf[2 * qs + o];
+        const float j12 = Jf[3 * qs + o], j13 = Jf[4 * qs + o], j23 = Jf[5 * qs + o];
+        float psi = 1.0f;
+        if (mode != 0) {
+            float E = j11 * a * a + j22 * b * b + j23 * b + 2.0f * j12 * a * b + 2.0f * j13 * a + j23 * b + j33;
+            E = fmaxf(E, 0.0f);
+            psi = ad.a[k] * powf(E + 1e-5f, ad.a[k] - 1.0f);
+        }
+        const float wp = Wf[o] * psi;
+        A11 = fmaf(wp, j11, A11);
+        A22 = fmaf(wp, j22, A22);
+        A12 = fmaf(wp, j12, A12);
+        C13 = fmaf(wp, j13, C13);
+        C23 = fmaf(wp, j23, C23);
+    }
+    const float sm = ((wx + wx) + wy) + wy;
+    const float den_u = sm + A11, den_v = sm + A22;
+    float* cf = coef + f * coef_fs;
+    cf[i] = A12;
+    cf[plane + i] = lap[f * lap_fs + i] - C13;
+    cf[2 * plane + i] = lap[f * lap_fs + plane + i] - C23;
+    cf[3 * plane + i] = den_u != 0.0f ? 1.0f / den_u : 0.0f;
+    cf[4 * plane + i] = den_v != 0.0f ? 1.0f / den_v : 0.0f;
+}
+
+cudaError_t launch_fold(const float* J, long long J_fs, const float* W, long long W_fs,
+                        const float* lap, long long lap_fs, float* du, float* dv,
+                        long long st_fs, float* coef, long long coef_fs, int n_frames, int K,
+                        DiagGeom g, const float* a_data, int mode, float wx, float wy,
+                        cudaStream_t st)
+{
+    AData ad;
+    for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0f;
+    const long long plane = (long long)g.D * g.P;
+    dim3 blk(256), grd((unsigned)((plane + 255) / 256), n_frames);
+    k_fold<<<grd, blk, 0, st>>>(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, K, g, ad,
+                                mode, wx, wy);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Exact-order SOR (core/level_solver.py:257-364) as a pipelined wavefront.
+//
+// The reference sweeps columns outer, rows inner, in place, so the update of
+// pixel (r, c) in iteration t reads iteration t values at (r-1, c), (r, c-1)
+// and iteration t-1 values at (r+1, c), (r, c+1).  Processing (r, c, t) at
+// step s = r + c + 2t satisfies all four dependencies with a one-step gap, and
+// at any step the pixels being written (diagonals of s's parity) and the
+// pixels being read (the other parity) are disjoint.  Neighbours across the
+// level border read the pixel's own pre-update value (the Neumann copy of
+// set_boundary_2d, :45-66, taken at the start of the iteration).
+//
+// One CTA owns one frame of the level for G consecutive iterations (the span
+// between two psi ticks).  Thread a owns row a.  A shared-memory ring keeps the
+// 2G+2 diagonals that are live; diagonal s+2 is stored into the ring at step s
+// from registers filled kPrefetch steps earlier, and the diagonal that leaves
+// the ring is written back to global memory.
+// Ring slot layout: 7 planes of P floats: du, dv, A12, BU, BV, 1/den_u, 1/den_v.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMaxLane) k_sor(const float* __restrict__ coef, long long coef_fs,
+                                                  float* __restrict__ du_g, float* __restrict__ dv_g,
+                                                  long long st_fs, DiagGeom g, int G, float wa, float wb,
+                                                  float omega)
+{
+    extern __shared__ float sm[];
+    const int P = g.P, A = g.h, B = g.w, D = g.D;
+    const int R = 2 * G + 2;
+    const int a = threadIdx.x;
+    const long long plane = (long long)D * P;
+    const float* cf = coef + blockIdx.x * coef_fs;
+    float* du = du_g + blockIdx.x * st_fs;
+    float* dv = dv_g + blockIdx.x * st_fs;
+    const float one_m_omega = 1.0f - omega;
+
+    auto row_valid = [&](int d) { return d >= 0 && d < D && a < A && a <= d && d - a < B; };
+    auto load = [&](int d, float* r) {
+        if (row_valid(d)) {
+            const long long o = (long long)d * P + a;
+            r[0] = du[o];
+            r[1] = dv[o];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) r[2 + q] = cf[q * plane + o];
+        }
+    };
+    auto put = [&](int d, const float* r) {
+        if (row_valid(d)) {
+            float* S = sm + (long long)(d % R) * 7 * P + a;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) S[q * P] = r[q];
+        }
+    };
+    auto writeback = [&](int d) {
+        if (row_valid(d)) {
+            const float* S = sm + (long long)(d % R) * 7 * P + a;
+            const long long o = (long long)d * P + a;
+            du[o] = S[0];
+            dv[o] = S[P];
+        }
+    };
+
+    float buf[kPrefetch][7];
+    {
+        float r0[7], r1[7];
+        load(0, r0);
+        load(1, r1);
+        put(0, r0);
+        put(1, r1);
+    }
+#pragma unroll
+    for (int j = 0; j < kPrefetch; ++j) load(2 + j, buf[(2 + j) % kPrefetch]);
+    __syncthreads();
+
+    const int nsteps = D + 2 * (G - 1);
+    for (int s0 = 0; s0 < nsteps; s0 += kPrefetch) {
+#pragma unroll
+        for (int q = 0; q < kPrefetch; ++q) {
+            const int s = s0 + q;
+            if (s < nsteps) {
+                for (int gi = 0; gi < G; ++gi) {
+                    const int d = s - 2 * gi;
+                    if (d < 0) break;
+                    if (d >= D) continue;
+                    const int b = d - a;
+                    if (a >= A || b < 0 || b >= B) continue;
+                    float* S = sm + (long long)(d % R) * 7 * P;
+                    const float* Sm = sm + (long long)((d + R - 1) % R) * 7 * P;
+                    const float* Sp = sm + (long long)((d + 1) % R) * 7 * P;
+                    const float duc = S[a], dvc = S[P + a];
+                    const float A12 = S[2 * P + a], BU = S[3 * P + a], BV = S[4 * P + a];
+                    const float iDu = S[5 * P + a], iDv = S[6 * P + a];
+                    const float duAm = a > 0 ? Sm[a - 1] : duc;
+                    const float dvAm = a > 0 ? Sm[P + a - 1] : dvc;
+                    const float duBm = b > 0 ? Sm[a] : duc;
+                    const float dvBm = b > 0 ? Sm[P + a] : dvc;
+                    const float duAp = a < A - 1 ? Sp[a + 1] : duc;
+                    const float dvAp = a < A - 1 ? Sp[P + a + 1] : dvc;
+                    const float duBp = b < B - 1 ? Sp[a] : duc;
+                    const float dvBp = b < B - 1 ? Sp[P + a] : dvc;
+                    const float nu = wa * (duAm + duAp) + wb * (duBm + duBp) + BU - A12 * dvc;
+                    const float dun = one_m_omega * duc + omega * (nu * iDu);
+                    const float nv = wa * (dvAm + dvAp) + wb * (dvBm + dvBp) + BV - A12 * dun;
+                    const float dvn = one_m_omega * dvc + omega * (nv * iDv);
+                    S[a] = dun;
+                    S[P + a] = dvn;
+                }
+                writeback(s - 2 * G);
+                put(s + 2, buf[(q + 2) % kPrefetch]);
+                load(s + 2 + kPrefetch, buf[(q + 2) % kPrefetch]);
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = max(0, nsteps - 2 * G); e < D; ++e) writeback(e);
+}
+
+cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                       int n_frames, DiagGeom g, int G, float wa, float wb, float omega,
+                       cudaStream_t st)
+{
+    if (g.P > kMaxLane || G < 1 || G > kGMax || (g.P & 31)) return cudaErrorInvalidValue;
+    const int R = 2 * G + 2;
+    const size_t smem = (size_t)R * 7 * g.P * sizeof(float);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_sor, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)((size_t)kRing * 7 * kMaxLane * sizeof(float)));
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    k_sor<<<n_frames, g.P, smem, st>>>(coef, coef_fs, du, dv, st_fs, g, G, wa, wb, omega);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// 5x5 median with scipy's "mirror" boundary on du and dv (core/optical_flow.py:
+// 607-609), then u + du, v + dv on the interior (:610-611).
+// The median is a forgetful selection: keep 14 candidates, repeatedly drop the
+// minimum and maximum and admit the next value; the middle of the last three
+// is the 13th smallest of the 25.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cswap(float& x, float& y)
+{
+    const float lo = fminf(x, y), hi = fmaxf(x, y);
+    x = lo;
+    y = hi;
+}
+
+__device__ __forceinline__ int mirror(int i, int n)
+{
+    // valid for n >= 3 and |offset| <= 2 beyond the edge
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+    return i;
+}
+
+__device__ float median25(float v[25])
+{
+    float t[14];
+#pragma unroll
+    for (int i = 0; i < 14; ++i) t[i] = v[i];
+#pragma unroll
+    for (int round = 0; round < 11; ++round) {
+        const int lo = round;  // window t[lo..13]
+#pragma unroll
+        for (int i = lo + 1; i < 14; ++i) cswap(t[lo], t[i]);
+#pragma unroll
+        for (int i = lo + 1; i < 13; ++i) cswap(t[i], t[13]);
+        t[13] = v[14 + round];
+    }
+    // window t[11..13]: median of three
+    cswap(t[11], t[12]);
+    cswap(t[12], t[13]);
+    cswap(t[11], t[12]);
+    return t[12];
+}
+
+__global__ void k_median_accum(const float* __restrict__ du, const float* __restrict__ dv, long long st_fs,
+                               View u, View v, DiagGeom g, int do_median, ViewW out_u, ViewW out_v)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= g.w) return;
+    const float* duf = du + f * st_fs;
+    const float* dvf = dv + f * st_fs;
+    float mu, mv;
+    if (do_median) {
+        float a[25], b[25];
+        int q = 0;
+#pragma unroll
+        for (int dy = -2; dy <= 2; ++dy) {
+            const int yy = mirror(y + dy, g.h);
+#pragma unroll
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int xx = mirror(x + dx, g.w);
+                const long long o = diag_index(g, yy, xx);
+                a[q] = duf[o];
+                b[q] = dvf[o];
+                ++q;
+            }
+        }
+        mu = median25(a);
+        mv = median25(b);
+    } else {
+        const long long o = diag_index(g, y, x);
+        mu = duf[o];
+        mv = dvf[o];
+    }
+    const float uc = u.p[f * u.fs + (long long)(y + 1) * u.rs + (long long)(x + 1) * u.cs];
+    const float vc = v.p[f * v.fs + (long long)(y + 1) * v.rs + (long long)(x + 1) * v.cs];
+    out_u.p[f * out_u.fs + (long long)y * out_u.rs + (long long)x * out_u.cs] = uc + mu;
+    out_v.p[f * out_v.fs + (long long)y * out_v.rs + (long long)x * out_v.cs] = vc + mv;
+}
+
+cudaError_t launch_median_accum(const float* du, const float* dv, long long st_fs, View u, View v,
+                                int n_frames, DiagGeom g, int do_median, ViewW out_u, ViewW out_v,
+                                cudaStream_t st)
+{
+    dim3 blk(128), grd((g.w + 127) / 128, g.h, n_frames);
+    k_median_accum<<<grd, blk, 0, st>>>(du, dv, st_fs, u, v, g, do_median, out_u, out_v);
+    return cudaGetLastError();
+}
+
+}  // namespace frg
