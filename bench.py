@@ -1,0 +1,423 @@
+"""Benchmark of the GB300 optical-flow path on the 512x512x2 photon-count video.
+
+One step = one pass of get_displacement over one batch of frames (default
+400, pyflowreg's OFOptions.buffer_size) against the reference frame (mean of
+the first 50 frames), with pyflowreg's default flow options (alpha 1.5,
+eta 0.8, 50 iterations, update_lag 5, a_data 0.45, gradient constancy,
+quality preset -> min_level 0, channel weights 0.5/0.5).
+
+Prints one JSON line.  ``value`` is frames/s with the batch resident in HBM;
+``e2e`` is the same through the public device API with the batch in pinned
+host memory and the flows copied back, copies inside the timed region.
+``--impl reference`` times the CPU oracle (a restatement of pyflowreg's
+numba path; pyflowreg itself cannot run here) on the host cores instead.
+
+Multi-GPU (torchrun): frames are sharded, every rank registers its own batch
+(weak scaling, no data-path collective); the step time is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "frames/s 512²×2ch batched vs per-frame GPU at ≤1e-3 px vs ref; bwd/fwd ratio"
+H = W = 512
+K = 2
+OPTIONS = dict(alpha=(1.5, 1.5), eta=0.8, levels=100, min_level=0, iterations=50, update_lag=5, a_smooth=1.0,
+               a_data=0.45, const_assumption="gc")
+WEIGHT = (0.5, 0.5)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--frames", type=int, default=400, help="frames per step and rank")
+    ap.add_argument("--plain-frames", type=int, default=8, help="frames timed in the one-frame-per-call form")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="frames of the CPU baseline sample (0: one per core)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+# workload
+# --------------------------------------------------------------------------
+def make_workload(n_frames: int, device, seed: int = 1, frame0: int = 50):
+    """(reference (H, W, K), frames (T, H, W, K)) preprocessed, float32, on device."""
+    import torch
+
+    from pyflowreg_gb300.synthetic import TorchVideo, preprocess_torch
+
+    vid = TorchVideo(seed=seed, h=H, w=W, K=K, device=device)
+    with torch.no_grad():
+        first = vid.frames(0, 50)
+        ref_raw = first.mean(0)
+        distinct = min(n_frames, 64)
+        raw = vid.frames(frame0, distinct)
+        proc = preprocess_torch(raw, ref_raw)
+        ref = preprocess_torch(ref_raw, ref_raw)
+        reps = (n_frames + distinct - 1) // distinct
+        frames = proc.repeat(reps, 1, 1, 1)[:n_frames].contiguous()
+    return ref.contiguous(), frames
+
+
+def weight_tensor(device):
+    import torch
+
+    w = torch.empty((H, W, K), dtype=torch.float32, device=device)
+    for k in range(K):
+        w[:, :, k] = WEIGHT[k] / sum(WEIGHT)
+    return w
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the SOR kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "k_sor" and parts[1] == "bytes_per_algorithmic_byte":
+                return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    import pyflowreg_gb300 as G
+    from pyflowreg_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    T = args.frames
+    ref, frames = make_workload(T, dev, seed=1, frame0=50 + rank * T)
+    wt = weight_tensor(dev)
+    params = G.make_params(K=K, **OPTIONS)
+    plan = G.get_plan(params, H, W, K, T)
+    plan.set_reference(ref, wt)
+    out = torch.empty((T, H, W, 2), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        plan.displacement(frames, None, out)
+    torch.cuda.synchronize()
+
+    lib = _lib.load()
+    sampler = ClockSampler(local)
+    plan.set_profiling(True)
+    n0 = lib.frg_launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        plan.displacement(frames, None, out)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    launches = lib.frg_launch_count() - n0
+    sor_n, sor_ms, sor_bytes = plan.profile()
+    plan.set_profiling(False)
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * T * args.steps / (ms / 1e3)
+
+    # e2e through the public API: pinned host batch in, flows out, every step
+    host_in = frames.cpu().pin_memory()
+    host_out = torch.empty((T, H, W, 2), dtype=torch.float32).pin_memory()
+    dev_in = torch.empty_like(frames)
+
+    def e2e_step():
+        dev_in.copy_(host_in, non_blocking=True)
+        G.get_displacement_device(ref, dev_in, None, wt, out_t=out, **OPTIONS)
+        host_out.copy_(out, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e_value = world * T * args.steps / (e_ms / 1e3)
+
+    # plain form: one frame per call (the same kernels, batch of one)
+    plain = None
+    if args.plain_frames > 0:
+        pplan = G.Plan(params, H, W, K, 1)
+        pplan.set_reference(ref, wt)
+        pout = torch.empty((1, H, W, 2), dtype=torch.float32, device=dev)
+        pplan.displacement(frames[:1], None, pout)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for i in range(args.plain_frames):
+            pplan.displacement(frames[i:i + 1], None, pout)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        p_ms = p0.elapsed_time(p1)
+        plain = {"value": args.plain_frames / (p_ms / 1e3), "unit": "frames/s", "frames": args.plain_frames,
+                 "ms_per_frame": p_ms / args.plain_frames}
+        pplan.close()
+
+    peak, peak_src = measured_peak()
+    achieved = (sor_bytes / (sor_ms / 1e3) / 1e9) if sor_ms > 0 else None
+    per_launch_bytes = sor_bytes / max(sor_n, 1)
+    ratio = profiled_traffic()
+    roofline = {
+        "kernel": "k_sor (exact-order wavefront SOR)",
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "peak_source": peak_src,
+        "unit": "GB/s",
+        "frac": (achieved / peak) if achieved else None,
+        "traffic": (per_launch_bytes * ratio) if ratio else None,
+        "algorithmic_bytes_per_launch": per_launch_bytes,
+        "launches": sor_n,
+        "share_of_step": (sor_ms / ms) if ms > 0 else None,
+        "note": "36 B per interior pixel per pipelined SOR iteration (streaming model); "
+                "the kernel keeps G iterations in shared memory, so frac can exceed 1",
+    }
+
+    cpu = None
+    parity = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, parity = cpu_baseline(args, ref, frames, out)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "frames/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": max(args.warmup, 3),
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded photon-count blob video, preprocessed on device)",
+            "config": {"workload": "512x512x2 video, batched get_displacement against the mean of frames 0-49",
+                       "frames_per_step": T * world, "frames_per_rank": T, "height": H, "width": W,
+                       "channels": K, "options": {**OPTIONS, "alpha": list(OPTIONS["alpha"]),
+                                                  "weight": list(WEIGHT)},
+                       "l2": "inputs larger than L2 (%.0f MB per step)" % (T * H * W * K * 4 / 1e6),
+                       "parallelism": f"frames sharded over {world} GPU(s)"},
+            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": T * H * W * K * 4,
+                    "d2h_bytes_per_step": T * H * W * 2 * 4},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "plain": plain,
+            "batched_over_plain": (value / world / plain["value"]) if plain else None,
+            "bwd_fwd_ratio": None,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+            "parity": parity,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, ref, frames, gpu_out):
+    """Oracle on the host cores on a bounded sample of the same frames; also
+    the flow difference GPU vs oracle on that sample."""
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    n = args.cpu_sample or cores
+    n = min(n, frames.shape[0])
+    fx = ref.cpu().numpy().astype(np.float64)
+    mv = frames[:n].cpu().numpy().astype(np.float64)
+    wt = np.empty((H, W, K))
+    for k in range(K):
+        wt[:, :, k] = WEIGHT[k] / sum(WEIGHT)
+    t0 = time.perf_counter()
+    flows = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
+    dt = time.perf_counter() - t0
+    g = gpu_out[:n].cpu().numpy().astype(np.float64)
+    d = g - flows
+    parity = {"frames": n, "max_abs_px": float(np.abs(d).max()),
+              "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean()),
+              "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4}}
+    cpu = {"value": n / dt, "unit": "frames/s", "cores": cores, "kind": "port",
+           "sample": f"{n} frames of the same batch, one frame per thread (OpenMP), fp64 lexicographic oracle"}
+    return cpu, parity
+
+
+# --------------------------------------------------------------------------
+# reference arm: the CPU restatement of pyflowreg's numba path
+# --------------------------------------------------------------------------
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    n = args.cpu_sample or cores
+    ref, frames = make_workload(n, "cpu", seed=1, frame0=50)
+    fx = ref.numpy().astype(np.float64)
+    mv = frames.numpy().astype(np.float64)
+    wt = np.empty((H, W, K))
+    for k in range(K):
+        wt[:, :, k] = WEIGHT[k] / sum(WEIGHT)
+    for _ in range(args.warmup):
+        O.get_displacement_batch(fx, mv[:1], n_threads=1, weight=wt, **OPTIONS)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
+    dt = time.perf_counter() - t0
+    value = n * args.steps / dt
+    del torch
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded photon-count blob video, preprocessed)",
+        "config": {"workload": "512x512x2 video, batched get_displacement against the mean of frames 0-49",
+                   "frames_per_step": n, "height": H, "width": W, "channels": K},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} frames per step, one frame per thread"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "pyflowreg's numba/OpenCV path cannot be installed here; the fp64 C restatement of it "
+                "(oracle/) is timed instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

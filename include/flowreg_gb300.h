@@ -104,6 +104,18 @@ int frg_set_reference(frg_plan* plan, const float* fixed, const float* weight, v
 int frg_get_displacement(frg_plan* plan, int n_frames, const float* moving, const float* uv_init,
                          float* flow_out, void* stream);
 
+/* Measurement hooks (no reference counterpart; pyflowreg has no tracing,
+ * only wall-clock prints in compensate_recording.py:770-890):
+ *   frg_launch_count: kernels launched by this library in this process.
+ *   frg_plan_set_profiling: when enabled, every SOR launch of the plan is
+ *     bracketed by CUDA events on its stream (counters reset on each call).
+ *   frg_plan_profile: waits for those events and returns the number of SOR
+ *     launches, their summed device time (ms) and their algorithmic bytes
+ *     (36 B per interior pixel per pipelined iteration). */
+long long frg_launch_count(void);
+int frg_plan_set_profiling(frg_plan* plan, int enable);
+int frg_plan_profile(frg_plan* plan, long long* sor_launches, double* sor_ms, double* sor_bytes);
+
 /* Backward warp of frames (n_frames, height, width, channels) by flow
  * (n_frames, height, width, 2); out-of-bounds pixels take reference
  * (height, width, channels).  cubic = 1 bicubic, 0 bilinear. */

@@ -80,6 +80,9 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_plan_device_bytes", S, [P])
         _sig(lib, "frg_plan_num_levels", I, [P])
         _sig(lib, "frg_plan_level_info", I, [P, I, pI, pI, pD, pD])
+        _sig(lib, "frg_launch_count", ctypes.c_longlong, [])
+        _sig(lib, "frg_plan_set_profiling", I, [P, I])
+        _sig(lib, "frg_plan_profile", I, [P, ctypes.POINTER(ctypes.c_longlong), pD, pD])
         _sig(lib, "frg_set_reference", I, [P, P, P, P])
         _sig(lib, "frg_get_displacement", I, [P, I, P, P, P, P])
         _sig(lib, "frg_imregister", I, [I, I, I, I, P, P, P, I, P, P])

@@ -184,6 +184,16 @@ class Plan:
     def device_bytes(self) -> int:
         return int(self.lib.frg_plan_device_bytes(self.handle))
 
+    def set_profiling(self, enable: bool) -> None:
+        _lib.check(self.lib.frg_plan_set_profiling(self.handle, 1 if enable else 0))
+
+    def profile(self):
+        """(SOR launches, summed SOR device ms, SOR algorithmic bytes) since set_profiling."""
+        n = ctypes.c_longlong()
+        ms, b = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.frg_plan_profile(self.handle, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
+        return n.value, ms.value, b.value
+
     def set_reference(self, fixed_t, weight_t=None, stream=None, key=None):
         """fixed_t (H, W, K) float32 CUDA tensor; weight_t the same shape or None."""
         if key is not None and key == self._ref_key:

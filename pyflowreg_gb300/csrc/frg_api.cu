@@ -10,6 +10,7 @@
 #include "../../include/flowreg_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,15 @@ int fail(int code, const std::string& msg)
         cudaError_t e_ = (call);                                                            \
         if (e_ != cudaSuccess)                                                              \
             return fail(FRG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+// Every kernel launch made by this library goes through FRG_LAUNCH, which
+// counts it (frg_launch_count) so a caller can state how many kernels ran.
+std::atomic<long long> g_launches{0};
+#define FRG_LAUNCH(call)                                                                    \
+    do {                                                                                    \
+        g_launches.fetch_add(1, std::memory_order_relaxed);                                 \
+        FRG_CUDA(call);                                                                     \
     } while (0)
 
 // ---------------------------------------------------------------------------
@@ -263,6 +273,17 @@ std::vector<Pass> make_passes(int iterations, int update_lag)
     return out;
 }
 
+// CUDA-event timing of every SOR launch, enabled by frg_plan_set_profiling.
+// Algorithmic bytes of one launch: per interior pixel and pipelined
+// iteration, five coefficients and du, dv read plus du, dv written (36 B).
+struct SorProfile {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;  // begin/end pairs
+    size_t used = 0;
+    double bytes = 0.0;
+    long long launches = 0;
+};
+
 }  // namespace
 
 struct frg_plan {
@@ -287,6 +308,7 @@ struct frg_plan {
     float* uacc[2] = {nullptr, nullptr};  // (T, 2, h, w)
     float* ones = nullptr;    // (H, W, K) default weight
     float a_data[kMaxK] = {0};
+    SorProfile prof;
 };
 
 namespace {
@@ -344,18 +366,41 @@ ViewW vieww(float* p, long long fs, long long ps, long long rs, long long cs)
     return v;
 }
 
+int record_event(SorProfile* pr, cudaStream_t st)
+{
+    if (pr->used == pr->ev.size()) {
+        cudaEvent_t e;
+        FRG_CUDA(cudaEventCreate(&e));
+        pr->ev.push_back(e);
+    }
+    FRG_CUDA(cudaEventRecord(pr->ev[pr->used++], st));
+    return FRG_OK;
+}
+
 // Runs the passes of one level: fold at ticks, wavefront SOR passes.
 int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs, const float* W,
                 long long W_fs, const float* lap, long long lap_fs, float* du, float* dv,
                 long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
-                const float* a_data, float wx, float wy, float omega, cudaStream_t st)
+                const float* a_data, float wx, float wy, float omega, cudaStream_t st,
+                SorProfile* prof = nullptr)
 {
     for (const Pass& ps : passes) {
         if (ps.fold_mode >= 0)
-            FRG_CUDA(launch_fold(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, T, K, g,
-                                 a_data, ps.fold_mode, wx, wy, st));
+            FRG_LAUNCH(launch_fold(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, T, K, g,
+                                   a_data, ps.fold_mode, wx, wy, st));
+        const bool timed = prof && prof->on;
+        if (timed) {
+            int rc = record_event(prof, st);
+            if (rc) return rc;
+        }
         // thread index runs along rows: rows are the a-direction (weight wy)
-        FRG_CUDA(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+        FRG_LAUNCH(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+        if (timed) {
+            int rc = record_event(prof, st);
+            if (rc) return rc;
+            prof->bytes += 36.0 * ps.G * (double)T * g.h * g.w;
+            prof->launches += 1;
+        }
     }
     return FRG_OK;
 }
@@ -389,7 +434,36 @@ void frg_plan_destroy(frg_plan* plan)
 {
     if (!plan) return;
     for (void* p : plan->allocs) cudaFree(p);
+    for (cudaEvent_t e : plan->prof.ev) cudaEventDestroy(e);
     delete plan;
+}
+
+long long frg_launch_count(void) { return g_launches.load(); }
+
+int frg_plan_set_profiling(frg_plan* plan, int enable)
+{
+    if (!plan) return fail(FRG_EINVAL, "plan is NULL");
+    plan->prof.on = enable != 0;
+    plan->prof.used = 0;
+    plan->prof.bytes = 0.0;
+    plan->prof.launches = 0;
+    return FRG_OK;
+}
+
+int frg_plan_profile(frg_plan* plan, long long* sor_launches, double* sor_ms, double* sor_bytes)
+{
+    if (!plan) return fail(FRG_EINVAL, "plan is NULL");
+    double ms = 0.0;
+    for (size_t i = 0; i + 1 < plan->prof.used; i += 2) {
+        FRG_CUDA(cudaEventSynchronize(plan->prof.ev[i + 1]));
+        float t = 0.0f;
+        FRG_CUDA(cudaEventElapsedTime(&t, plan->prof.ev[i], plan->prof.ev[i + 1]));
+        ms += t;
+    }
+    if (sor_launches) *sor_launches = plan->prof.launches;
+    if (sor_ms) *sor_ms = ms;
+    if (sor_bytes) *sor_bytes = plan->prof.bytes;
+    return FRG_OK;
 }
 
 int frg_plan_create(const frg_params* params, int height, int width, int channels, int max_frames,
@@ -570,15 +644,15 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
     for (LevelPlan& L : pl->levels) {
         // reference level: resize(fixed) (core/optical_flow.py:519)
         View src = view(fixed, 0, 1, (long long)W * K, K);
-        FRG_CUDA(launch_resize_h(src, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
-        FRG_CUDA(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(L.ref, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
+        FRG_LAUNCH(launch_resize_h(src, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
+        FRG_LAUNCH(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(L.ref, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
                                  L.img.iy, L.img.wy, L.img.P, st));
         // weight level: resize(weight) (core/optical_flow.py:565-570), diagonal-major
         View wv = view(wsrc, 0, 1, (long long)W * K, K);
-        FRG_CUDA(launch_resize_h(wv, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
-        FRG_CUDA(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(pl->f2, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
+        FRG_LAUNCH(launch_resize_h(wv, 1, K, H, W, pl->tmp, L.w, L.img.ix, L.img.wx, L.img.P, st));
+        FRG_LAUNCH(launch_resize_v(pl->tmp, 1, K, H, L.w, vieww(pl->f2, 0, (long long)L.h * L.w, L.w, 1), L.h, 0,
                                  L.img.iy, L.img.wy, L.img.P, st));
-        FRG_CUDA(launch_to_diag(view(pl->f2, 0, (long long)L.h * L.w, L.w, 1), 1, K, L.h, L.w, L.wdiag, 0, L.g,
+        FRG_LAUNCH(launch_to_diag(view(pl->f2, 0, (long long)L.h * L.w, L.w, 1), 1, K, L.h, L.w, L.wdiag, 0, L.g,
                                 st));
     }
     pl->has_ref = true;
@@ -602,18 +676,18 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         const long long hw = (long long)h * w, pad = (long long)(h + 2) * (w + 2);
         const long long dp = (long long)L.g.D * L.g.P;
         // 1. moving level images from full resolution (core/optical_flow.py:520)
-        FRG_CUDA(launch_resize_h(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->tmp, w, L.img.ix,
+        FRG_LAUNCH(launch_resize_h(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->tmp, w, L.img.ix,
                                  L.img.wx, L.img.P, st));
-        FRG_CUDA(launch_resize_v(pl->tmp, T, K, H, w, vieww(pl->f2, K * hw, hw, w, 1), h, 0, L.img.iy, L.img.wy,
+        FRG_LAUNCH(launch_resize_v(pl->tmp, T, K, H, w, vieww(pl->f2, K * hw, hw, w, 1), h, 0, L.img.iy, L.img.wy,
                                  L.img.P, st));
         // 2. flow at this level with an edge ring (core/optical_flow.py:530-536)
         long long uv_fs;
         if (L.top) {
             uv_fs = 0;  // one field shared by every frame
             if (uv_init) {
-                FRG_CUDA(launch_resize_h(view(uv_init, 0, 1, (long long)W * 2, 2), 1, 2, H, W, pl->tmp, w,
+                FRG_LAUNCH(launch_resize_h(view(uv_init, 0, 1, (long long)W * 2, 2), 1, 2, H, W, pl->tmp, w,
                                          L.flow.ix, L.flow.wx, L.flow.P, st));
-                FRG_CUDA(launch_resize_v(pl->tmp, 1, 2, H, w, vieww(pl->uvpad, 0, pad, w + 2, 1), h, 1, L.flow.iy,
+                FRG_LAUNCH(launch_resize_v(pl->tmp, 1, 2, H, w, vieww(pl->uvpad, 0, pad, w + 2, 1), h, 1, L.flow.iy,
                                          L.flow.wy, L.flow.P, st));
             } else {
                 FRG_CUDA(cudaMemsetAsync(pl->uvpad, 0, sizeof(float) * 2 * pad, st));
@@ -621,9 +695,9 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         } else {
             uv_fs = 2 * pad;
             const long long phw = (long long)prev->h * prev->w;
-            FRG_CUDA(launch_resize_h(view(pl->uacc[cur], 2 * phw, phw, prev->w, 1), T, 2, prev->h, prev->w,
+            FRG_LAUNCH(launch_resize_h(view(pl->uacc[cur], 2 * phw, phw, prev->w, 1), T, 2, prev->h, prev->w,
                                      pl->tmp, w, L.flow.ix, L.flow.wx, L.flow.P, st));
-            FRG_CUDA(launch_resize_v(pl->tmp, T, 2, prev->h, w, vieww(pl->uvpad, 2 * pad, pad, w + 2, 1), h, 1,
+            FRG_LAUNCH(launch_resize_v(pl->tmp, T, 2, prev->h, w, vieww(pl->uvpad, 2 * pad, pad, w + 2, 1), h, 1,
                                      L.flow.iy, L.flow.wy, L.flow.P, st));
         }
         View up = view(pl->uvpad, uv_fs, 0, w + 2, 1);
@@ -635,18 +709,18 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         if (!L.top) {
             View ui = view(pl->uvpad + (w + 2) + 1, uv_fs, 0, w + 2, 1);
             View vi = view(pl->uvpad + pad + (w + 2) + 1, uv_fs, 0, w + 2, 1);
-            FRG_CUDA(launch_warp(f2v, f1v, ui, vi, T, K, h, w, (float)L.h_col, (float)L.h_row, 1,
+            FRG_LAUNCH(launch_warp(f2v, f1v, ui, vi, T, K, h, w, (float)L.h_col, (float)L.h_row, 1,
                                  vieww(pl->warped, K * hw, hw, w, 1), st));
             img2 = view(pl->warped, K * hw, hw, w, 1);
         }
         // 4. motion tensor and smoothness constants (core/optical_flow.py:547-563)
         const long long J_fs = 6LL * K * dp;
-        FRG_CUDA(launch_tensor(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
+        FRG_LAUNCH(launch_tensor(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
                                pl->J, J_fs, L.g, st));
-        FRG_CUDA(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
+        FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
         // 5. level solve (core/optical_flow.py:584-606)
         int rc = solve_level(pl->passes, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du, pl->dv, dp, pl->coef,
-                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st);
+                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st, &pl->prof);
         if (rc) return rc;
         // 6. median + accumulate (core/optical_flow.py:607-611)
         const int do_median = std::min(h, w) > 5 ? 1 : 0;
@@ -661,7 +735,7 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
             ov = vieww(pl->uacc[nxt] + hw, 2 * hw, 0, w, 1);
             cur = nxt;
         }
-        FRG_CUDA(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
+        FRG_LAUNCH(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
         prev = &L;
     }
     return FRG_OK;
@@ -681,7 +755,7 @@ int frg_imregister(int n_frames, int height, int width, int channels, const floa
     View u = view(flow, H * W * 2, 0, W * 2, 2);
     View v = view(flow + 1, H * W * 2, 0, W * 2, 2);
     ViewW o = vieww(out, H * W * K, 1, W * K, K);
-    FRG_CUDA(launch_warp(f2, f1, u, v, n_frames, channels, height, width, 1.0f, 1.0f, cubic ? 1 : 0, o,
+    FRG_LAUNCH(launch_warp(f2, f1, u, v, n_frames, channels, height, width, 1.0f, 1.0f, cubic ? 1 : 0, o,
                          (cudaStream_t)stream));
     return FRG_OK;
 }
@@ -716,17 +790,17 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
     auto run = [&]() -> int {
         // J arrays (m, n, K) channel-last; interior starts at (1, 1)
         for (int q = 0; q < 6; ++q)
-            FRG_CUDA(launch_to_diag(view(J + q * mn * K + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K,
+            FRG_LAUNCH(launch_to_diag(view(J + q * mn * K + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K,
                                     h, w, Jd + q * K * dp, 0, g, st));
-        FRG_CUDA(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd,
+        FRG_LAUNCH(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd,
                                 0, g, st));
-        FRG_CUDA(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
+        FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
         std::vector<Pass> passes = make_passes(iterations, update_lag);
         int r = solve_level(passes, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy, (float)omega,
                             st);
         if (r) return r;
-        FRG_CUDA(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
-        FRG_CUDA(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
+        FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
+        FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
         return FRG_OK;
     };
     rc = run();
@@ -755,9 +829,9 @@ int frg_resize(int n_planes, int ih, int iw, const float* src, int oh, int ow, f
         FRG_CUDA(cudaMemcpyAsync(wx, tx.wt.data(), tx.wt.size() * 4, cudaMemcpyHostToDevice, st));
         FRG_CUDA(cudaMemcpyAsync(iy, ty.idx.data(), ty.idx.size() * 4, cudaMemcpyHostToDevice, st));
         FRG_CUDA(cudaMemcpyAsync(wy, ty.wt.data(), ty.wt.size() * 4, cudaMemcpyHostToDevice, st));
-        FRG_CUDA(launch_resize_h(view(src, 0, (long long)ih * iw, iw, 1), 1, n_planes, ih, iw, tmp, ow, ix, wx, tx.P,
+        FRG_LAUNCH(launch_resize_h(view(src, 0, (long long)ih * iw, iw, 1), 1, n_planes, ih, iw, tmp, ow, ix, wx, tx.P,
                                  st));
-        FRG_CUDA(launch_resize_v(tmp, 1, n_planes, ih, ow, vieww(dst, 0, (long long)oh * ow, ow, 1), oh, 0, iy, wy,
+        FRG_LAUNCH(launch_resize_v(tmp, 1, n_planes, ih, ow, vieww(dst, 0, (long long)oh * ow, ow, 1), oh, 0, iy, wy,
                                  ty.P, st));
         // the host vectors must outlive the asynchronous copies
         FRG_CUDA(cudaStreamSynchronize(st));
@@ -780,10 +854,10 @@ int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy,
     float* Jd = nullptr;
     FRG_CUDA(cudaMallocAsync((void**)&Jd, 6 * dp * sizeof(float), st));
     auto run = [&]() -> int {
-        FRG_CUDA(launch_tensor(view(f1, 0, 0, w, 1), view(f2, 0, 0, w, 1), 1, 1, h, w, (float)hy, (float)hx,
+        FRG_LAUNCH(launch_tensor(view(f1, 0, 0, w, 1), view(f2, 0, 0, w, 1), 1, 1, h, w, (float)hy, (float)hx,
                                gray ? 1 : 0, Jd, 0, g, st));
         const long long pad = (long long)(h + 2) * (w + 2);
-        FRG_CUDA(launch_from_diag(Jd, 0, 1, 6, g, vieww(out, 0, pad, w + 2, 1), 1, 1, st));
+        FRG_LAUNCH(launch_from_diag(Jd, 0, 1, 6, g, vieww(out, 0, pad, w + 2, 1), 1, 1, st));
         return FRG_OK;
     };
     int rc = run();
@@ -805,11 +879,11 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream)
     float* zeros = buf + 2 * dp;
     auto run = [&]() -> int {
         FRG_CUDA(cudaMemsetAsync(zeros, 0, pad * sizeof(float), st));
-        FRG_CUDA(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1, 0, g, st));
-        FRG_CUDA(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1 + dp, 0, g, st));
+        FRG_LAUNCH(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1, 0, g, st));
+        FRG_LAUNCH(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1 + dp, 0, g, st));
         View z = view(zeros, 0, 0, w + 2, 1);
         // the v output duplicates u; write it to the same destination
-        FRG_CUDA(launch_median_accum(d1, d1 + dp, 0, z, z, 1, g, 1, vieww(dst, 0, 0, w, 1),
+        FRG_LAUNCH(launch_median_accum(d1, d1 + dp, 0, z, z, 1, g, 1, vieww(dst, 0, 0, w, 1),
                                      vieww(dst, 0, 0, w, 1), st));
         return FRG_OK;
     };

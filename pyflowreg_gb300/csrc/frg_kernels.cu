@@ -318,8 +318,8 @@ cudaError_t launch_from_diag(const float* src, long long src_fs, int n_frames, i
 
 // ---------------------------------------------------------------------------
 // Coefficient fold at a lagged-nonlinearity tick (core/level_solver.py:229-255,
-// 342-364).  mode 0: first group, psi = 1 and du = dv = 0; mode 1: psi from the
-// current (du, dv).  Writes, per pixel, the five coefficients the SOR update
+// 342-364).  mode bit 0: first pass, du = dv = 0; bit 1: psi from the current
+// (du, dv) (a tick), else psi = 1.  Writes, per pixel, the five coefficients the SOR update
 // needs: A12 = sum_k W psi J12, BU = lap_u - sum_k W psi J13,
 // BV = lap_v - sum_k W psi J23, 1/den_u, 1/den_v (0 where the denominator is 0).
 // ---------------------------------------------------------------------------
@@ -341,8 +341,10 @@ __global__ void k_fold(const float* __restrict__ J, long long J_fs, const float*
     if (r >= g.h || c < 0 || c >= g.w) return;
     float* duf = du + f * st_fs;
     float* dvf = dv + f * st_fs;
+    const bool zero_init = (mode & 1) != 0;
+    const bool tick = (mode & 2) != 0;
     float a = 0.0f, b = 0.0f;
-    if (mode == 0) {
+    if (zero_init) {
         duf[i] = 0.0f;
         dvf[i] = 0.0f;
     } else {
@@ -358,7 +360,7 @@ __global__ void k_fold(const float* __restrict__ J, long long J_fs, const float*
         const float j11 = Jf[o], j22 = Jf[qs + o], j33 = Jf[2 * qs + o];
         const float j12 = Jf[3 * qs + o], j13 = Jf[4 * qs + o], j23 = Jf[5 * qs + o];
         float psi = 1.0f;
-        if (mode != 0) {
+        if (tick) {
             float E = j11 * a * a + j22 * b * b + j23 * b + 2.0f * j12 * a * b + 2.0f * j13 * a + j23 * b + j33;
             E = fmaxf(E, 0.0f);
             psi = ad.a[k] * powf(E + 1e-5f, ad.a[k] - 1.0f);

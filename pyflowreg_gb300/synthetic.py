@@ -134,3 +134,104 @@ class Video:
         for i in range(n):
             fr[i], tr[i] = self.frame(t0 + i)
         return fr, tr
+
+
+# --------------------------------------------------------------------------
+# Device-side renderer for large batches (torch; CPU or CUDA)
+# --------------------------------------------------------------------------
+class TorchVideo:
+    """The photon-count video above rendered with torch on `device`.
+
+    Per channel a fixed set of blobs; per frame t a rigid shift N(0, shift_std)
+    plus a sinusoid field whose phases drift as 2*pi*t/period, Poisson counts
+    with a per-frame mean in [50, 2000].  Seeds are per frame, so any frame can
+    be rendered independently and every call is reproducible.
+    """
+
+    def __init__(self, seed=1, h=512, w=512, K=2, n_blobs=40, sinus_amp=2.0, shift_std=3.0, period=250.0,
+                 device="cpu"):
+        import torch
+
+        self.torch = torch
+        self.h, self.w, self.K = h, w, K
+        self.device = torch.device(device)
+        rng = np.random.default_rng(seed)
+        self.blobs = []
+        for _ in range(K):
+            b = Blobs(rng, h, w, n_blobs)
+            self.blobs.append([torch.tensor(a, dtype=torch.float32, device=self.device)
+                               for a in (b.cy, b.cx, b.s, b.a)])
+        self.field = SinusoidField(rng, sinus_amp)
+        self.field.calibrate(h, w)
+        self.fk = [[torch.tensor(np.asarray(a), dtype=torch.float32, device=self.device) for a in comp]
+                   for comp in self.field.k]
+        self.shift_std, self.period, self.seed = shift_std, period, seed
+        yy, xx = torch.meshgrid(torch.arange(h, dtype=torch.float32, device=self.device),
+                                torch.arange(w, dtype=torch.float32, device=self.device), indexing="ij")
+        self.yy, self.xx = yy, xx
+
+    def _field(self, yy, xx, phase):
+        out = []
+        for ky, kx, ph in self.fk:
+            arg = ky[:, None, None] * yy[None] + kx[:, None, None] * xx[None] + ph[:, None, None] + phase
+            out.append(self.torch.sin(arg).sum(0) * float(self.field.scale))
+        return out
+
+    def _blobs(self, k, yy, xx):
+        cy, cx, s, a = self.blobs[k]
+        out = self.torch.full_like(yy, 0.05)
+        for i in range(cy.shape[0]):
+            out = out + a[i] * self.torch.exp(-((yy - cy[i]) ** 2 + (xx - cx[i]) ** 2) / (2.0 * s[i] * s[i]))
+        return out
+
+    def frame(self, t: int):
+        torch = self.torch
+        rng = np.random.default_rng(1000 * self.seed + t)
+        shift = rng.normal(0.0, self.shift_std, 2)
+        lam = float(rng.uniform(50.0, 2000.0))
+        phase = 2.0 * np.pi * t / self.period
+        px, py = self.xx.clone(), self.yy.clone()
+        for _ in range(30):
+            u, v = self._field(py, px, phase)
+            px = self.xx - u - float(shift[0])
+            py = self.yy - v - float(shift[1])
+        gen = torch.Generator(device=self.device)
+        gen.manual_seed(int(1000 * self.seed + t))
+        out = torch.empty((self.h, self.w, self.K), dtype=torch.float32, device=self.device)
+        for k in range(self.K):
+            img = self._blobs(k, py, px)
+            out[:, :, k] = torch.poisson(lam * torch.clamp(img / 2.0, min=0.0), generator=gen)
+        return out
+
+    def frames(self, t0: int, n: int):
+        out = self.torch.empty((n, self.h, self.w, self.K), dtype=self.torch.float32, device=self.device)
+        for i in range(n):
+            out[i] = self.frame(t0 + i)
+        return out
+
+
+def preprocess_torch(frames, ref_raw, sigma=1.0, truncate=4.0):
+    """Normalise by the raw reference's joint min/max and blur each channel with
+    a spatial Gaussian (sigma 1, truncate 4, reflect) -- the input preparation
+    compensate_recording applies before get_displacement
+    (motion_correction/compensate_recording.py:521-561), used here only to give
+    the synthetic workload the value range the flow path sees."""
+    import torch
+    import torch.nn.functional as F
+
+    lo, hi = float(ref_raw.min()), float(ref_raw.max())
+    x = (frames - lo) / max(hi - lo, 1e-12)
+    r = int(truncate * sigma + 0.5)
+    g = torch.exp(-0.5 * (torch.arange(-r, r + 1, dtype=torch.float32, device=frames.device) / sigma) ** 2)
+    g = g / g.sum()
+    single = x.ndim == 3
+    if single:
+        x = x[None]
+    T, H, W, K = x.shape
+    y = x.permute(0, 3, 1, 2).reshape(T * K, 1, H, W)
+    y = F.pad(y, (r, r, 0, 0), mode="reflect")
+    y = F.conv2d(y, g.view(1, 1, 1, -1))
+    y = F.pad(y, (0, 0, r, r), mode="reflect")
+    y = F.conv2d(y, g.view(1, 1, -1, 1))
+    y = y.reshape(T, K, H, W).permute(0, 2, 3, 1).contiguous()
+    return y[0] if single else y
