@@ -348,11 +348,21 @@ def cpu_baseline(args, ref, frames, gpu_out):
     t0 = time.perf_counter()
     flows = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
     dt = time.perf_counter() - t0
-    g = gpu_out[:n].cpu().numpy().astype(np.float64)
-    d = g - flows
-    parity = {"frames": n, "max_abs_px": float(np.abs(d).max()),
-              "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean()),
-              "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4}}
+
+    def diff(a):
+        d = a - flows
+        return {"max_abs_px": float(np.abs(d).max()), "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean())}
+
+    import pyflowreg_gb300 as G
+
+    f64 = G.get_displacement_device(ref, frames[:n].contiguous(), None, weight_tensor(ref.device),
+                                    precision="fp64", **OPTIONS)
+    parity = {"frames": n,
+              "fp64_reference_order": diff(f64.cpu().numpy()),
+              "fp32_fast_path": diff(gpu_out[:n].cpu().numpy().astype(np.float64)),
+              "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4},
+              "note": "fp32 deviation is bounded by the reference's own rounding amplification "
+                      "(oracle vs itself under 1e-7 input perturbation), see DESIGN.md"}
     cpu = {"value": n / dt, "unit": "frames/s", "cores": cores, "kind": "port",
            "sample": f"{n} frames of the same batch, one frame per thread (OpenMP), fp64 lexicographic oracle"}
     return cpu, parity

@@ -53,7 +53,17 @@ typedef struct frg_params {
     double a_data[FRG_MAX_CHANNELS];      /* data-term exponent per channel */
     int const_assumption;                 /* 0: gradient constancy "gc", 1: gray value "gray" */
     double omega;                         /* SOR relaxation factor (reference: 1.95) */
+    int precision;                        /* FRG_FP32 (default) or FRG_FP64_REFERENCE */
 } frg_params;
+
+/* precision: FRG_FP32 is the fast path (float32 arithmetic, folded SOR
+ * coefficients, shared-memory wavefront).  FRG_FP64_REFERENCE computes in
+ * the reference's own precision and operation order (float32 images and
+ * resize products, float64 accumulators, tensors and solver) with the same
+ * exact update order; it is the parity mode.  Its plans are driven with
+ * frg_get_displacement_f64. */
+#define FRG_FP32 0
+#define FRG_FP64_REFERENCE 1
 
 typedef struct frg_plan frg_plan;
 
@@ -91,6 +101,18 @@ int frg_plan_num_levels(const frg_plan* plan);
 int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double* alpha_x,
                         double* alpha_y);
 
+/* Replaces the resize tap tables of one level (host pointers, copied):
+ * kind 0 resizes the full-size frame to the level, kind 1 the previous
+ * level's flow (the full-size uv_init at the top level) to the level.
+ * ix/wx are (w, taps), iy/wy (h, taps), int32 / float32, as
+ * _precompute_fused_gauss_cubic returns them (util/resize_util.py:216-229).
+ * The library builds equivalent tables itself; the reference builds them with
+ * numpy, whose float32 exp differs in the last bit between CPU builds, and the
+ * solver amplifies such differences, so a host that wants the reference's
+ * tables bit for bit passes them here.  taps must equal the plan's. */
+int frg_plan_set_level_tables(frg_plan* plan, int level, int kind, int taps, const int* ix, const float* wx,
+                              const int* iy, const float* wy);
+
 /* Reference (fixed) frame (height, width, channels) float32 and the per-pixel
  * channel weight (height, width, channels) float32 (NULL: 1/channels), as
  * get_displacement receives them after its input normalisation
@@ -103,6 +125,11 @@ int frg_set_reference(frg_plan* plan, const float* fixed, const float* weight, v
  * the initial field shared by all frames (the executors' w_init). */
 int frg_get_displacement(frg_plan* plan, int n_frames, const float* moving, const float* uv_init,
                          float* flow_out, void* stream);
+
+/* The same for a plan created with precision = FRG_FP64_REFERENCE; flow_out
+ * (n_frames, height, width, 2) is float64 like the reference's return value. */
+int frg_get_displacement_f64(frg_plan* plan, int n_frames, const float* moving, const float* uv_init,
+                             double* flow_out, void* stream);
 
 /* Measurement hooks (no reference counterpart; pyflowreg has no tracing,
  * only wall-clock prints in compensate_recording.py:770-890):

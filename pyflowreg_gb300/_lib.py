@@ -37,7 +37,12 @@ class FrgParams(ctypes.Structure):
         ("a_data", ctypes.c_double * FRG_MAX_CHANNELS),
         ("const_assumption", ctypes.c_int),
         ("omega", ctypes.c_double),
+        ("precision", ctypes.c_int),
     ]
+
+
+FRG_FP32 = 0
+FRG_FP64_REFERENCE = 1
 
 
 class FrgError(RuntimeError):
@@ -80,11 +85,13 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_plan_device_bytes", S, [P])
         _sig(lib, "frg_plan_num_levels", I, [P])
         _sig(lib, "frg_plan_level_info", I, [P, I, pI, pI, pD, pD])
+        _sig(lib, "frg_plan_set_level_tables", I, [P, I, I, I, pI, pF, pI, pF])
         _sig(lib, "frg_launch_count", ctypes.c_longlong, [])
         _sig(lib, "frg_plan_set_profiling", I, [P, I])
         _sig(lib, "frg_plan_profile", I, [P, ctypes.POINTER(ctypes.c_longlong), pD, pD])
         _sig(lib, "frg_set_reference", I, [P, P, P, P])
         _sig(lib, "frg_get_displacement", I, [P, I, P, P, P, P])
+        _sig(lib, "frg_get_displacement_f64", I, [P, I, P, P, P, P])
         _sig(lib, "frg_imregister", I, [I, I, I, I, P, P, P, I, P, P])
         _sig(lib, "frg_level_solve", I, [I, I, I, P, P, P, P, D, D, I, I, pD, D, D, D, D, P, P, P])
         _sig(lib, "frg_resize", I, [I, I, I, P, I, I, P, P])

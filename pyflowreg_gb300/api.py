@@ -126,11 +126,21 @@ def alpha_pair(alpha):
     return float(alpha[0]), float(alpha[1] if len(alpha) > 1 else alpha[0])
 
 
+PRECISIONS = {"fp32": _lib.FRG_FP32, "fp64": _lib.FRG_FP64_REFERENCE}
+
+
 def make_params(alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
-                a_smooth=1.0, a_data=0.45, const_assumption="gc", K=1, omega=1.95) -> "_lib.FrgParams":
+                a_smooth=1.0, a_data=0.45, const_assumption="gc", K=1, omega=1.95,
+                precision="fp32") -> "_lib.FrgParams":
+    """Options as a frg_params struct.  precision "fp32" is the fast path;
+    "fp64" computes in the reference's precision and operation order (the
+    parity mode)."""
     if K > _lib.FRG_MAX_CHANNELS:
         raise ValueError(f"at most {_lib.FRG_MAX_CHANNELS} channels are supported")
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
     p = _lib.FrgParams()
+    p.precision = PRECISIONS[precision]
     p.alpha_x, p.alpha_y = alpha_pair(alpha)
     p.eta = float(eta)
     p.levels = int(levels)
@@ -150,7 +160,7 @@ def make_params(alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=5
 
 def _params_key(p) -> tuple:
     return (p.alpha_x, p.alpha_y, p.eta, p.levels, p.min_level, p.iterations, p.update_lag, p.a_smooth,
-            tuple(p.a_data), p.const_assumption, p.omega)
+            tuple(p.a_data), p.const_assumption, p.omega, p.precision)
 
 
 # --------------------------------------------------------------------------
@@ -170,6 +180,23 @@ class Plan:
                    "frg_plan_create")
         self.handle = h
         self._ref_key = None
+        self._load_tables()
+
+    def _load_tables(self):
+        """Uploads the reference's numpy-built resize tables for every level."""
+        from . import tables
+
+        pI = ctypes.POINTER(ctypes.c_int)
+        pF = ctypes.POINTER(ctypes.c_float)
+        prev = None
+        for i, (h, w, _, _) in enumerate(self.levels()):
+            srcs = ((0, (self.H, self.W)), (1, prev if prev is not None else (self.H, self.W)))
+            for kind, src in srcs:
+                ix, wx, iy, wy = tables.level_tables(src, (h, w))
+                _lib.check(self.lib.frg_plan_set_level_tables(
+                    self.handle, i, kind, ix.shape[1], ix.ctypes.data_as(pI), wx.ctypes.data_as(pF),
+                    iy.ctypes.data_as(pI), wy.ctypes.data_as(pF)), "frg_plan_set_level_tables")
+            prev = (h, w)
 
     def levels(self):
         out = []
@@ -206,27 +233,33 @@ class Plan:
                                               _stream_ptr(stream)), "frg_set_reference")
         self._ref_key = key
 
+    @property
+    def fp64(self) -> bool:
+        return self.params.precision == _lib.FRG_FP64_REFERENCE
+
     def displacement(self, moving_t, uv_t=None, out_t=None, stream=None):
-        """moving_t (T, H, W, K) float32 CUDA tensor -> flow (T, H, W, 2) float32."""
+        """moving_t (T, H, W, K) float32 CUDA tensor -> flow (T, H, W, 2), float32
+        (float64 for an fp64 plan)."""
         T = moving_t.shape[0]
         self._check(moving_t, (T, self.H, self.W, self.K))
         if uv_t is not None:
             self._check(uv_t, (self.H, self.W, 2))
+        odt = torch.float64 if self.fp64 else torch.float32
         if out_t is None:
-            out_t = torch.empty((T, self.H, self.W, 2), dtype=torch.float32, device=moving_t.device)
-        self._check(out_t, (T, self.H, self.W, 2))
+            out_t = torch.empty((T, self.H, self.W, 2), dtype=odt, device=moving_t.device)
+        self._check(out_t, (T, self.H, self.W, 2), odt)
+        fn = self.lib.frg_get_displacement_f64 if self.fp64 else self.lib.frg_get_displacement
         for t0 in range(0, T, self.max_frames):
             t1 = min(T, t0 + self.max_frames)
-            _lib.check(self.lib.frg_get_displacement(self.handle, t1 - t0, _ptr(moving_t[t0:t1]),
-                                                     None if uv_t is None else _ptr(uv_t),
-                                                     _ptr(out_t[t0:t1]), _stream_ptr(stream)),
-                       "frg_get_displacement")
+            _lib.check(fn(self.handle, t1 - t0, _ptr(moving_t[t0:t1]), None if uv_t is None else _ptr(uv_t),
+                          _ptr(out_t[t0:t1]), _stream_ptr(stream)), "frg_get_displacement")
         return out_t
 
     @staticmethod
-    def _check(t, shape):
-        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
-            raise ValueError("expected a contiguous float32 CUDA tensor")
+    def _check(t, shape, dtype=None):
+        dtype = dtype or torch.float32
+        if not (t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+            raise ValueError(f"expected a contiguous {dtype} CUDA tensor")
         if tuple(t.shape) != tuple(shape):
             raise ValueError(f"expected shape {tuple(shape)}, got {tuple(t.shape)}")
 
@@ -272,7 +305,7 @@ def clear_plans():
 # get_displacement (core/optical_flow.py:773-929)
 # --------------------------------------------------------------------------
 def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_level, levels, eta, a_smooth,
-             const_assumption, gnc_schedule, warping_steps, level_solver_backend):
+             const_assumption, gnc_schedule, warping_steps, level_solver_backend, precision="fp32"):
     const = resolve_const_assumption(const_assumption)
     if normalize_gnc_schedule(gnc_schedule) is not None:
         raise NotImplementedError("graduated non-convexity (gnc_schedule) is not implemented by the GB300 backend")
@@ -285,37 +318,40 @@ def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_l
     m, n = fixed.shape[:2]
     w = normalize_weight(weight, m, n, K)
     params = make_params(alpha, update_lag, iterations, min_level, levels, eta, a_smooth, a_data,
-                         ["gc", "gray"][const], K)
+                         ["gc", "gray"][const], K, precision=precision)
     return fixed, moving, w, params, m, n, K
 
 
 def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
                      a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None, weight=None,
-                     level_solver_backend=None, gnc_schedule=None, warping_steps=None):
+                     level_solver_backend=None, gnc_schedule=None, warping_steps=None, precision="fp32"):
     """Drop-in for pyflowreg.core.optical_flow.get_displacement on the GPU.
 
     Returns the (H, W, 2) float64 displacement, [..., 0] = u (columns),
-    [..., 1] = v (rows), like the reference.
+    [..., 1] = v (rows), like the reference.  ``precision`` ("fp32" fast path,
+    "fp64" reference precision and operation order) is the only argument the
+    reference does not have.
     """
     assert fixed.ndim == moving.ndim, (
         f"Fixed and moving must have same dimensions: fixed.shape={fixed.shape}, moving.shape={moving.shape}"
     )
     fixed, moving, w, params, m, n, K = _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations,
                                                  min_level, levels, eta, a_smooth, const_assumption, gnc_schedule,
-                                                 warping_steps, level_solver_backend)
+                                                 warping_steps, level_solver_backend, precision)
     flow = _run_host(params, fixed.reshape(m, n, K), moving.reshape(1, m, n, K), w, uv)
     return flow[0].astype(np.float64)
 
 
 def get_displacement_batch(fixed, moving_frames, alpha=(2, 2), update_lag=5, iterations=50, min_level=0,
                            levels=50, eta=0.8, a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None,
-                           weight=None, gnc_schedule=None, warping_steps=None, max_frames=None):
+                           weight=None, gnc_schedule=None, warping_steps=None, max_frames=None, precision="fp32"):
     """Many moving frames (T, H, W[, K]) against one fixed frame in one device
-    pass; returns (T, H, W, 2) float32 (the dtype the executors store)."""
+    pass; returns (T, H, W, 2) float32 (the dtype the executors store), float64
+    for precision="fp64"."""
     moving_frames = np.asarray(moving_frames)
     fixed, _, w, params, m, n, K = _prepare(fixed, moving_frames[0], weight, a_data, alpha, update_lag,
                                             iterations, min_level, levels, eta, a_smooth, const_assumption,
-                                            gnc_schedule, warping_steps, None)
+                                            gnc_schedule, warping_steps, None, precision)
     T = moving_frames.shape[0]
     return _run_host(params, fixed.reshape(m, n, K), moving_frames.reshape(T, m, n, K), w, uv, max_frames)
 

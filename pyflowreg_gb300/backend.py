@@ -27,14 +27,15 @@ SUPPORTED_EXECUTORS = {"sequential", EXECUTOR_NAME}
 
 
 def _factory(**backend_params):
-    """Backend factory: ``backend_params`` are accepted for API compatibility
-    (pyflowreg passes ``OFOptions.backend_params``); ``max_frames`` bounds the
-    device batch of one call."""
+    """Backend factory, called with ``OFOptions.backend_params``: ``device``
+    selects the CUDA device, ``precision`` is "fp32" (default) or "fp64"
+    (reference precision, the parity mode), ``max_frames`` bounds the device
+    batch of one call."""
     from functools import partial
 
     from . import api
 
-    unknown = set(backend_params) - {"max_frames", "device"}
+    unknown = set(backend_params) - {"max_frames", "device", "precision"}
     if unknown:
         raise ValueError(f"unknown backend_params for {BACKEND_NAME}: {sorted(unknown)}")
     dev = backend_params.get("device")
@@ -42,7 +43,7 @@ def _factory(**backend_params):
         import torch
 
         torch.cuda.set_device(torch.device(dev))
-    return partial(api.get_displacement)
+    return partial(api.get_displacement, precision=backend_params.get("precision", "fp32"))
 
 
 def register(executor: bool = True) -> None:

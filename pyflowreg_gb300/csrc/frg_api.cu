@@ -210,6 +210,7 @@ int ensure_remap_tables()
     float cub[128], lin[64];
     remap_tables(cub, lin);
     FRG_CUDA(upload_cubic_table(cub, lin));
+    FRG_CUDA(upload_cubic_table_x(cub));
     done = true;
     done_dev = dev;
     return FRG_OK;
@@ -244,6 +245,7 @@ struct LevelPlan {
     DevTables img, flow;  // full-res -> level, flow source -> level
     float* ref = nullptr;    // (K, h, w) reference level
     float* wdiag = nullptr;  // (K, D*P) weight level, diagonal-major
+    double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
 };
 
 // Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
@@ -309,6 +311,14 @@ struct frg_plan {
     float* ones = nullptr;    // (H, W, K) default weight
     float a_data[kMaxK] = {0};
     SorProfile prof;
+    // FP64 reference-order workspace (precision == FRG_FP64_REFERENCE)
+    double* xJ = nullptr;     // (T, 6, K, m*n)
+    double* xwp = nullptr;    // (T, K, m*n) weight * psi
+    double* xdu = nullptr;    // (T, m*n)
+    double* xdv = nullptr;    // (T, m*n)
+    double* xuv = nullptr;    // (T, 2, m*n)
+    double* xacc[2] = {nullptr, nullptr};  // (T, 2, h*w)
+    double a_data64[kMaxK] = {0};
 };
 
 namespace {
@@ -419,6 +429,8 @@ int check_params(const frg_params* p, int K)
         return fail(FRG_EUNSUPPORTED, "only the 'gc' and 'gray' constancy assumptions are supported");
     for (int k = 0; k < K; ++k)
         if (!(p->a_data[k] > 0.0)) return fail(FRG_EINVAL, "a_data must be > 0");
+    if (p->precision != FRG_FP32 && p->precision != FRG_FP64_REFERENCE)
+        return fail(FRG_EINVAL, "precision must be FRG_FP32 or FRG_FP64_REFERENCE");
     return FRG_OK;
 }
 
@@ -515,7 +527,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             frg_plan_destroy(pl);
             return fail(FRG_EINVAL, "degenerate pyramid level");
         }
-        if ((L.h + 31) / 32 * 32 > kMaxLane) {
+        if (params->precision == FRG_FP32 && (L.h + 31) / 32 * 32 > kMaxLane) {
             frg_plan_destroy(pl);
             return fail(FRG_EUNSUPPORTED, "frames taller than 512 rows are not supported yet");
         }
@@ -537,7 +549,11 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         HostTables fx = make_tables(L.fw, L.w, sigf), fy = make_tables(L.fh, L.h, sigf);
         if ((rc = upload_tables(pl, fx, L.w, fy, L.h, &L.flow))) { frg_plan_destroy(pl); return rc; }
         if ((rc = dev_alloc(pl, &L.ref, (size_t)channels * L.h * L.w))) { frg_plan_destroy(pl); return rc; }
-        if ((rc = dev_alloc(pl, &L.wdiag, (size_t)channels * L.g.D * L.g.P))) { frg_plan_destroy(pl); return rc; }
+        if (params->precision == FRG_FP64_REFERENCE)
+            rc = dev_alloc(pl, &L.wpad64, (size_t)channels * (L.h + 2) * (L.w + 2));
+        else
+            rc = dev_alloc(pl, &L.wdiag, (size_t)channels * L.g.D * L.g.P);
+        if (rc) { frg_plan_destroy(pl); return rc; }
         max_dp = std::max(max_dp, (size_t)L.g.D * L.g.P);
         max_hw = std::max(max_hw, (size_t)L.h * L.w);
         max_pad = std::max(max_pad, (size_t)(L.h + 2) * (L.w + 2));
@@ -551,13 +567,28 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     const size_t tmp_elems = T * std::max<size_t>(K, 2) * (size_t)height * width;
     if ((rc = dev_alloc(pl, &pl->tmp, tmp_elems)) || (rc = dev_alloc(pl, &pl->f2, T * K * max_hw)) ||
         (rc = dev_alloc(pl, &pl->warped, T * K * max_hw)) ||
-        (rc = dev_alloc(pl, &pl->J, T * 6 * K * max_dp)) || (rc = dev_alloc(pl, &pl->lap, T * 2 * max_dp)) ||
-        (rc = dev_alloc(pl, &pl->coef, T * 5 * max_dp)) || (rc = dev_alloc(pl, &pl->du, T * max_dp)) ||
-        (rc = dev_alloc(pl, &pl->dv, T * max_dp)) || (rc = dev_alloc(pl, &pl->uvpad, T * 2 * max_pad)) ||
-        (rc = dev_alloc(pl, &pl->uacc[0], T * 2 * max_hw)) || (rc = dev_alloc(pl, &pl->uacc[1], T * 2 * max_hw)) ||
         (rc = dev_alloc(pl, &pl->ones, K * (size_t)height * width))) {
         frg_plan_destroy(pl);
         return rc;
+    }
+    if (params->precision == FRG_FP64_REFERENCE) {
+        if ((rc = dev_alloc(pl, &pl->xJ, T * 6 * K * max_pad)) || (rc = dev_alloc(pl, &pl->xwp, T * K * max_pad)) ||
+            (rc = dev_alloc(pl, &pl->xdu, T * max_pad)) || (rc = dev_alloc(pl, &pl->xdv, T * max_pad)) ||
+            (rc = dev_alloc(pl, &pl->xuv, T * 2 * max_pad)) || (rc = dev_alloc(pl, &pl->xacc[0], T * 2 * max_hw)) ||
+            (rc = dev_alloc(pl, &pl->xacc[1], T * 2 * max_hw))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
+        for (int k = 0; k < channels; ++k) pl->a_data64[k] = params->a_data[k];
+    } else {
+        if ((rc = dev_alloc(pl, &pl->J, T * 6 * K * max_dp)) || (rc = dev_alloc(pl, &pl->lap, T * 2 * max_dp)) ||
+            (rc = dev_alloc(pl, &pl->coef, T * 5 * max_dp)) || (rc = dev_alloc(pl, &pl->du, T * max_dp)) ||
+            (rc = dev_alloc(pl, &pl->dv, T * max_dp)) || (rc = dev_alloc(pl, &pl->uvpad, T * 2 * max_pad)) ||
+            (rc = dev_alloc(pl, &pl->uacc[0], T * 2 * max_hw)) ||
+            (rc = dev_alloc(pl, &pl->uacc[1], T * 2 * max_hw))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
     }
     {
         std::vector<float> ones(K * (size_t)height * width, 1.0f / (float)channels);
@@ -624,6 +655,28 @@ int frg_iteration_passes(int iterations, int update_lag, int max_passes, int* G,
 
 int frg_plan_num_levels(const frg_plan* plan) { return plan ? (int)plan->levels.size() : 0; }
 
+int frg_plan_set_level_tables(frg_plan* plan, int level, int kind, int taps, const int* ix, const float* wx,
+                              const int* iy, const float* wy)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    if (kind != 0 && kind != 1) return fail(FRG_EINVAL, "kind must be 0 (image) or 1 (flow)");
+    if (!ix || !wx || !iy || !wy) return fail(FRG_EINVAL, "NULL table");
+    const LevelPlan& L = plan->levels[level];
+    const DevTables& d = kind == 0 ? L.img : L.flow;
+    const int in_h = kind == 0 ? plan->H : L.fh, in_w = kind == 0 ? plan->W : L.fw;
+    if (taps != d.P) return fail(FRG_EINVAL, "tap count differs from the plan's");
+    const size_t nx = (size_t)L.w * taps, ny = (size_t)L.h * taps;
+    for (size_t i = 0; i < nx; ++i)
+        if (ix[i] < 0 || ix[i] >= in_w) return fail(FRG_EINVAL, "column index out of range");
+    for (size_t i = 0; i < ny; ++i)
+        if (iy[i] < 0 || iy[i] >= in_h) return fail(FRG_EINVAL, "row index out of range");
+    FRG_CUDA(cudaMemcpy(d.ix, ix, nx * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d.wx, wx, nx * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d.iy, iy, ny * 4, cudaMemcpyHostToDevice));
+    FRG_CUDA(cudaMemcpy(d.wy, wy, ny * 4, cudaMemcpyHostToDevice));
+    return FRG_OK;
+}
+
 int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double* alpha_x, double* alpha_y)
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
@@ -641,6 +694,21 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
     cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
     const float* wsrc = weight ? weight : pl->ones;
+    if (pl->p.precision == FRG_FP64_REFERENCE) {
+        for (LevelPlan& L : pl->levels) {
+            const long long hw = (long long)L.h * L.w, mn = (long long)(L.h + 2) * (L.w + 2);
+            FRG_LAUNCH(launch_x_resize_h_f(fixed, 0, 1, (long long)W * K, K, 1, K, H, pl->tmp, L.w, L.img.ix,
+                                           L.img.wx, L.img.P, st));
+            FRG_LAUNCH(launch_x_resize_v_f(pl->tmp, 1, K, H, L.w, L.ref, 0, hw, L.w, L.h, 0, L.img.iy, L.img.wy,
+                                           L.img.P, st));
+            FRG_LAUNCH(launch_x_resize_h_f(wsrc, 0, 1, (long long)W * K, K, 1, K, H, pl->tmp, L.w, L.img.ix,
+                                           L.img.wx, L.img.P, st));
+            FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, 1, K, H, L.w, L.wpad64, 0, mn, L.w + 2, L.h, 2, L.img.iy,
+                                           L.img.wy, L.img.P, st));
+        }
+        pl->has_ref = true;
+        return FRG_OK;
+    }
     for (LevelPlan& L : pl->levels) {
         // reference level: resize(fixed) (core/optical_flow.py:519)
         View src = view(fixed, 0, 1, (long long)W * K, K);
@@ -665,6 +733,8 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
     if (!pl || !moving || !flow_out) return fail(FRG_EINVAL, "NULL argument");
     if (!pl->has_ref) return fail(FRG_EINVAL, "frg_set_reference has not been called");
     if (T < 1 || T > pl->max_T) return fail(FRG_EINVAL, "n_frames out of range for this plan");
+    if (pl->p.precision != FRG_FP32)
+        return fail(FRG_EINVAL, "this plan computes in fp64: use frg_get_displacement_f64");
     cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
     const long long fsz = (long long)H * W * K;
@@ -736,6 +806,75 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
             cur = nxt;
         }
         FRG_LAUNCH(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
+        prev = &L;
+    }
+    return FRG_OK;
+}
+
+int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out,
+                             void* stream)
+{
+    if (!pl || !moving || !flow_out) return fail(FRG_EINVAL, "NULL argument");
+    if (!pl->has_ref) return fail(FRG_EINVAL, "frg_set_reference has not been called");
+    if (T < 1 || T > pl->max_T) return fail(FRG_EINVAL, "n_frames out of range for this plan");
+    if (pl->p.precision != FRG_FP64_REFERENCE)
+        return fail(FRG_EINVAL, "this plan computes in fp32: use frg_get_displacement");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int H = pl->H, W = pl->W, K = pl->K;
+    const long long fsz = (long long)H * W * K;
+    int cur = 0;
+    const LevelPlan* prev = nullptr;
+    for (size_t li = 0; li < pl->levels.size(); ++li) {
+        const LevelPlan& L = pl->levels[li];
+        const int h = L.h, w = L.w;
+        const long long hw = (long long)h * w, mn = (long long)(h + 2) * (w + 2);
+        // moving level images (numba typing of the resize)
+        FRG_LAUNCH(launch_x_resize_h_f(moving, fsz, 1, (long long)W * K, K, T, K, H, pl->tmp, w, L.img.ix, L.img.wx,
+                                       L.img.P, st));
+        FRG_LAUNCH(launch_x_resize_v_f(pl->tmp, T, K, H, w, pl->f2, K * hw, hw, w, h, 0, L.img.iy, L.img.wy, L.img.P,
+                                       st));
+        // flow with its edge ring
+        long long uv_fs;
+        if (L.top) {
+            uv_fs = 0;
+            if (uv_init) {
+                FRG_LAUNCH(launch_x_resize_h_f(uv_init, 0, 1, (long long)W * 2, 2, 1, 2, H, pl->tmp, w, L.flow.ix,
+                                               L.flow.wx, L.flow.P, st));
+                FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, 1, 2, H, w, pl->xuv, 0, mn, w + 2, h, 1, L.flow.iy, L.flow.wy,
+                                               L.flow.P, st));
+            } else {
+                FRG_CUDA(cudaMemsetAsync(pl->xuv, 0, sizeof(double) * 2 * mn, st));
+            }
+        } else {
+            uv_fs = 2 * mn;
+            const long long phw = (long long)prev->h * prev->w;
+            FRG_LAUNCH(launch_x_resize_h_d(pl->xacc[cur], 2 * phw, phw, prev->w, 1, T, 2, prev->h, pl->tmp, w,
+                                           L.flow.ix, L.flow.wx, L.flow.P, st));
+            FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, T, 2, prev->h, w, pl->xuv, 2 * mn, mn, w + 2, h, 1, L.flow.iy,
+                                           L.flow.wy, L.flow.P, st));
+        }
+        const float* img2 = pl->f2;
+        if (!L.top) {
+            FRG_LAUNCH(launch_x_warp(pl->f2, L.ref, pl->xuv, pl->xuv + mn, uv_fs, T, K, h, w, L.h_col, L.h_row,
+                                     pl->warped, st));
+            img2 = pl->warped;
+        }
+        FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1, pl->p.const_assumption,
+                                   pl->xJ, st));
+        FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv, pl->xwp, T, K, h, w,
+                                L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations, pl->p.update_lag,
+                                pl->a_data64, pl->p.omega, st));
+        const int do_median = std::min(h, w) > 5 ? 1 : 0;
+        const bool last = (li + 1 == pl->levels.size());
+        if (last) {
+            FRG_LAUNCH(launch_x_median_accum(pl->xdu, pl->xdv, pl->xuv, pl->xuv + mn, uv_fs, T, h, w, do_median,
+                                             flow_out, flow_out + 1, (long long)H * W * 2, (long long)W * 2, 2, st));
+        } else {
+            const int nxt = cur ^ 1;
+            FRG_LAUNCH(launch_x_median_accum(pl->xdu, pl->xdv, pl->xuv, pl->xuv + mn, uv_fs, T, h, w, do_median,
+                                             pl->xacc[nxt], pl->xacc[nxt] + hw, 2 * hw, w, 1, st));
+            cur = nxt;
+        }
         prev = &L;
     }
     return FRG_OK;

@@ -1,0 +1,490 @@
+// FP64 reference-order kernels (parity mode).
+//
+// These follow the numba typing of pyflowreg's arithmetic operation by
+// operation -- float32 images and resize products, float64 accumulators,
+// tensors and solver -- with explicit round-to-nearest intrinsics so that no
+// multiply-add is contracted.  They share the schedule, the tap tables and the
+// exact lexicographic SOR order with the FP32 path; their purpose is to show
+// that the GB300 pipeline reproduces the reference's result to within the
+// reference's own rounding when it computes in the reference's precision.
+// Layout: row-major planes, the level arrays with their one-pixel ring
+// (m = h + 2 rows, n = w + 2 columns), like the reference's numpy arrays.
+#include "frg_internal.h"
+
+#include <math.h>
+
+namespace frg {
+
+__device__ __forceinline__ int xclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// Resize with numba typing (util/resize_util.py:116-141): float32 input and
+// products, float64 accumulator, float32 result (stored as float or double).
+// ---------------------------------------------------------------------------
+template <typename Tin>
+__global__ void kx_resize_h(const Tin* __restrict__ src, long long fs, long long ps, long long rs, long long cs,
+                            int n_planes, int ih, float* __restrict__ dst, int ow, const int32_t* __restrict__ ix,
+                            const float* __restrict__ wx, int P)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int fp = blockIdx.z;
+    if (x >= ow) return;
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    const Tin* row = src + f * fs + pl * ps + (long long)y * rs;
+    double s = 0.0;
+    for (int p = 0; p < P; ++p) {
+        const float a = (float)row[(long long)ix[(long long)x * P + p] * cs];
+        s = dadd(s, (double)__fmul_rn(a, wx[(long long)x * P + p]));
+    }
+    dst[((long long)fp * ih + y) * ow + x] = (float)s;
+}
+
+// ring: 0 none, 1 edge-replicated ring (add_boundary), 2 zero ring
+// (cv2.copyMakeBorder BORDER_CONSTANT 0, core/optical_flow.py:565-568).
+template <typename Tout>
+__global__ void kx_resize_v(const float* __restrict__ src, int n_planes, int ih, int ow, Tout* __restrict__ dst,
+                            long long fs, long long ps, long long rs, int oh, int ring,
+                            const int32_t* __restrict__ iy, const float* __restrict__ wy, int P)
+{
+    const int pad = ring ? 1 : 0;
+    const int xo = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yo = blockIdx.y;
+    const int fp = blockIdx.z;
+    if (xo >= ow + 2 * pad) return;
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    Tout* out = dst + f * fs + pl * ps + (long long)yo * rs + xo;
+    const bool inside = xo >= pad && xo < ow + pad && yo >= pad && yo < oh + pad;
+    if (!inside && ring == 2) {
+        *out = (Tout)0;
+        return;
+    }
+    const int x = xclamp(xo - pad, 0, ow - 1);
+    const int y = xclamp(yo - pad, 0, oh - 1);
+    const float* col = src + (long long)fp * ih * ow + x;
+    double s = 0.0;
+    for (int p = 0; p < P; ++p)
+        s = dadd(s, (double)__fmul_rn(col[(long long)iy[(long long)y * P + p] * ow], wy[(long long)y * P + p]));
+    *out = (Tout)(float)s;
+}
+
+cudaError_t launch_x_resize_h_f(const float* src, long long fs, long long ps, long long rs, long long cs,
+                                int n_frames, int n_planes, int ih, float* dst, int ow, const int32_t* ix,
+                                const float* wx, int P, cudaStream_t st)
+{
+    dim3 blk(128), grd((ow + 127) / 128, ih, n_frames * n_planes);
+    kx_resize_h<float><<<grd, blk, 0, st>>>(src, fs, ps, rs, cs, n_planes, ih, dst, ow, ix, wx, P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_x_resize_h_d(const double* src, long long fs, long long ps, long long rs, long long cs,
+                                int n_frames, int n_planes, int ih, float* dst, int ow, const int32_t* ix,
+                                const float* wx, int P, cudaStream_t st)
+{
+    dim3 blk(128), grd((ow + 127) / 128, ih, n_frames * n_planes);
+    kx_resize_h<double><<<grd, blk, 0, st>>>(src, fs, ps, rs, cs, n_planes, ih, dst, ow, ix, wx, P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_x_resize_v_f(const float* src, int n_frames, int n_planes, int ih, int ow, float* dst,
+                                long long fs, long long ps, long long rs, int oh, int ring, const int32_t* iy,
+                                const float* wy, int P, cudaStream_t st)
+{
+    const int pad = ring ? 1 : 0;
+    dim3 blk(128), grd((ow + 2 * pad + 127) / 128, oh + 2 * pad, n_frames * n_planes);
+    kx_resize_v<float><<<grd, blk, 0, st>>>(src, n_planes, ih, ow, dst, fs, ps, rs, oh, ring, iy, wy, P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_x_resize_v_d(const float* src, int n_frames, int n_planes, int ih, int ow, double* dst,
+                                long long fs, long long ps, long long rs, int oh, int ring, const int32_t* iy,
+                                const float* wy, int P, cudaStream_t st)
+{
+    const int pad = ring ? 1 : 0;
+    dim3 blk(128), grd((ow + 2 * pad + 127) / 128, oh + 2 * pad, n_frames * n_planes);
+    kx_resize_v<double><<<grd, blk, 0, st>>>(src, n_planes, ih, ow, dst, fs, ps, rs, oh, ring, iy, wy, P);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Warp (core/warping.py:160-234) with float64 flow: map = float32(x + u/h_col),
+// float64 accumulation of float32 weights, float32 result.
+// u, v: padded (m, n) planes, frame stride uv_fs.  f2: (T, K, h, w) float,
+// f1: (K, h, w) float shared, out (T, K, h, w) float.
+// ---------------------------------------------------------------------------
+__constant__ float cx_cubic[32 * 4];
+
+cudaError_t upload_cubic_table_x(const float* tab128)
+{
+    return cudaMemcpyToSymbol(cx_cubic, tab128, sizeof(float) * 128);
+}
+
+__global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ f1, const double* __restrict__ u,
+                        const double* __restrict__ v, long long uv_fs, int K, int h, int w, double h_col,
+                        double h_row, float* __restrict__ out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const long long n = w + 2;
+    const long long hw = (long long)h * w;
+    const long long o = (long long)(y + 1) * n + (x + 1);
+    const float mx = (float)dadd((double)x, ddiv(u[f * uv_fs + o], h_col));
+    const float my = (float)dadd((double)y, ddiv(v[f * uv_fs + o], h_row));
+    const bool oob = (mx < 0.0f) || (mx >= (float)w) || (my < 0.0f) || (my >= (float)h);
+    for (int k = 0; k < K; ++k) {
+        float* dst = out + ((long long)f * K + k) * hw + (long long)y * w + x;
+        if (oob) {
+            *dst = f1[(long long)k * hw + (long long)y * w + x];
+            continue;
+        }
+        const float cx = fminf(fmaxf(mx, 0.0f), (float)(w - 1));
+        const float cy = fminf(fmaxf(my, 0.0f), (float)(h - 1));
+        const int X = __float2int_rn(cx * 32.0f), Y = __float2int_rn(cy * 32.0f);
+        const int ix = X >> 5, fx = X & 31, iy = Y >> 5, fy = Y & 31;
+        const float* src = f2 + ((long long)f * K + k) * hw;
+        double acc = 0.0;
+        for (int i = 0; i < 4; ++i) {
+            const int yy = xclamp(iy - 1 + i, 0, h - 1);
+            for (int j = 0; j < 4; ++j) {
+                const int xx = xclamp(ix - 1 + j, 0, w - 1);
+                const float w2 = __fmul_rn(cx_cubic[fy * 4 + i], cx_cubic[fx * 4 + j]);
+                acc = dadd(acc, dmul((double)src[(long long)yy * w + xx], (double)w2));
+            }
+        }
+        *dst = (float)acc;
+    }
+}
+
+cudaError_t launch_x_warp(const float* f2, const float* f1, const double* u, const double* v, long long uv_fs,
+                          int n_frames, int K, int h, int w, double h_col, double h_row, float* out, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    kx_warp<<<grd, blk, 0, st>>>(f2, f1, u, v, uv_fs, K, h, w, h_col, h_row, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Motion tensor (core/optical_flow.py:73-228), the oracle's arithmetic:
+// float64, except that the derivatives of the warped image are float32
+// (numpy keeps a float32 array float32 under a Python-float spacing) when
+// f2_f32 is set (every level below the top).
+// f1: (K, h, w) float shared; f2: (T, K, h, w) float; J: (T, 6, K, m*n) double
+// with a zero ring.
+// ---------------------------------------------------------------------------
+__global__ void kx_tensor(const float* __restrict__ f1, const float* __restrict__ f2, int K, int h, int w,
+                          double hy, double hx, int f2_f32, int gray, double* __restrict__ J)
+{
+    const int xo = blockIdx.x * blockDim.x + threadIdx.x;  // padded column
+    const int yo = blockIdx.y;                             // padded row
+    const int f = blockIdx.z;
+    const int n = w + 2, m = h + 2;
+    if (xo >= n) return;
+    const long long mn = (long long)m * n;
+    const long long hw = (long long)h * w;
+    const long long o = (long long)yo * n + xo;
+    const bool ring = xo == 0 || xo == n - 1 || yo == 0 || yo == m - 1;
+    const double h2x = dmul(2.0, hx), h2y = dmul(2.0, hy), hxx = dmul(hx, hx), hyy = dmul(hy, hy);
+    const float hx_f = (float)hx, hy_f = (float)hy, h2x_f = (float)h2x, h2y_f = (float)h2y;
+    const float hxx_f = (float)hxx, hyy_f = (float)hyy;
+    for (int k = 0; k < K; ++k) {
+        double* Jk = J + (long long)f * 6 * K * mn + (long long)k * mn;
+        if (ring) {
+            for (int q = 0; q < 6; ++q) Jk[(long long)q * K * mn + o] = 0.0;
+            continue;
+        }
+        const float* a = f1 + (long long)k * hw;
+        const float* b = f2 + ((long long)f * K + k) * hw;
+        // padded (yy, xx) -> unpadded clamp
+        auto A = [&](int yy, int xx) { return (double)a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+        auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+        // numpy.gradient of the padded arrays at an interior padded position
+        auto gx1 = [&](int yy, int xx) { return ddiv(dsub(A(yy, xx + 1), A(yy, xx - 1)), h2x); };
+        auto gy1 = [&](int yy, int xx) { return ddiv(dsub(A(yy + 1, xx), A(yy - 1, xx)), h2y); };
+        auto gx2 = [&](int yy, int xx) {
+            if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), h2x_f);
+            return ddiv(dsub((double)Bf(yy, xx + 1), (double)Bf(yy, xx - 1)), h2x);
+        };
+        auto gy2 = [&](int yy, int xx) {
+            if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), h2y_f);
+            return ddiv(dsub((double)Bf(yy + 1, xx), (double)Bf(yy - 1, xx)), h2y);
+        };
+        // fx, fy, ft re-padded from the interior: clamp the padded index to [1, h] x [1, w]
+        auto FX = [&](int yy, int xx) {
+            yy = xclamp(yy, 1, h);
+            xx = xclamp(xx, 1, w);
+            return dmul(0.5, dadd(gx1(yy, xx), gx2(yy, xx)));
+        };
+        auto FT = [&](int yy, int xx) {
+            yy = xclamp(yy, 1, h);
+            xx = xclamp(xx, 1, w);
+            return dsub((double)Bf(yy, xx), A(yy, xx));
+        };
+        double j11, j22, j33, j12, j13, j23;
+        if (gray) {
+            const double fxv = FX(yo, xo);
+            const double fyv = dmul(0.5, dadd(gy1(yo, xo), gy2(yo, xo)));
+            const double ftv = FT(yo, xo);
+            j11 = dmul(fxv, fxv); j22 = dmul(fyv, fyv); j33 = dmul(ftv, ftv);
+            j12 = dmul(fxv, fyv); j13 = dmul(fxv, ftv); j23 = dmul(fyv, ftv);
+        } else {
+            const double fxy = ddiv(dsub(FX(yo + 1, xo), FX(yo - 1, xo)), h2y);
+            const double fxt = ddiv(dsub(FT(yo, xo + 1), FT(yo, xo - 1)), h2x);
+            const double fyt = ddiv(dsub(FT(yo + 1, xo), FT(yo - 1, xo)), h2y);
+            const double fxx1 = ddiv(dadd(dsub(A(yo, xo - 1), dmul(2.0, A(yo, xo))), A(yo, xo + 1)), hxx);
+            const double fyy1 = ddiv(dadd(dsub(A(yo - 1, xo), dmul(2.0, A(yo, xo))), A(yo + 1, xo)), hyy);
+            double fxx2, fyy2;
+            if (f2_f32) {
+                fxx2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)), hxx_f);
+                fyy2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)), hyy_f);
+            } else {
+                fxx2 = ddiv(dadd(dsub((double)Bf(yo, xo - 1), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo, xo + 1)), hxx);
+                fyy2 = ddiv(dadd(dsub((double)Bf(yo - 1, xo), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo + 1, xo)), hyy);
+            }
+            const double fxx = dmul(0.5, dadd(fxx1, fxx2));
+            const double fyy = dmul(0.5, dadd(fyy1, fyy2));
+            const double sx = __dsqrt_rn(dadd(dmul(fxx, fxx), dmul(fxy, fxy)));
+            const double sy = __dsqrt_rn(dadd(dmul(fxy, fxy), dmul(fyy, fyy)));
+            const double reg_x = ddiv(1.0, dadd(dmul(sx, sx), 1e-6));
+            const double reg_y = ddiv(1.0, dadd(dmul(sy, sy), 1e-6));
+            j11 = dadd(dmul(reg_x, dmul(fxx, fxx)), dmul(reg_y, dmul(fxy, fxy)));
+            j22 = dadd(dmul(reg_x, dmul(fxy, fxy)), dmul(reg_y, dmul(fyy, fyy)));
+            j33 = dadd(dmul(reg_x, dmul(fxt, fxt)), dmul(reg_y, dmul(fyt, fyt)));
+            j12 = dadd(dmul(dmul(reg_x, fxx), fxy), dmul(dmul(reg_y, fxy), fyy));
+            j13 = dadd(dmul(dmul(reg_x, fxx), fxt), dmul(dmul(reg_y, fxy), fyt));
+            j23 = dadd(dmul(dmul(reg_x, fxy), fxt), dmul(dmul(reg_y, fyy), fyt));
+        }
+        const long long qs = (long long)K * mn;
+        Jk[0 * qs + o] = j11;
+        Jk[1 * qs + o] = j22;
+        Jk[2 * qs + o] = j33;
+        Jk[3 * qs + o] = j12;
+        Jk[4 * qs + o] = j13;
+        Jk[5 * qs + o] = j23;
+    }
+    (void)hx_f;
+    (void)hy_f;
+}
+
+cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int K, int h, int w, double hy, double hx,
+                            int f2_f32, int gray, double* J, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 2 + 127) / 128, h + 2, n_frames);
+    kx_tensor<<<grd, blk, 0, st>>>(f1, f2, K, h, w, hy, hx, f2_f32, gray, J);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// compute_flow (core/level_solver.py:158-369) in its own order and arithmetic,
+// all iterations in one launch.  One CTA per frame, threads over rows; the
+// exact lexicographic order is kept by the wavefront schedule of the FP32
+// solver (pixel (r, c) of iteration t at step r + c + 2t), here on global
+// memory so that any number of iterations is pipelined.  The psi update of a
+// tick iteration is pixel-local, so it is applied to each pixel just before
+// its own update, from its own (iteration t-1) du, dv -- the same values the
+// reference's full-array psi pass reads.  __syncthreads orders the global
+// stores of one step before the loads of the next within the CTA.
+// J: (T, 6, K, m*n); W: (K, m*n) shared; u, v: (T, m*n) (frame stride uv_fs);
+// du, dv: (T, m*n); wp: (T, K, m*n) scratch holding weight * psi.
+// ---------------------------------------------------------------------------
+struct XAData { double a[kMaxK]; };
+
+__global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ W, const double* __restrict__ u,
+                       const double* __restrict__ v, long long uv_fs, double* du_g, double* dv_g, double* wp_g,
+                       int K, int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
+                       int update_lag, XAData ad, double omega)
+{
+    const int f = blockIdx.x;
+    const int n = w + 2, m = h + 2;
+    const long long mn = (long long)m * n;
+    const double* Jf = J + (long long)f * 6 * K * mn;
+    const double* uf = u + f * uv_fs;
+    const double* vf = v + f * uv_fs;
+    double* du = du_g + (long long)f * mn;
+    double* dv = dv_g + (long long)f * mn;
+    double* wp = wp_g + (long long)f * K * mn;
+    const long long qs = (long long)K * mn;
+    for (long long i = threadIdx.x; i < mn; i += blockDim.x) {
+        du[i] = 0.0;
+        dv[i] = 0.0;
+        for (int k = 0; k < K; ++k) wp[(long long)k * mn + i] = W[(long long)k * mn + i];  // psi = 1
+    }
+    __syncthreads();
+    const double tx = ddiv(alpha_x, dmul(hx, hx));
+    const double ty = ddiv(alpha_y, dmul(hy, hy));
+    const double one_m_omega = dsub(1.0, omega);
+    const int nsteps = (h - 1) + (w - 1) + 2 * (iterations - 1) + 1;
+    for (int s = 0; s < nsteps; ++s) {
+        for (int r = threadIdx.x; r < h; r += blockDim.x) {
+            for (int t = 0; t < iterations; ++t) {
+                const int c = s - r - 2 * t;
+                if (c < 0) break;
+                if (c >= w) continue;
+                const long long o = (long long)(r + 1) * n + (c + 1);
+                const double duc = du[o], dvc = dv[o];
+                if ((t + 1) % update_lag == 0) {
+                    // core/level_solver.py:230-246 (J23*dv appears twice, as in the reference)
+                    for (int k = 0; k < K; ++k) {
+                        const long long ok = (long long)k * mn + o;
+                        double val = dmul(dmul(Jf[ok], duc), duc);
+                        val = dadd(val, dmul(dmul(Jf[qs + ok], dvc), dvc));
+                        val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
+                        val = dadd(val, dmul(dmul(dmul(2.0, Jf[3 * qs + ok]), duc), dvc));
+                        val = dadd(val, dmul(dmul(2.0, Jf[4 * qs + ok]), duc));
+                        val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
+                        val = dadd(val, Jf[2 * qs + ok]);
+                        if (val < 0.0) val = 0.0;
+                        const double psi = dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0)));
+                        wp[ok] = dmul(W[ok], psi);
+                    }
+                }
+                // neighbours; across the level border the Neumann copy equals the pixel's own old value
+                const double duL = c > 0 ? du[o - 1] : duc, dvL = c > 0 ? dv[o - 1] : dvc;
+                const double duR = c < w - 1 ? du[o + 1] : duc, dvR = c < w - 1 ? dv[o + 1] : dvc;
+                const double duD = r < h - 1 ? du[o + n] : duc, dvD = r < h - 1 ? dv[o + n] : dvc;
+                const double duU = r > 0 ? du[o - n] : duc, dvU = r > 0 ? dv[o - n] : dvc;
+                const double uc = uf[o], vc = vf[o];
+                double num_u = 0.0, num_v = 0.0, den_u = 0.0, den_v = 0.0;
+                // left, right, down, up (core/level_solver.py:318-340)
+                num_u = dadd(num_u, dmul(tx, dsub(dadd(uf[o - 1], duL), uc)));
+                num_v = dadd(num_v, dmul(tx, dsub(dadd(vf[o - 1], dvL), vc)));
+                den_u = dadd(den_u, tx);
+                den_v = dadd(den_v, tx);
+                num_u = dadd(num_u, dmul(tx, dsub(dadd(uf[o + 1], duR), uc)));
+                num_v = dadd(num_v, dmul(tx, dsub(dadd(vf[o + 1], dvR), vc)));
+                den_u = dadd(den_u, tx);
+                den_v = dadd(den_v, tx);
+                num_u = dadd(num_u, dmul(ty, dsub(dadd(uf[o + n], duD), uc)));
+                num_v = dadd(num_v, dmul(ty, dsub(dadd(vf[o + n], dvD), vc)));
+                den_u = dadd(den_u, ty);
+                den_v = dadd(den_v, ty);
+                num_u = dadd(num_u, dmul(ty, dsub(dadd(uf[o - n], duU), uc)));
+                num_v = dadd(num_v, dmul(ty, dsub(dadd(vf[o - n], dvU), vc)));
+                den_u = dadd(den_u, ty);
+                den_v = dadd(den_v, ty);
+                for (int k = 0; k < K; ++k) {
+                    const long long ok = (long long)k * mn + o;
+                    const double wpk = wp[ok];
+                    num_u = dsub(num_u, dmul(wpk, dadd(Jf[4 * qs + ok], dmul(Jf[3 * qs + ok], dvc))));
+                    den_u = dadd(den_u, dmul(wpk, Jf[ok]));
+                    den_v = dadd(den_v, dmul(wpk, Jf[qs + ok]));
+                }
+                const double du_kp1 = den_u != 0.0 ? ddiv(num_u, den_u) : 0.0;
+                const double dun = dadd(dmul(one_m_omega, duc), dmul(omega, du_kp1));
+                double num_v2 = num_v;
+                for (int k = 0; k < K; ++k) {
+                    const long long ok = (long long)k * mn + o;
+                    num_v2 = dsub(num_v2, dmul(wp[ok], dadd(Jf[5 * qs + ok], dmul(Jf[3 * qs + ok], dun))));
+                }
+                const double dv_kp1 = den_v != 0.0 ? ddiv(num_v2, den_v) : 0.0;
+                const double dvn = dadd(dmul(one_m_omega, dvc), dmul(omega, dv_kp1));
+                du[o] = dun;
+                dv[o] = dvn;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
+                         double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
+                         double alpha_y, double hx, double hy, int iterations, int update_lag,
+                         const double* a_data, double omega, cudaStream_t st)
+{
+    XAData ad;
+    for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0;
+    const int threads = h >= 512 ? 512 : ((h + 31) / 32) * 32;
+    kx_sor<<<n_frames, threads, 0, st>>>(J, W, u, v, uv_fs, du, dv, wp, K, h, w, alpha_x, alpha_y, hx, hy,
+                                         iterations, update_lag, ad, omega);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Median (scipy "mirror", exact selection) and accumulate in float64
+// (core/optical_flow.py:607-611).  du, dv, u, v: padded (m, n) planes; output
+// u + du, v + dv interiors with strides (frame, row, col) in elements.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dswap(double& x, double& y)
+{
+    const double lo = fmin(x, y), hi = fmax(x, y);
+    x = lo;
+    y = hi;
+}
+
+__device__ double median25d(double v[25])
+{
+    double t[14];
+#pragma unroll
+    for (int i = 0; i < 14; ++i) t[i] = v[i];
+#pragma unroll
+    for (int round = 0; round < 11; ++round) {
+        const int lo = round;
+#pragma unroll
+        for (int i = lo + 1; i < 14; ++i) dswap(t[lo], t[i]);
+#pragma unroll
+        for (int i = lo + 1; i < 13; ++i) dswap(t[i], t[13]);
+        t[13] = v[14 + round];
+    }
+    dswap(t[11], t[12]);
+    dswap(t[12], t[13]);
+    dswap(t[11], t[12]);
+    return t[12];
+}
+
+__global__ void kx_median_accum(const double* __restrict__ du, const double* __restrict__ dv,
+                                const double* __restrict__ u, const double* __restrict__ v, long long uv_fs, int h,
+                                int w, int do_median, double* ou, double* ov, long long o_fs, long long o_rs,
+                                long long o_cs)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const long long n = w + 2, mn = (long long)(h + 2) * n;
+    const double* duf = du + (long long)f * mn;
+    const double* dvf = dv + (long long)f * mn;
+    double mu, mv;
+    if (do_median) {
+        double a[25], b[25];
+        int q = 0;
+        for (int dy = -2; dy <= 2; ++dy) {
+            int yy = y + dy;
+            if (yy < 0) yy = -yy;
+            if (yy >= h) yy = 2 * (h - 1) - yy;
+            for (int dx = -2; dx <= 2; ++dx) {
+                int xx = x + dx;
+                if (xx < 0) xx = -xx;
+                if (xx >= w) xx = 2 * (w - 1) - xx;
+                const long long o = (long long)(yy + 1) * n + xx + 1;
+                a[q] = duf[o];
+                b[q] = dvf[o];
+                ++q;
+            }
+        }
+        mu = median25d(a);
+        mv = median25d(b);
+    } else {
+        const long long o = (long long)(y + 1) * n + x + 1;
+        mu = duf[o];
+        mv = dvf[o];
+    }
+    const long long oc = (long long)(y + 1) * n + x + 1;
+    ou[f * o_fs + y * o_rs + x * o_cs] = dadd(u[f * uv_fs + oc], mu);
+    ov[f * o_fs + y * o_rs + x * o_cs] = dadd(v[f * uv_fs + oc], mv);
+}
+
+cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
+                                  long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
+                                  long long o_fs, long long o_rs, long long o_cs, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    kx_median_accum<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
+    return cudaGetLastError();
+}
+
+}  // namespace frg

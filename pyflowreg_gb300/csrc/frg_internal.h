@@ -65,4 +65,30 @@ cudaError_t launch_median_accum(const float* du, const float* dv, long long st_f
                                 cudaStream_t st);
 cudaError_t upload_cubic_table(const float* tab128, const float* lin64);
 
+// FP64 reference-order kernels (frg_exact.cu).
+cudaError_t upload_cubic_table_x(const float* tab128);
+cudaError_t launch_x_resize_h_f(const float* src, long long fs, long long ps, long long rs, long long cs,
+                                int n_frames, int n_planes, int ih, float* dst, int ow, const int32_t* ix,
+                                const float* wx, int P, cudaStream_t st);
+cudaError_t launch_x_resize_h_d(const double* src, long long fs, long long ps, long long rs, long long cs,
+                                int n_frames, int n_planes, int ih, float* dst, int ow, const int32_t* ix,
+                                const float* wx, int P, cudaStream_t st);
+cudaError_t launch_x_resize_v_f(const float* src, int n_frames, int n_planes, int ih, int ow, float* dst,
+                                long long fs, long long ps, long long rs, int oh, int ring, const int32_t* iy,
+                                const float* wy, int P, cudaStream_t st);
+cudaError_t launch_x_resize_v_d(const float* src, int n_frames, int n_planes, int ih, int ow, double* dst,
+                                long long fs, long long ps, long long rs, int oh, int ring, const int32_t* iy,
+                                const float* wy, int P, cudaStream_t st);
+cudaError_t launch_x_warp(const float* f2, const float* f1, const double* u, const double* v, long long uv_fs,
+                          int n_frames, int K, int h, int w, double h_col, double h_row, float* out, cudaStream_t st);
+cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int K, int h, int w, double hy, double hx,
+                            int f2_f32, int gray, double* J, cudaStream_t st);
+cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
+                         double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
+                         double alpha_y, double hx, double hy, int iterations, int update_lag,
+                         const double* a_data, double omega, cudaStream_t st);
+cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
+                                  long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
+                                  long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
+
 }  // namespace frg

@@ -96,3 +96,31 @@ def test_iteration_passes(iterations, lag):
     got = list(zip(G, M))
     assert got == _passes_model(iterations, lag)
     assert sum(G) == iterations
+
+
+@pytest.mark.parametrize("in_len,out_len", [(512, 9), (512, 410), (256, 205), (410, 512), (37, 30), (1024, 11),
+                                            (72, 58), (9, 11)])
+def test_host_tables_equal_oracle_bit_for_bit(oracle, in_len, out_len):
+    """The plan's tables (pyflowreg_gb300.tables, uploaded into every plan) are
+    the reference's numpy construction: identical to the oracle's, bit for bit."""
+    from pyflowreg_gb300 import tables
+
+    sig = tables.sigma_for((in_len, in_len), (out_len, out_len))
+    assert sig == oracle.sigma_for((in_len, in_len), (out_len, out_len))
+    ix, wx = tables.resize_tables(in_len, out_len, sig)
+    iy, wy = oracle.resize_tables(in_len, out_len, sig, "numba")
+    np.testing.assert_array_equal(ix, iy)
+    np.testing.assert_array_equal(wx, wy)
+
+
+def test_host_tables_pinned_to_golden(golden_dir):
+    """Tables of the reference source itself (golden vectors, plain-Python
+    typing) agree with the plan's numba-typed tables to float32 rounding."""
+    from pyflowreg_gb300 import tables
+
+    g = np.load(os.path.join(golden_dir, "resize.npz"))
+    for q, (ih, iw, oh, ow) in enumerate(g["cases"]):
+        sig = tables.sigma_for((ih, iw), (oh, ow))
+        ix, wx = tables.resize_tables(iw, ow, sig)
+        np.testing.assert_array_equal(ix, g[f"ix{q}"])
+        np.testing.assert_allclose(wx, g[f"wx{q}"], rtol=0, atol=2e-7)
