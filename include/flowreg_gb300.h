@@ -160,6 +160,32 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
                     const double* a_data, double a_smooth, double hx, double hy, double omega,
                     float* du, float* dv, void* stream);
 
+/* frg_level_solve for callers that cannot allocate device memory -- code
+ * running while a CUDA graph is being captured (allocation calls are not
+ * allowed then), or a host whose device memory is reserved up front by
+ * another framework's pool, where a cudaMalloc would fail or would
+ * synchronise the device.  It has no counterpart in pyflowreg.
+ *
+ * Same arguments and results as frg_level_solve; it allocates nothing.  Its
+ * scratch is a fixed 8 MiB device array inside the library (every GPU that
+ * loads the library holds it until the process exits), so the level must fit
+ * in it: (7*K + 9) * (h + w - 1) * ceil32(h) floats, h = m - 2, w = n - 2,
+ * ceil32 = rounded up to a multiple of 32 (for K = 2 about 200 x 200 pixels;
+ * frg_level_solve_noalloc_capacity() returns the byte size).  Larger levels
+ * are rejected with FRG_EINVAL.
+ *
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one array: calls whose work overlaps on the GPU (on
+ * different streams, or from different threads) race and corrupt each
+ * other's results; serialise them.  Each call writes every scratch element
+ * it reads, so no clearing between calls is needed. */
+int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* weight, const float* u,
+                            const float* v, double alpha_x, double alpha_y, int iterations,
+                            int update_lag, const double* a_data, double a_smooth, double hx, double hy,
+                            double omega, float* du, float* dv, void* stream);
+size_t frg_level_solve_noalloc_capacity(void);
+
 /* Fused Gauss-cubic resize of n_planes planes (n_planes, ih, iw) to
  * (n_planes, oh, ow), sigma = 0.6 / min(oh/ih, ow/iw) when that is < 1. */
 int frg_resize(int n_planes, int ih, int iw, const float* src, int oh, int ow, float* dst,

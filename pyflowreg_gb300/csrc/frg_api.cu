@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -946,6 +947,102 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
     cudaError_t e = cudaFreeAsync(scratch, st);
     if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
     return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// frg_level_solve_noalloc: frg_level_solve for callers that cannot allocate
+// device memory.  Its scratch is this file-scope device array, a fixed 8 MiB
+// that every GPU loading the library keeps until the process exits.  Host code
+// must not use `g_noalloc_scratch` as a pointer (it names the host-side shadow);
+// the device address comes from cudaGetSymbolAddress, looked up once per device
+// with that device current, on the first call on that device.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocFloats = size_t(2) << 20;  // 2 Mi floats = 8 MiB
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocFloats];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+int noalloc_scratch(float** out)
+{
+    int dev = -1;
+    FRG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(FRG_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        FRG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = (float*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return FRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t frg_level_solve_noalloc_capacity(void) { return kNoAllocFloats * sizeof(float); }
+
+int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* weight, const float* u, const float* v,
+                            double alpha_x, double alpha_y, int iterations, int update_lag, const double* a_data,
+                            double a_smooth, double hx, double hy, double omega, float* du, float* dv, void* stream)
+{
+    if (!J || !weight || !u || !v || !a_data || !du || !dv) return fail(FRG_EINVAL, "NULL argument");
+    if (m < 3 || n < 3 || K < 1 || K > kMaxK) return fail(FRG_EINVAL, "bad shape");
+    if (iterations < 1 || update_lag < 1) return fail(FRG_EINVAL, "iterations and update_lag must be >= 1");
+    if (a_smooth != 1.0) return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
+    const int h = m - 2, w = n - 2;
+    DiagGeom g = make_geom(h, w);
+    if (g.P > kMaxLane) return fail(FRG_EUNSUPPORTED, "levels taller than 512 rows are not supported yet");
+    const long long dp = (long long)g.D * g.P;
+    const size_t elems = (size_t)(6 * K + K + 2 + 5 + 2) * (size_t)dp;
+    if (elems > kNoAllocFloats)
+        return fail(FRG_EINVAL, "level too large for the 8 MiB scratch of frg_level_solve_noalloc: needs " +
+                                    std::to_string(elems * sizeof(float)) + " bytes ((7K+9)*(h+w-1)*ceil32(h) floats)");
+    float* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long mn = (long long)m * n;
+    float* Jd = scratch;
+    float* Wd = Jd + 6LL * K * dp;
+    float* lap = Wd + (long long)K * dp;
+    float* coef = lap + 2 * dp;
+    float* dud = coef + 5 * dp;
+    float* dvd = dud + dp;
+    float ad[kMaxK];
+    for (int k = 0; k < K; ++k) ad[k] = (float)a_data[k];
+    const float wx = (float)(alpha_x / (hx * hx)), wy = (float)(alpha_y / (hy * hy));
+    // Every scratch element read below is first written in this call: to_diag
+    // and lap fill all pixels of the level, and the first fold sets du = dv = 0.
+    for (int q = 0; q < 6; ++q)
+        FRG_LAUNCH(launch_to_diag(view(J + q * mn * K + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h,
+                                  w, Jd + q * K * dp, 0, g, st));
+    FRG_LAUNCH(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd, 0, g,
+                              st));
+    FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
+    // the passes of make_passes, generated in place (no host container)
+    for (int t = 0; t < iterations;) {
+        const bool tick = ((t + 1) % update_lag) == 0;
+        int end = t + 1;
+        while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
+        const int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
+        for (int s = t; s < end; s += kGMax) {
+            if (s == t)
+                FRG_LAUNCH(launch_fold(Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, mode, wx, wy, st));
+            FRG_LAUNCH(launch_sor(coef, 0, dud, dvd, 0, 1, g, std::min(kGMax, end - s), wy, wx, (float)omega, st));
+        }
+        t = end;
+    }
+    FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
+    FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
+    return FRG_OK;
 }
 
 int frg_resize(int n_planes, int ih, int iw, const float* src, int oh, int ow, float* dst, void* stream)
