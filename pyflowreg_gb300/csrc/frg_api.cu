@@ -309,6 +309,7 @@ struct frg_plan {
     float* dv = nullptr;      // (T, D*P)
     float* uvpad = nullptr;   // (T, 2, h+2, w+2)
     float* uacc[2] = {nullptr, nullptr};  // (T, 2, h, w)
+    float* durm = nullptr;    // (2, T, h, w): the level's final du, dv, row-major
     float* ones = nullptr;    // (H, W, K) default weight
     float a_data[kMaxK] = {0};
     SorProfile prof;
@@ -388,15 +389,20 @@ int record_event(SorProfile* pr, cudaStream_t st)
     return FRG_OK;
 }
 
-// Runs the passes of one level: fold at ticks, wavefront SOR passes.
+// Runs the passes of one level.  K <= 4: one fused launch per pass (the fold
+// happens in the SOR's loader; a group cut into several passes stores its
+// coefficients in its first pass and the others read them).  Larger K: a fold
+// kernel at each group start, then the row-per-thread SOR.
 int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs, const float* W,
                 long long W_fs, const float* lap, long long lap_fs, float* du, float* dv,
                 long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
                 const float* a_data, float wx, float wy, float omega, cudaStream_t st,
-                SorProfile* prof = nullptr)
+                SorProfile* prof = nullptr, float* rm_du = nullptr, float* rm_dv = nullptr, long long rm_fs = 0)
 {
-    for (const Pass& ps : passes) {
-        if (ps.fold_mode >= 0)
+    const bool fused = sor_fused_supports(K);
+    for (size_t pi = 0; pi < passes.size(); ++pi) {
+        const Pass& ps = passes[pi];
+        if (!fused && ps.fold_mode >= 0)
             FRG_LAUNCH(launch_fold(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, T, K, g,
                                    a_data, ps.fold_mode, wx, wy, st));
         const bool timed = prof && prof->on;
@@ -404,8 +410,17 @@ int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs,
             int rc = record_event(prof, st);
             if (rc) return rc;
         }
-        // thread index runs along rows: rows are the a-direction (weight wy)
-        FRG_LAUNCH(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+        if (fused) {
+            const bool continued = pi + 1 < passes.size() && passes[pi + 1].fold_mode < 0;
+            const bool final_pass = pi + 1 == passes.size();
+            FRG_LAUNCH(launch_sor_fused(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, T, K, g, ps.G,
+                                        ps.fold_mode, (ps.fold_mode >= 0 && continued) ? 1 : 0, a_data, wx, wy,
+                                        omega, st, final_pass ? rm_du : nullptr, final_pass ? rm_dv : nullptr,
+                                        rm_fs));
+        } else {
+            // thread index runs along rows: rows are the a-direction (weight wy)
+            FRG_LAUNCH(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+        }
         if (timed) {
             int rc = record_event(prof, st);
             if (rc) return rc;
@@ -586,7 +601,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             (rc = dev_alloc(pl, &pl->coef, T * 5 * max_dp)) || (rc = dev_alloc(pl, &pl->du, T * max_dp)) ||
             (rc = dev_alloc(pl, &pl->dv, T * max_dp)) || (rc = dev_alloc(pl, &pl->uvpad, T * 2 * max_pad)) ||
             (rc = dev_alloc(pl, &pl->uacc[0], T * 2 * max_hw)) ||
-            (rc = dev_alloc(pl, &pl->uacc[1], T * 2 * max_hw))) {
+            (rc = dev_alloc(pl, &pl->uacc[1], T * 2 * max_hw)) || (rc = dev_alloc(pl, &pl->durm, T * 2 * max_hw))) {
             frg_plan_destroy(pl);
             return rc;
         }
@@ -791,7 +806,8 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
         // 5. level solve (core/optical_flow.py:584-606)
         int rc = solve_level(pl->passes, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du, pl->dv, dp, pl->coef,
-                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st, &pl->prof);
+                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st, &pl->prof,
+                             pl->durm, pl->durm + (long long)T * hw, hw);
         if (rc) return rc;
         // 6. median + accumulate (core/optical_flow.py:607-611)
         const int do_median = std::min(h, w) > 5 ? 1 : 0;
@@ -806,7 +822,11 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
             ov = vieww(pl->uacc[nxt] + hw, 2 * hw, 0, w, 1);
             cur = nxt;
         }
-        FRG_LAUNCH(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
+        if (sor_fused_supports(K))
+            FRG_LAUNCH(launch_median_rm(pl->durm, pl->durm + (long long)T * hw, hw, up, vp, T, h, w, do_median, ou,
+                                        ov, st));
+        else
+            FRG_LAUNCH(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
         prev = &L;
     }
     return FRG_OK;
@@ -1027,16 +1047,27 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
     FRG_LAUNCH(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd, 0, g,
                               st));
     FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
-    // the passes of make_passes, generated in place (no host container)
+    // the passes of make_passes, generated in place (no host container), run
+    // with the same kernels as solve_level uses for frg_level_solve
+    const bool fused = sor_fused_supports(K);
     for (int t = 0; t < iterations;) {
         const bool tick = ((t + 1) % update_lag) == 0;
         int end = t + 1;
         while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
         const int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
         for (int s = t; s < end; s += kGMax) {
-            if (s == t)
-                FRG_LAUNCH(launch_fold(Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, mode, wx, wy, st));
-            FRG_LAUNCH(launch_sor(coef, 0, dud, dvd, 0, 1, g, std::min(kGMax, end - s), wy, wx, (float)omega, st));
+            const int G = std::min(kGMax, end - s);
+            const int pass_mode = s == t ? mode : -1;
+            if (fused) {
+                const int store = (s == t && s + kGMax < end) ? 1 : 0;
+                FRG_LAUNCH(launch_sor_fused(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode, store,
+                                            ad, wx, wy, (float)omega, st));
+            } else {
+                if (pass_mode >= 0)
+                    FRG_LAUNCH(launch_fold(Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, pass_mode, wx, wy,
+                                           st));
+                FRG_LAUNCH(launch_sor(coef, 0, dud, dvd, 0, 1, g, G, wy, wx, (float)omega, st));
+            }
         }
         t = end;
     }
@@ -1106,21 +1137,17 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream)
 {
     if (!src || !dst || h < 3 || w < 3) return fail(FRG_EINVAL, "bad argument");
     cudaStream_t st = (cudaStream_t)stream;
-    DiagGeom g = make_geom(h, w);
-    const long long dp = (long long)g.D * g.P;
     const long long pad = (long long)(h + 2) * (w + 2);
     float* buf = nullptr;
-    FRG_CUDA(cudaMallocAsync((void**)&buf, (2 * dp + pad) * sizeof(float), st));
-    float* d1 = buf;
-    float* zeros = buf + 2 * dp;
+    FRG_CUDA(cudaMallocAsync((void**)&buf, pad * sizeof(float), st));
+    float* zeros = buf;
     auto run = [&]() -> int {
         FRG_CUDA(cudaMemsetAsync(zeros, 0, pad * sizeof(float), st));
-        FRG_LAUNCH(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1, 0, g, st));
-        FRG_LAUNCH(launch_to_diag(view(src, 0, 0, w, 1), 1, 1, h, w, d1 + dp, 0, g, st));
         View z = view(zeros, 0, 0, w + 2, 1);
-        // the v output duplicates u; write it to the same destination
-        FRG_LAUNCH(launch_median_accum(d1, d1 + dp, 0, z, z, 1, g, 1, vieww(dst, 0, 0, w, 1),
-                                     vieww(dst, 0, 0, w, 1), st));
+        // the pipeline's median kernel on one plane; the v output duplicates u
+        // and goes to the same destination
+        FRG_LAUNCH(launch_median_rm(src, src, 0, z, z, 1, h, w, 1, vieww(dst, 0, 0, w, 1), vieww(dst, 0, 0, w, 1),
+                                    st));
         return FRG_OK;
     };
     int rc = run();

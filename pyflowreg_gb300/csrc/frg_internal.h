@@ -60,6 +60,20 @@ cudaError_t launch_fold(const float* J, long long J_fs, const float* W, long lon
 cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
                        int n_frames, DiagGeom g, int G, float wa, float wb, float omega,
                        cudaStream_t st);
+// SOR with the fold in its loader (frg_sor.cu), K <= 4.  mode: -1 reads the
+// coefficients stored by the group's first pass; else bit0 du = dv = 0, bit1
+// psi tick.  store_coef writes the folded coefficients for continuation passes.
+bool sor_fused_supports(int K);
+// out_du/out_dv (optional, frame stride out_fs): the pass writes its result
+// row-major (h, w) there instead of back into du/dv (the level's last pass).
+cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
+                             long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                             int n_frames, int K, DiagGeom g, int G, int mode, int store_coef, const float* a_data,
+                             float wx, float wy, float omega, cudaStream_t st, float* out_du = nullptr,
+                             float* out_dv = nullptr, long long out_fs = 0);
+// 5x5 median (mirror) of row-major du, dv (T, h, w) plus accumulation into u, v.
+cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
+                             int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st);
 cudaError_t launch_median_accum(const float* du, const float* dv, long long st_fs, View u, View v,
                                 int n_frames, DiagGeom g, int do_median, ViewW out_u, ViewW out_v,
                                 cudaStream_t st);

@@ -620,4 +620,63 @@ cudaError_t launch_median_accum(const float* du, const float* dv, long long st_f
     return cudaGetLastError();
 }
 
+// Median + accumulate on row-major du, dv (T, h, w): a 32 x 8 output tile with
+// its mirrored 2-pixel halo is staged in shared memory by coalesced row loads.
+constexpr int kMedTx = 32, kMedTy = 8;
+
+__global__ void __launch_bounds__(kMedTx * kMedTy) k_median_rm(const float* __restrict__ du,
+                                                               const float* __restrict__ dv, long long fs, View u,
+                                                               View v, int h, int w, int do_median, ViewW out_u,
+                                                               ViewW out_v)
+{
+    __shared__ float su[kMedTy + 4][kMedTx + 4];
+    __shared__ float sv[kMedTy + 4][kMedTx + 4];
+    const int f = blockIdx.z;
+    const int x0 = blockIdx.x * kMedTx, y0 = blockIdx.y * kMedTy;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * kMedTx + tx;
+    const float* duf = du + f * fs;
+    const float* dvf = dv + f * fs;
+    if (do_median) {
+        for (int i = tid; i < (kMedTy + 4) * (kMedTx + 4); i += kMedTx * kMedTy) {
+            const int r = i / (kMedTx + 4), c = i - r * (kMedTx + 4);
+            const int yy = mirror(min(y0 - 2 + r, h + 1), h);
+            const int xx = mirror(min(x0 - 2 + c, w + 1), w);
+            su[r][c] = duf[(long long)yy * w + xx];
+            sv[r][c] = dvf[(long long)yy * w + xx];
+        }
+        __syncthreads();
+    }
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= w || y >= h) return;
+    float mu, mv;
+    if (do_median) {
+        float a[25], b[25];
+#pragma unroll
+        for (int dy = 0; dy < 5; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 5; ++dx) {
+                a[dy * 5 + dx] = su[ty + dy][tx + dx];
+                b[dy * 5 + dx] = sv[ty + dy][tx + dx];
+            }
+        mu = median25(a);
+        mv = median25(b);
+    } else {
+        mu = duf[(long long)y * w + x];
+        mv = dvf[(long long)y * w + x];
+    }
+    const float uc = u.p[f * u.fs + (long long)(y + 1) * u.rs + (long long)(x + 1) * u.cs];
+    const float vc = v.p[f * v.fs + (long long)(y + 1) * v.rs + (long long)(x + 1) * v.cs];
+    out_u.p[f * out_u.fs + (long long)y * out_u.rs + (long long)x * out_u.cs] = uc + mu;
+    out_v.p[f * out_v.fs + (long long)y * out_v.rs + (long long)x * out_v.cs] = vc + mv;
+}
+
+cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
+                             int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st)
+{
+    dim3 blk(kMedTx, kMedTy), grd((w + kMedTx - 1) / kMedTx, (h + kMedTy - 1) / kMedTy, n_frames);
+    k_median_rm<<<grd, blk, 0, st>>>(du, dv, fs, u, v, h, w, do_median, out_u, out_v);
+    return cudaGetLastError();
+}
+
 }  // namespace frg

@@ -148,6 +148,20 @@ def test_batch_equals_single_frames():
             np.testing.assert_array_equal(batch[t], single.astype(batch.dtype))
 
 
+def test_many_channels_generic_path(oracle):
+    """K = 5 runs the generic kernels (separate fold, row-per-thread SOR,
+    diagonal-major median); fp64 parity still holds and fp32 stays close."""
+    rng = np.random.default_rng(9)
+    fixed, moving, _ = pair_256(8, h=48, w=56)
+    f5 = np.stack([fixed * (1 + 0.1 * k) for k in range(5)], axis=2)
+    m5 = np.stack([moving * (1 + 0.1 * k) for k in range(5)], axis=2) + 0.001 * rng.standard_normal((48, 56, 5))
+    kw = dict(alpha=(1.5, 1.5), iterations=20)
+    ref, env_max, env_epe = envelope(oracle, f5, m5.astype(np.float32), kw)
+    assert_parity(G.get_displacement(f5, m5.astype(np.float32), precision="fp64", **kw), ref)
+    mx, ep = flow_diff(G.get_displacement(f5, m5.astype(np.float32), **kw), ref)
+    assert mx <= 2 * env_max and ep <= 2 * env_epe, (mx, ep, env_max, env_epe)
+
+
 def test_deterministic():
     fixed, moving, _ = pair_256(6, h=128, w=128)
     a = G.get_displacement(fixed, moving, alpha=(1.5, 1.5))
