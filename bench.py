@@ -276,7 +276,7 @@ def run_gb300(args):
     per_launch_bytes = sor_bytes / max(sor_n, 1)
     ratio = profiled_traffic()
     roofline = {
-        "kernel": "k_sor (exact-order wavefront SOR)",
+        "kernel": "k_sor_fused (exact-order wavefront SOR, fold in the loader)",
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
@@ -287,8 +287,10 @@ def run_gb300(args):
         "algorithmic_bytes_per_launch": per_launch_bytes,
         "launches": sor_n,
         "share_of_step": (sor_ms / ms) if ms > 0 else None,
-        "note": "36 B per interior pixel per pipelined SOR iteration (streaming model); "
-                "the kernel keeps G iterations in shared memory, so frac can exceed 1",
+        "note": "achieved = 36 B per interior pixel per pipelined SOR iteration (streaming model) / "
+                "CUDA-event time of the SOR launches; the kernel keeps G iterations in shared memory, so "
+                "frac can exceed 1; traffic = measured DRAM/model ratio (profiles/dram_traffic.txt) x model "
+                "bytes per launch",
     }
 
     cpu = None

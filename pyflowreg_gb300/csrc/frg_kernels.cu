@@ -63,9 +63,75 @@ __global__ void k_resize_v(const float* __restrict__ src, int n_planes, int ih, 
     dst.p[f * dst.fs + pl * dst.ps + (long long)yo * dst.rs + (long long)xo * dst.cs] = s;
 }
 
+// Horizontal pass, shared-memory form: one block takes `rows` input rows of
+// one frame (all planes), stages them and the level's tap table in shared
+// memory, and each thread produces one (plane, output column) for all the
+// block's rows, so each table entry is read once per `rows` outputs.
+__global__ void k_resize_h_smem(View src, int n_planes, int ih, int iw, float* __restrict__ dst, int ow,
+                                const int32_t* __restrict__ ix, const float* __restrict__ wx, int P, int rows)
+{
+    extern __shared__ float sh[];
+    int32_t* tix = reinterpret_cast<int32_t*>(sh);
+    float* twx = sh + (size_t)ow * P;
+    float* srow = twx + (size_t)ow * P;  // [rows][n_planes][iw]
+    const int f = blockIdx.y;
+    const int y0 = blockIdx.x * rows;
+    const int nr = min(rows, ih - y0);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int i = tid; i < ow * P; i += nth) {
+        tix[i] = ix[i];
+        twx[i] = wx[i];
+    }
+    const float* base = src.p + f * src.fs;
+    const int row_elems = n_planes * iw;
+    for (int i = tid; i < nr * row_elems; i += nth) {
+        const int r = i / row_elems, rem = i - r * row_elems;
+        int pl, x;
+        if (src.cs == 1) {  // planar rows
+            pl = rem / iw;
+            x = rem - pl * iw;
+        } else {  // interleaved channels: consecutive elements walk the channels
+            x = rem / n_planes;
+            pl = rem - x * n_planes;
+        }
+        srow[((size_t)r * n_planes + pl) * iw + x] =
+            base[pl * src.ps + (long long)(y0 + r) * src.rs + (long long)x * src.cs];
+    }
+    __syncthreads();
+    for (int item = tid; item < n_planes * ow; item += nth) {
+        const int pl = item / ow, x = item - pl * ow;
+        float acc[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) acc[r] = 0.0f;
+        for (int p = 0; p < P; ++p) {
+            const int j = tix[x * P + p];
+            const float wgt = twx[x * P + p];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                if (r < nr) acc[r] = fmaf(srow[((size_t)r * n_planes + pl) * iw + j], wgt, acc[r]);
+        }
+        for (int r = 0; r < nr; ++r)
+            dst[(((long long)f * n_planes + pl) * ih + y0 + r) * ow + x] = acc[r];
+    }
+}
+
 cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
                             const int32_t* ix, const float* wx, int P, cudaStream_t st)
 {
+    const int rows = 8;
+    const size_t smem = (size_t)ow * P * 8 + (size_t)rows * n_planes * iw * 4;
+    if (smem <= 96 * 1024 && n_frames <= 65535) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_resize_h_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 96 * 1024);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        dim3 grd((ih + rows - 1) / rows, n_frames);
+        k_resize_h_smem<<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, rows);
+        return cudaGetLastError();
+    }
     dim3 blk(128), grd((ow + 127) / 128, ih, n_frames * n_planes);
     k_resize_h<<<grd, blk, 0, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P);
     return cudaGetLastError();
@@ -154,21 +220,15 @@ cudaError_t launch_warp(View f2, View f1, View u, View v, int n_frames, int K, i
 // padding: every neighbour index is clamped into the level.  Output is
 // diagonal-major, per frame [6][K][D*P] in the order J11, J22, J33, J12, J13, J23.
 // ---------------------------------------------------------------------------
-__global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float hx, int gray,
-                         float* __restrict__ J, long long J_fs, DiagGeom g)
+// J11..J23 of channel k at pixel (y, x) of frame f.
+__device__ __forceinline__ void tensor_at(const View& f1, const View& f2, int f, int k, int y, int x, int h, int w,
+                                          float hy, float hx, int gray, float* out)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
-    const int f = blockIdx.z;
-    if (x >= w) return;
     const int xm = max(x - 1, 0), xp = min(x + 1, w - 1);
     const int ym = max(y - 1, 0), yp = min(y + 1, h - 1);
-    const long long di = diag_index(g, y, x);
-    const long long plane = (long long)g.D * g.P;
-    float* Jf = J + f * J_fs;
     const float h2x = 2.0f * hx, h2y = 2.0f * hy;
     const float hxx = hx * hx, hyy = hy * hy;
-    for (int k = 0; k < K; ++k) {
+    {
         const float* a = f1.p + f * f1.fs + k * f1.ps;
         const float* b = f2.p + f * f2.fs + k * f2.ps;
 #define A_(r, c) a[(long long)(r) * f1.rs + (long long)(c) * f1.cs]
@@ -204,20 +264,92 @@ __global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float 
         }
 #undef A_
 #undef B_
+        out[0] = j11;
+        out[1] = j22;
+        out[2] = j33;
+        out[3] = j12;
+        out[4] = j13;
+        out[5] = j23;
+    }
+}
+
+__global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float hx, int gray,
+                         float* __restrict__ J, long long J_fs, DiagGeom g)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const long long di = diag_index(g, y, x);
+    const long long plane = (long long)g.D * g.P;
+    const long long qs = (long long)K * plane;
+    float* Jf = J + f * J_fs;
+    for (int k = 0; k < K; ++k) {
+        float j[6];
+        tensor_at(f1, f2, f, k, y, x, h, w, hy, hx, gray, j);
         const long long kb = (long long)k * plane + di;
-        const long long qs = (long long)K * plane;
-        Jf[0 * qs + kb] = j11;
-        Jf[1 * qs + kb] = j22;
-        Jf[2 * qs + kb] = j33;
-        Jf[3 * qs + kb] = j12;
-        Jf[4 * qs + kb] = j13;
-        Jf[5 * qs + kb] = j23;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) Jf[q * qs + kb] = j[q];
+    }
+}
+
+// Tiled form: a 32 x 32 pixel tile is computed into shared memory, then every
+// diagonal crossing the tile is written as one contiguous run of the
+// diagonal-major layout (up to 128 bytes per warp store instead of 32
+// scattered 4-byte stores).
+constexpr int kTensTile = 32;
+
+__global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, int h, int w, float hy, float hx,
+                                                      int gray, float* __restrict__ J, long long J_fs, DiagGeom g)
+{
+    extern __shared__ float tile[];  // [6K][32][33]
+    const int f = blockIdx.z;
+    const int r0 = blockIdx.y * kTensTile, c0 = blockIdx.x * kTensTile;
+    const int tx = threadIdx.x & 31, tw = threadIdx.x >> 5;  // 8 warps
+    const int ld = kTensTile + 1;
+    for (int rr = tw; rr < kTensTile; rr += 8) {
+        const int y = r0 + rr, x = c0 + tx;
+        if (y < h && x < w) {
+            for (int k = 0; k < K; ++k) {
+                float j[6];
+                tensor_at(f1, f2, f, k, y, x, h, w, hy, hx, gray, j);
+#pragma unroll
+                for (int q = 0; q < 6; ++q) tile[((q * K + k) * kTensTile + rr) * ld + tx] = j[q];
+            }
+        }
+    }
+    __syncthreads();
+    const long long plane = (long long)g.D * g.P;
+    float* Jf = J + f * J_fs;
+    // local diagonal dd = rr + cc in [0, 62]; rows of the segment are contiguous
+    for (int dd = tw; dd < 2 * kTensTile - 1; dd += 8) {
+        const int rr_lo = max(0, dd - (kTensTile - 1));
+        const int rr = rr_lo + tx;
+        const int cc = dd - rr;
+        if (rr > min(kTensTile - 1, dd)) continue;
+        const int y = r0 + rr, x = c0 + cc;
+        if (y >= h || x >= w) continue;
+        const long long di = diag_index(g, y, x);
+        for (int qk = 0; qk < 6 * K; ++qk) Jf[(long long)qk * plane + di] = tile[(qk * kTensTile + rr) * ld + cc];
     }
 }
 
 cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
                           int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st)
 {
+    const size_t smem = (size_t)6 * K * kTensTile * (kTensTile + 1) * sizeof(float);
+    if (smem <= 200 * 1024) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_tensor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 200 * 1024);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        dim3 grd((w + kTensTile - 1) / kTensTile, (h + kTensTile - 1) / kTensTile, n_frames);
+        k_tensor_tiled<<<grd, 256, smem, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g);
+        return cudaGetLastError();
+    }
     dim3 blk(128), grd((w + 127) / 128, h, n_frames);
     k_tensor<<<grd, blk, 0, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g);
     return cudaGetLastError();
