@@ -163,41 +163,63 @@ double resize_sigma(int ih, int iw, int oh, int ow)
     return s < 1.0 ? 0.6 / s : 0.0;
 }
 
-// cv2.remap weights at the 32 sub-pixel positions, restated from the
-// documented Keys (A = -0.75) and bilinear kernels, single precision with a
-// fixed operation order.
+// The four Keys (A = -0.75) weights OpenCV documents for bicubic sampling at
+// fractional offset t (taps at distances 1+t, t, 1-t, 2-t; the last is one
+// minus the others), single precision with a fixed operation order.
+void keys4(float tf, float* out)
+{
+    volatile float t = tf;
+    const float A = -0.75f;
+    auto inner = [&](float x) {
+        volatile float a = (A + 2.0f) * x;
+        volatile float b = a - (A + 3.0f);
+        volatile float xx = x * x;
+        volatile float c = b * xx;
+        return (float)(c + 1.0f);
+    };
+    auto outer = [&](float x) {
+        volatile float a = A * x;
+        volatile float b = a - 5.0f * A;
+        volatile float c = b * x;
+        volatile float d = c + 8.0f * A;
+        volatile float e = d * x;
+        return (float)(e - 4.0f * A);
+    };
+    const float w0 = outer(1.0f + t);
+    const float w1 = inner(t);
+    const float w2 = inner(1.0f - t);
+    volatile float r = 1.0f - w0;
+    r = r - w1;
+    r = r - w2;
+    out[0] = w0;
+    out[1] = w1;
+    out[2] = w2;
+    out[3] = r;
+}
+
+// cv2.remap weights at the 32 sub-pixel positions (bicubic and bilinear).
 void remap_tables(float* cub, float* lin)
 {
     for (int k = 0; k < 32; ++k) {
         volatile float t = (float)k / 32.0f;
-        const float A = -0.75f;
-        auto inner = [&](float x) {
-            volatile float a = (A + 2.0f) * x;
-            volatile float b = a - (A + 3.0f);
-            volatile float xx = x * x;
-            volatile float c = b * xx;
-            return (float)(c + 1.0f);
-        };
-        auto outer = [&](float x) {
-            volatile float a = A * x;
-            volatile float b = a - 5.0f * A;
-            volatile float c = b * x;
-            volatile float d = c + 8.0f * A;
-            volatile float e = d * x;
-            return (float)(e - 4.0f * A);
-        };
-        const float w0 = outer(1.0f + t);
-        const float w1 = inner(t);
-        const float w2 = inner(1.0f - t);
-        volatile float r = 1.0f - w0;
-        r = r - w1;
-        r = r - w2;
-        cub[k * 4 + 0] = w0;
-        cub[k * 4 + 1] = w1;
-        cub[k * 4 + 2] = w2;
-        cub[k * 4 + 3] = r;
+        keys4(t, cub + k * 4);
         lin[k * 2 + 0] = 1.0f - t;
         lin[k * 2 + 1] = t;
+    }
+}
+
+// Tap start and weights of cv2.resize INTER_CUBIC along one axis
+// (in_len -> out_len): source coordinate (d + 0.5) * in/out - 0.5.
+void upsample_tables(int in_len, int out_len, std::vector<int32_t>& s0, std::vector<float>& wt)
+{
+    s0.resize(out_len);
+    wt.resize((size_t)out_len * 4);
+    const double scale = (double)in_len / (double)out_len;
+    for (int d = 0; d < out_len; ++d) {
+        const double f = (d + 0.5) * scale - 0.5;
+        const double s = std::floor(f);
+        s0[d] = (int32_t)s;
+        keys4((float)(f - s), wt.data() + (size_t)d * 4);
     }
 }
 
@@ -256,7 +278,7 @@ struct Pass {
     int fold_mode;  // -1: no fold; else bit0 zero-init, bit1 psi from (du, dv)
 };
 
-std::vector<Pass> make_passes(int iterations, int update_lag)
+std::vector<Pass> make_passes(int iterations, int update_lag, int gmax = kGMax)
 {
     std::vector<Pass> out;
     int t = 0;
@@ -265,9 +287,9 @@ std::vector<Pass> make_passes(int iterations, int update_lag)
         int end = t + 1;
         while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
         int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
-        for (int s = t; s < end; s += kGMax) {
+        for (int s = t; s < end; s += gmax) {
             Pass p;
-            p.G = std::min(kGMax, end - s);
+            p.G = std::min(gmax, end - s);
             p.fold_mode = (s == t) ? mode : -1;
             out.push_back(p);
         }
@@ -294,7 +316,6 @@ struct frg_plan {
     int H = 0, W = 0, K = 0, max_T = 0;
     int min_level = 0;
     std::vector<LevelPlan> levels;
-    std::vector<Pass> passes;
     std::vector<void*> allocs;
     size_t bytes = 0;
     bool has_ref = false;
@@ -321,6 +342,12 @@ struct frg_plan {
     double* xuv = nullptr;    // (T, 2, m*n)
     double* xacc[2] = {nullptr, nullptr};  // (T, 2, h*w)
     double a_data64[kMaxK] = {0};
+    // final cubic upsampling when min_level > 0 (tables per output column / row)
+    int32_t* up_sx = nullptr;
+    float* up_wx = nullptr;
+    int32_t* up_sy = nullptr;
+    float* up_wy = nullptr;
+    double* xtmp = nullptr;   // fp64 width-pass buffer (T, 2, h_min, W)
 };
 
 namespace {
@@ -393,13 +420,28 @@ int record_event(SorProfile* pr, cudaStream_t st)
 // happens in the SOR's loader; a group cut into several passes stores its
 // coefficients in its first pass and the others read them).  Larger K: a fold
 // kernel at each group start, then the row-per-thread SOR.
-int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs, const float* W,
+// Which SOR kernel a level uses: the fused shared-memory ring (K <= 4, up to
+// 1024 rows), the row-per-thread ring with a separate fold (K > 4, up to 512
+// rows), or the global-memory wavefront with a separate fold (anything else).
+enum SorKind { kSorFused = 0, kSorRows = 1, kSorGlobal = 2 };
+
+SorKind sor_kind(int K, const DiagGeom& g)
+{
+    if (sor_fused_supports(K) && sor_fused_gmax(g.P) >= 1) return kSorFused;
+    if (g.P <= kMaxLane) return kSorRows;
+    return kSorGlobal;
+}
+
+int solve_level(int iterations, int update_lag, const float* J, long long J_fs, const float* W,
                 long long W_fs, const float* lap, long long lap_fs, float* du, float* dv,
                 long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
                 const float* a_data, float wx, float wy, float omega, cudaStream_t st,
                 SorProfile* prof = nullptr, float* rm_du = nullptr, float* rm_dv = nullptr, long long rm_fs = 0)
 {
-    const bool fused = sor_fused_supports(K);
+    const SorKind kind = sor_kind(K, g);
+    const bool fused = kind == kSorFused;
+    const int gmax = kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag);
+    const std::vector<Pass> passes = make_passes(iterations, update_lag, gmax);
     for (size_t pi = 0; pi < passes.size(); ++pi) {
         const Pass& ps = passes[pi];
         if (!fused && ps.fold_mode >= 0)
@@ -417,9 +459,11 @@ int solve_level(const std::vector<Pass>& passes, const float* J, long long J_fs,
                                         ps.fold_mode, (ps.fold_mode >= 0 && continued) ? 1 : 0, a_data, wx, wy,
                                         omega, st, final_pass ? rm_du : nullptr, final_pass ? rm_dv : nullptr,
                                         rm_fs));
-        } else {
+        } else if (kind == kSorRows) {
             // thread index runs along rows: rows are the a-direction (weight wy)
             FRG_LAUNCH(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
+        } else {
+            FRG_LAUNCH(launch_sor_global(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
         }
         if (timed) {
             int rc = record_event(prof, st);
@@ -528,10 +572,6 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     if (top <= min_level) min_level = top - 1;
     if (min_level < 0) min_level = 0;
     pl->min_level = min_level;
-    if (min_level > 0) {
-        frg_plan_destroy(pl);
-        return fail(FRG_EUNSUPPORTED, "min_level > 0 (final cubic upsampling) is not supported yet");
-    }
     int ph = 0, pw = 0;
     size_t max_dp = 0, max_hw = 0, max_pad = 0;
     for (int i = top; i >= min_level; --i) {
@@ -542,10 +582,6 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         if (L.h < 1 || L.w < 1) {
             frg_plan_destroy(pl);
             return fail(FRG_EINVAL, "degenerate pyramid level");
-        }
-        if (params->precision == FRG_FP32 && (L.h + 31) / 32 * 32 > kMaxLane) {
-            frg_plan_destroy(pl);
-            return fail(FRG_EUNSUPPORTED, "frames taller than 512 rows are not supported yet");
         }
         L.top = (i == top);
         L.h_row = (double)m / L.h;
@@ -577,7 +613,31 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         pw = L.w;
         pl->levels.push_back(L);
     }
-    pl->passes = make_passes(params->iterations, params->update_lag);
+    if (min_level > 0) {
+        const LevelPlan& Lm = pl->levels.back();
+        std::vector<int32_t> sx, sy;
+        std::vector<float> wxu, wyu;
+        upsample_tables(Lm.w, width, sx, wxu);
+        upsample_tables(Lm.h, height, sy, wyu);
+        if ((rc = dev_alloc(pl, &pl->up_sx, sx.size())) || (rc = dev_alloc(pl, &pl->up_wx, wxu.size())) ||
+            (rc = dev_alloc(pl, &pl->up_sy, sy.size())) || (rc = dev_alloc(pl, &pl->up_wy, wyu.size()))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
+        cudaMemcpy(pl->up_sx, sx.data(), sx.size() * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(pl->up_wx, wxu.data(), wxu.size() * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(pl->up_sy, sy.data(), sy.size() * 4, cudaMemcpyHostToDevice);
+        cudaError_t e = cudaMemcpy(pl->up_wy, wyu.data(), wyu.size() * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            frg_plan_destroy(pl);
+            return fail(FRG_ECUDA, cudaGetErrorString(e));
+        }
+        if (params->precision == FRG_FP64_REFERENCE &&
+            (rc = dev_alloc(pl, &pl->xtmp, (size_t)max_frames * 2 * Lm.h * width))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
+    }
 
     const size_t T = (size_t)max_frames, K = (size_t)channels;
     const size_t tmp_elems = T * std::max<size_t>(K, 2) * (size_t)height * width;
@@ -805,15 +865,16 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
                                pl->J, J_fs, L.g, st));
         FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
         // 5. level solve (core/optical_flow.py:584-606)
-        int rc = solve_level(pl->passes, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du, pl->dv, dp, pl->coef,
-                             5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st, &pl->prof,
-                             pl->durm, pl->durm + (long long)T * hw, hw);
+        const bool fused = sor_kind(K, L.g) == kSorFused;
+        int rc = solve_level(pl->p.iterations, pl->p.update_lag, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du,
+                             pl->dv, dp, pl->coef, 5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st,
+                             &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw);
         if (rc) return rc;
         // 6. median + accumulate (core/optical_flow.py:607-611)
         const int do_median = std::min(h, w) > 5 ? 1 : 0;
         const bool last = (li + 1 == pl->levels.size());
         ViewW ou, ov;
-        if (last) {
+        if (last && pl->min_level == 0) {
             ou = vieww(flow_out, (long long)H * W * 2, 0, (long long)W * 2, 2);
             ov = vieww(flow_out + 1, (long long)H * W * 2, 0, (long long)W * 2, 2);
         } else {
@@ -822,12 +883,18 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
             ov = vieww(pl->uacc[nxt] + hw, 2 * hw, 0, w, 1);
             cur = nxt;
         }
-        if (sor_fused_supports(K))
+        if (fused)
             FRG_LAUNCH(launch_median_rm(pl->durm, pl->durm + (long long)T * hw, hw, up, vp, T, h, w, do_median, ou,
                                         ov, st));
         else
             FRG_LAUNCH(launch_median_accum(pl->du, pl->dv, dp, up, vp, T, L.g, do_median, ou, ov, st));
         prev = &L;
+    }
+    if (pl->min_level > 0) {
+        // cv2.resize(w, (n, m), INTER_CUBIC) of the finest computed level (core/optical_flow.py:615-616)
+        FRG_LAUNCH(launch_cubic_up<float>(pl->uacc[cur], T, 2, prev->h, prev->w, pl->tmp, flow_out,
+                                          (long long)H * W * 2, 1, (long long)W * 2, 2, H, W, pl->up_sx, pl->up_wx,
+                                          pl->up_sy, pl->up_wy, st));
     }
     return FRG_OK;
 }
@@ -887,7 +954,7 @@ int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const flo
                                 pl->a_data64, pl->p.omega, st));
         const int do_median = std::min(h, w) > 5 ? 1 : 0;
         const bool last = (li + 1 == pl->levels.size());
-        if (last) {
+        if (last && pl->min_level == 0) {
             FRG_LAUNCH(launch_x_median_accum(pl->xdu, pl->xdv, pl->xuv, pl->xuv + mn, uv_fs, T, h, w, do_median,
                                              flow_out, flow_out + 1, (long long)H * W * 2, (long long)W * 2, 2, st));
         } else {
@@ -897,6 +964,11 @@ int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const flo
             cur = nxt;
         }
         prev = &L;
+    }
+    if (pl->min_level > 0) {
+        FRG_LAUNCH(launch_cubic_up<double>(pl->xacc[cur], T, 2, prev->h, prev->w, pl->xtmp, flow_out,
+                                           (long long)H * W * 2, 1, (long long)W * 2, 2, H, W, pl->up_sx, pl->up_wx,
+                                           pl->up_sy, pl->up_wy, st));
     }
     return FRG_OK;
 }
@@ -930,7 +1002,6 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
     if (a_smooth != 1.0) return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
     const int h = m - 2, w = n - 2;
     DiagGeom g = make_geom(h, w);
-    if (g.P > kMaxLane) return fail(FRG_EUNSUPPORTED, "levels taller than 512 rows are not supported yet");
     cudaStream_t st = (cudaStream_t)stream;
     const long long dp = (long long)g.D * g.P;
     const long long mn = (long long)m * n;
@@ -955,9 +1026,8 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
         FRG_LAUNCH(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd,
                                 0, g, st));
         FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
-        std::vector<Pass> passes = make_passes(iterations, update_lag);
-        int r = solve_level(passes, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy, (float)omega,
-                            st);
+        int r = solve_level(iterations, update_lag, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy,
+                            (float)omega, st);
         if (r) return r;
         FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
         FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));

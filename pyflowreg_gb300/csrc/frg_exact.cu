@@ -488,3 +488,87 @@ cudaError_t launch_x_median_accum(const double* du, const double* dv, const doub
 }
 
 }  // namespace frg
+
+namespace frg {
+
+// ---------------------------------------------------------------------------
+// Final upsampling of the flow when min_level > 0 (core/optical_flow.py:615-616,
+// cv2.resize INTER_CUBIC): along one axis, output d samples the input at
+// (d + 0.5) * in/out - 0.5 with four Keys (A = -0.75) float32 weights on
+// clamped taps (tables built on the host).  Width pass first, then height,
+// accumulating in the element type (float64 in parity mode).
+// src planes (n, ih, iw) contiguous; the width pass writes (n, ih, ow)
+// contiguous, the height pass writes through a strided view.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T addx(T a, T b);
+template <>
+__device__ __forceinline__ float addx<float>(float a, float b) { return a + b; }
+template <>
+__device__ __forceinline__ double addx<double>(double a, double b) { return __dadd_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T mulx(T a, T b);
+template <>
+__device__ __forceinline__ float mulx<float>(float a, float b) { return a * b; }
+template <>
+__device__ __forceinline__ double mulx<double>(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename T>
+__global__ void k_cubic_up_w(const T* __restrict__ src, int n, int ih, int iw, T* __restrict__ dst, int ow,
+                             const int32_t* __restrict__ s0, const float* __restrict__ wt)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, pl = blockIdx.z;
+    if (x >= ow) return;
+    const T* row = src + ((long long)pl * ih + y) * iw;
+    T acc = (T)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int j = xclamp(s0[x] - 1 + k, 0, iw - 1);
+        acc = addx<T>(acc, mulx<T>(row[j], (T)wt[x * 4 + k]));
+    }
+    dst[((long long)pl * ih + y) * ow + x] = acc;
+}
+
+template <typename T>
+__global__ void k_cubic_up_h(const T* __restrict__ src, int n_planes, int ih, int ow, T* __restrict__ dst,
+                             long long fs, long long ps, long long rs, long long cs, int oh,
+                             const int32_t* __restrict__ s0, const float* __restrict__ wt)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, fp = blockIdx.z;
+    if (x >= ow) return;
+    const T* col = src + (long long)fp * ih * ow + x;
+    T acc = (T)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int j = xclamp(s0[y] - 1 + k, 0, ih - 1);
+        acc = addx<T>(acc, mulx<T>(col[(long long)j * ow], (T)wt[y * 4 + k]));
+    }
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+    dst[f * fs + pl * ps + (long long)y * rs + (long long)x * cs] = acc;
+}
+
+template <typename T>
+cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, int iw, T* tmp, T* dst, long long fs,
+                            long long ps, long long rs, long long cs, int oh, int ow, const int32_t* sx,
+                            const float* wx, const int32_t* sy, const float* wy, cudaStream_t st)
+{
+    dim3 blk(128);
+    dim3 g1((ow + 127) / 128, ih, n_frames * n_planes);
+    k_cubic_up_w<T><<<g1, blk, 0, st>>>(src, n_frames * n_planes, ih, iw, tmp, ow, sx, wx);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 g2((ow + 127) / 128, oh, n_frames * n_planes);
+    k_cubic_up_h<T><<<g2, blk, 0, st>>>(tmp, n_planes, ih, ow, dst, fs, ps, rs, cs, oh, sy, wy);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_cubic_up<float>(const float*, int, int, int, int, float*, float*, long long, long long,
+                                           long long, long long, int, int, const int32_t*, const float*,
+                                           const int32_t*, const float*, cudaStream_t);
+template cudaError_t launch_cubic_up<double>(const double*, int, int, int, int, double*, double*, long long,
+                                            long long, long long, long long, int, int, const int32_t*, const float*,
+                                            const int32_t*, const float*, cudaStream_t);
+
+}  // namespace frg

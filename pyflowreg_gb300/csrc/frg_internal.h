@@ -60,6 +60,12 @@ cudaError_t launch_fold(const float* J, long long J_fs, const float* W, long lon
 cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
                        int n_frames, DiagGeom g, int G, float wa, float wb, float omega,
                        cudaStream_t st);
+// Pass on global memory for levels of any height (coefficients from the fold kernel).
+cudaError_t launch_sor_global(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                              int n_frames, DiagGeom g, int G, float wa, float wb, float omega, cudaStream_t st);
+// Largest pass length the fused kernel's shared-memory ring allows for a level
+// of P (padded) rows; 0 when the level is too tall for it.
+int sor_fused_gmax(int P);
 // SOR with the fold in its loader (frg_sor.cu), K <= 4.  mode: -1 reads the
 // coefficients stored by the group's first pass; else bit0 du = dv = 0, bit1
 // psi tick.  store_coef writes the folded coefficients for continuation passes.
@@ -101,6 +107,12 @@ cudaError_t launch_x_sor(const double* J, const double* W, const double* u, cons
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
                          double alpha_y, double hx, double hy, int iterations, int update_lag,
                          const double* a_data, double omega, cudaStream_t st);
+// cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
+// (oh, ow): width pass into tmp, height pass into the strided dst view.
+template <typename T>
+cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, int iw, T* tmp, T* dst, long long fs,
+                            long long ps, long long rs, long long cs, int oh, int ow, const int32_t* sx,
+                            const float* wx, const int32_t* sy, const float* wy, cudaStream_t st);
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);

@@ -663,6 +663,61 @@ cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* d
 }
 
 // ---------------------------------------------------------------------------
+// The same pass for levels too tall for a shared-memory ring: du, dv and the
+// folded coefficients stay in global memory (diagonal-major); one CTA per
+// frame walks the wavefront, each step's pixels spread over its threads.
+// __syncthreads orders one step's stores before the next step's loads.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_sor_global(const float* __restrict__ coef, long long coef_fs,
+                                                      float* du_g, float* dv_g, long long st_fs, DiagGeom g, int G,
+                                                      float wa, float wb, float omega)
+{
+    const int P = g.P, A = g.h, B = g.w, D = g.D;
+    const long long plane = (long long)D * P;
+    const float* cf = coef + blockIdx.x * coef_fs;
+    float* du = du_g + blockIdx.x * st_fs;
+    float* dv = dv_g + blockIdx.x * st_fs;
+    const float one_m_omega = 1.0f - omega;
+    const int nsteps = D + 2 * (G - 1);
+    for (int s = 0; s < nsteps; ++s) {
+        for (int gi = 0; gi < G; ++gi) {
+            const int d = s - 2 * gi;
+            if (d < 0) break;
+            if (d >= D) continue;
+            const int r0 = d - (B - 1) > 0 ? d - (B - 1) : 0;
+            const int r1 = d < A - 1 ? d : A - 1;
+            for (int a = r0 + threadIdx.x; a <= r1; a += blockDim.x) {
+                const int b = d - a;
+                const long long o = (long long)d * P + a;
+                const long long om = o - P, op = o + P;  // same row on diagonals d - 1, d + 1
+                const float duc = du[o], dvc = dv[o];
+                const float duAm = a > 0 ? du[om - 1] : duc, dvAm = a > 0 ? dv[om - 1] : dvc;
+                const float duBm = b > 0 ? du[om] : duc, dvBm = b > 0 ? dv[om] : dvc;
+                const float duAp = a < A - 1 ? du[op + 1] : duc, dvAp = a < A - 1 ? dv[op + 1] : dvc;
+                const float duBp = b < B - 1 ? du[op] : duc, dvBp = b < B - 1 ? dv[op] : dvc;
+                const float A12 = cf[o], BU = cf[plane + o], BV = cf[2 * plane + o];
+                const float iDu = cf[3 * plane + o], iDv = cf[4 * plane + o];
+                const float nu = wa * (duAm + duAp) + wb * (duBm + duBp) + BU - A12 * dvc;
+                const float dun = one_m_omega * duc + omega * (nu * iDu);
+                const float nv = wa * (dvAm + dvAp) + wb * (dvBm + dvBp) + BV - A12 * dun;
+                const float dvn = one_m_omega * dvc + omega * (nv * iDv);
+                du[o] = dun;
+                dv[o] = dvn;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_sor_global(const float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                              int n_frames, DiagGeom g, int G, float wa, float wb, float omega, cudaStream_t st)
+{
+    const int threads = g.h >= 1024 ? 1024 : ((g.h + 31) / 32) * 32;
+    k_sor_global<<<n_frames, threads, 0, st>>>(coef, coef_fs, du, dv, st_fs, g, G, wa, wb, omega);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // 5x5 median with scipy's "mirror" boundary on du and dv (core/optical_flow.py:
 // 607-609), then u + du, v + dv on the interior (:610-611).
 // The median is a forgetful selection: keep 14 candidates, repeatedly drop the

@@ -22,8 +22,6 @@ namespace frg {
 
 namespace {
 
-constexpr int kRingFused = 2 * kGMax + 3;
-
 struct SorArgs {
     const float* J;      // [6][K][D*P] per frame
     long long J_fs;
@@ -141,8 +139,8 @@ __device__ __forceinline__ void put_raw(const SorArgs& A, const Raw<K>& r, float
     C1[a] = iDv;
 }
 
-template <int K, int PF>
-__global__ void __launch_bounds__(kMaxLane) k_sor_fused(SorArgs A)
+template <int K, int PF, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_sor_fused(SorArgs A)
 {
     extern __shared__ __align__(16) float sm[];
     const DiagGeom g = A.g;
@@ -275,24 +273,42 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_fused(SorArgs A)
     for (int e = nsteps - 2 * G > 0 ? nsteps - 2 * G : 0; e < D; ++e) writeback(e, e % R);
 }
 
-template <int K, int PF>
-cudaError_t run_fused(const SorArgs& A, int n_frames, cudaStream_t st)
+constexpr int kSmemLimit = 232448;  // 227 KB of dynamic shared memory per CTA
+
+template <int K, int PF, int MAXT>
+cudaError_t run_fused_t(const SorArgs& A, int n_frames, cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_sor_fused<K, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)((size_t)kRingFused * 7 * kMaxLane * sizeof(float)));
+        cudaError_t e = cudaFuncSetAttribute(k_sor_fused<K, PF, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmemLimit);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     const size_t smem = (size_t)(2 * A.G + 3) * 7 * A.g.P * sizeof(float);
-    k_sor_fused<K, PF><<<n_frames, A.g.P, smem, st>>>(A);
+    k_sor_fused<K, PF, MAXT><<<n_frames, A.g.P, smem, st>>>(A);
     return cudaGetLastError();
+}
+
+// up to 512 rows: registers for 512 threads; 513..1024 rows: 1024 threads
+template <int K, int PF>
+cudaError_t run_fused(const SorArgs& A, int n_frames, cudaStream_t st)
+{
+    if (A.g.P <= kMaxLane) return run_fused_t<K, PF, kMaxLane>(A, n_frames, st);
+    return run_fused_t<K, 1, 2 * kMaxLane>(A, n_frames, st);
 }
 
 }  // namespace
 
 bool sor_fused_supports(int K) { return K >= 1 && K <= 4; }
+
+int sor_fused_gmax(int P)
+{
+    if (P > 2 * kMaxLane) return 0;
+    for (int G = kGMax; G >= 1; --G)
+        if ((size_t)(2 * G + 3) * 7 * P * sizeof(float) <= (size_t)kSmemLimit) return G;
+    return 0;
+}
 
 cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
                              long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
@@ -300,7 +316,7 @@ cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, lon
                              float wx, float wy, float omega, cudaStream_t st, float* out_du, float* out_dv,
                              long long out_fs)
 {
-    if (g.P > kMaxLane || G < 1 || G > kGMax || (g.P & 31) || !sor_fused_supports(K)) return cudaErrorInvalidValue;
+    if (G < 1 || G > sor_fused_gmax(g.P) || (g.P & 31) || !sor_fused_supports(K)) return cudaErrorInvalidValue;
     SorArgs A;
     A.J = J;
     A.J_fs = J_fs;

@@ -164,6 +164,8 @@ def main():
     full["c_flow"] = of.get_displacement(fx, mv, alpha=(2.0, 1.0), a_smooth=0.7, weight=np.array([0.8, 0.2]),
                                          iterations=15)
     full["d_flow"] = of.get_displacement(fx, mv, const_assumption="gray", iterations=12, eta=0.7)
+    # min_level > 0: the finest levels are skipped and the flow is upsampled by cv2.resize (cubic)
+    full["e_flow"] = of.get_displacement(fx, mv, alpha=(1.5, 1.5), min_level=2, iterations=10)
     out["full"] = full
 
     for name, d in out.items():

@@ -94,6 +94,43 @@ def test_fp64_update_lag_and_shapes(oracle, lag, its):
     assert_parity(got, oracle.get_displacement(fixed, moving, **kw))
 
 
+@pytest.mark.parametrize("min_level", [2, 4, 6])
+def test_fp64_min_level_cubic_upsampling(oracle, golden_dir, min_level):
+    """Quality presets 'balanced' (4) and 'fast' (6) stop above full resolution
+    and upsample with cv2.resize INTER_CUBIC (core/optical_flow.py:615-616)."""
+    fixed, moving, _ = pair_256(5, h=96, w=120)
+    kw = dict(alpha=(1.5, 1.5), min_level=min_level, iterations=15)
+    ref = oracle.get_displacement(fixed, moving, **kw)
+    got = G.get_displacement(fixed, moving, precision="fp64", **kw)
+    assert got.shape == (96, 120, 2)
+    assert_parity(got, ref)
+    if min_level == 2:
+        f = np.load(f"{golden_dir}/full.npz")
+        kw2 = dict(alpha=(1.5, 1.5), min_level=2, iterations=10)
+        g2 = G.get_displacement(f["b_fixed"], f["b_moving"], precision="fp64", **kw2)
+        assert flow_diff(g2, f["e_flow"])[0] < 1e-3
+
+
+def test_fp32_min_level_runs_and_stays_close(oracle):
+    fixed, moving, _ = pair_256(5, h=96, w=120)
+    kw = dict(alpha=(1.5, 1.5), min_level=4, iterations=15)
+    base, env_max, env_epe = envelope(oracle, fixed, moving, kw)
+    mx, ep = flow_diff(G.get_displacement(fixed, moving, **kw), base)
+    assert mx <= 2 * env_max + 1e-3 and ep <= 2 * env_epe + 1e-4, (mx, ep, env_max, env_epe)
+
+
+@pytest.mark.parametrize("h,w", [(700, 96), (1100, 72)])
+def test_frames_taller_than_512_rows(oracle, h, w):
+    """Levels over 512 rows use the 1024-thread ring (up to 1024 rows) and the
+    global-memory wavefront (taller); fp64 parity, fp32 within the envelope."""
+    fixed, moving, _ = pair_256(10 + h, h=h, w=w)
+    kw = dict(alpha=(1.5, 1.5), iterations=10, levels=100)
+    base, env_max, env_epe = envelope(oracle, fixed, moving, kw, seeds=(1,))
+    assert_parity(G.get_displacement(fixed, moving, precision="fp64", **kw), base)
+    mx, ep = flow_diff(G.get_displacement(fixed, moving, **kw), base)
+    assert mx <= 2 * env_max + 1e-3 and ep <= 2 * env_epe + 1e-4, (mx, ep, env_max, env_epe)
+
+
 def test_fp64_tall_frame(oracle):
     fixed, moving, _ = pair_256(3, h=160, w=64)
     kw = dict(alpha=(1.5, 1.5), iterations=20)

@@ -32,6 +32,8 @@ def level_inputs(rng, h, w, K, oracle):
     (9, 9, 1, 50, 5), (21, 17, 2, 23, 3), (40, 64, 1, 50, 5), (64, 40, 2, 50, 5), (33, 35, 1, 12, 1),
     (50, 70, 2, 30, 7), (100, 120, 1, 50, 5), (250, 300, 2, 50, 5), (512, 512, 1, 10, 5),
     (30, 40, 4, 20, 5), (30, 40, 5, 20, 5), (45, 38, 6, 17, 7), (64, 64, 3, 24, 12),
+    # taller than 512 rows: 1024-thread ring with shorter passes, then the global-memory wavefront
+    (600, 80, 2, 20, 5), (900, 60, 1, 23, 5), (1030, 50, 2, 12, 5), (700, 30, 6, 10, 5),
 ])
 def test_level_solve_matches_lexicographic_oracle(oracle, h, w, K, its, lag):
     rng = np.random.default_rng(h * 7 + w)

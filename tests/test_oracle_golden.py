@@ -65,6 +65,9 @@ def test_full_displacement(oracle, golden_dir):
     d = oracle.get_displacement(f["b_fixed"], f["b_moving"], const_assumption="gray", iterations=12, eta=0.7,
                                 semantics="python")
     np.testing.assert_array_equal(d, f["d_flow"])
+    e = oracle.get_displacement(f["b_fixed"], f["b_moving"], alpha=(1.5, 1.5), min_level=2, iterations=10,
+                                semantics="python")
+    np.testing.assert_array_equal(e, f["e_flow"])
     an = oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
     assert np.abs(an - f["a_flow"]).max() < 1e-4
 
