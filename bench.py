@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--plain-frames", type=int, default=8, help="frames timed in the one-frame-per-call form")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames of the CPU baseline sample (0: one per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--diff-frames", type=int, default=64,
+                    help="frames of the differentiation workload (512x512x1); 0 skips it")
     return ap.parse_args()
 
 
@@ -75,6 +77,69 @@ def make_workload(n_frames: int, device, seed: int = 1, frame0: int = 50):
         reps = (n_frames + distinct - 1) // distinct
         frames = proc.repeat(reps, 1, 1, 1)[:n_frames].contiguous()
     return ref.contiguous(), frames
+
+
+def run_diff(args, dev):
+    """Differentiation workload: 64 frames of 512x512x1 from the same video
+    generator, loss = MSE(warp(moving, flow), unwarped truth) + 0.1 * mean
+    |flow - true flow|^2, gradients with respect to the moving frames, the
+    reference and alpha through the hand-written adjoint (per-level
+    checkpoints, recomputation of each level).  Times the forward (flow +
+    compensation warp + loss) and the backward separately on the device."""
+    import torch
+
+    from pyflowreg_gb300 import diff
+    from pyflowreg_gb300.synthetic import TorchVideo, preprocess_torch
+
+    F = args.diff_frames
+    vid = TorchVideo(seed=3, h=H, w=W, K=1, device=dev)
+    with torch.no_grad():
+        ref_raw = vid.frames(0, 50).mean(0)
+        lo, hi = float(ref_raw.min()), float(ref_raw.max())
+        moving = preprocess_torch(vid.frames(50, F), ref_raw).permute(0, 3, 1, 2).contiguous()
+        fixed = preprocess_torch(ref_raw, ref_raw).permute(2, 0, 1).contiguous()
+        tr = [vid.truth(50 + i) for i in range(F)]
+        truth = torch.stack([(t[0] - lo) / (hi - lo) for t in tr]).permute(0, 3, 1, 2).contiguous()
+        w_true = torch.stack([t[1] for t in tr]).permute(0, 3, 1, 2).contiguous()
+    opts = {k: OPTIONS[k] for k in ("levels", "eta", "iterations", "update_lag")}
+    stream = torch.cuda.current_stream()
+    modes = {}
+    for name, kw in (("implicit", dict(checkpoint="ticks", gradient="implicit")),
+                     ("unrolled", dict(checkpoint="ticks", gradient="unrolled")),
+                     ("unrolled_store_sweeps", dict(checkpoint="sweeps", gradient="unrolled"))):
+        plan = diff.DiffPlan(H, W, 1, F, dtype=torch.float32, **kw, **opts)
+        plan.set_weight([1.0])
+        fwd_ms, bwd_ms, loss_v = [], [], None
+        for rep in range(1 + max(args.steps, 1)):
+            m = moving.clone().requires_grad_(True)
+            f = fixed.clone().requires_grad_(True)
+            a = torch.tensor(float(OPTIONS["alpha"][0]), dtype=torch.float32, device=dev, requires_grad=True)
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            loss = diff.registration_loss(f, m, truth, w_true, a, plan)
+            e1.record(stream)
+            loss.backward()
+            e2.record(stream)
+            torch.cuda.synchronize()
+            if rep > 0:
+                fwd_ms.append(e0.elapsed_time(e1))
+                bwd_ms.append(e1.elapsed_time(e2))
+            loss_v = float(loss.detach())
+        fw, bw = float(np.median(fwd_ms)), float(np.median(bwd_ms))
+        modes[name] = {**kw, "fwd_ms": fw, "bwd_ms": bw, "ratio": bw / fw, "fwd_frames_per_s": F / (fw / 1e3),
+                       "loss": loss_v, "grad_moving_norm": float(m.grad.norm()),
+                       "plan_device_bytes": plan.device_bytes(), "reps": len(fwd_ms)}
+        plan.close()
+        del plan
+        torch.cuda.empty_cache()
+    head = modes["implicit"]
+    return {"workload": f"{F} x 512x512x1 photon-count frames, registration loss (lambda 0.1)",
+            "dtype": "f32", "pixel_order": "gauss_seidel",
+            "headline": "implicit: per level one red-black SOR solve of M lam = dL/dx on the level's operator "
+                        "(psi held at its last tick); checkpoints per level (resized frames, input flow, "
+                        "solver state at each psi tick), the last window and J recomputed",
+            "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
 
 
 def weight_tensor(device):
@@ -297,6 +362,7 @@ def run_gb300(args):
     parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, parity = cpu_baseline(args, ref, frames, out)
+    backward = run_diff(args, dev) if (rank == 0 and args.diff_frames > 0) else None
 
     if rank == 0:
         line = {
@@ -324,7 +390,8 @@ def run_gb300(args):
             "roofline": roofline,
             "plain": plain,
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
-            "bwd_fwd_ratio": None,
+            "bwd_fwd_ratio": backward["ratio"] if backward else None,
+            "backward": backward,
             "clocks": clocks,
             "cpu_baseline": cpu,
             "parity": parity,

@@ -200,6 +200,87 @@ int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy,
 /* 5x5 median with mirror boundary of one plane (h, w), h, w >= 3. */
 int frg_median5(int h, int w, const float* src, float* dst, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiable mode.
+ *
+ * pyflowreg's flow path with the level solver of its torch backend
+ * ("flowreg_torch": torch/core/level_solver.py:11-199, registered at
+ * core/__init__.py:140-197; red-black order, eps = 1e-6, psi tick when
+ * it % update_lag == 0; within-pixel order selectable, below) and a continuous warp (the map is not rounded to
+ * 1/32 px as cv2.remap does in core/warping.py:160-234; Keys cubic,
+ * replicated borders, out-of-bounds pixels from the reference frame).  The
+ * reference runs that backend under torch.no_grad(); these entry points add
+ * what it has no counterpart for: the gradient of the flow with respect to
+ * both frames and alpha.  frg_diff_forward stores per-level checkpoints (the
+ * resized frames, the level's input flow and the solver state at every psi
+ * tick); frg_diff_backward recomputes each level from them and runs the
+ * adjoint sweeps.  Supported: gradient constancy, a_smooth = 1, min_level 0.
+ *
+ * Arrays are device memory, planar: frames (F, K, H, W), flows (F, 2, H, W)
+ * with plane 0 = u (columns) and plane 1 = v (rows).  The element type is
+ * float for a plan created with precision FRG_FP32 and double for
+ * FRG_FP64_REFERENCE (the pointers below are void* for that reason).
+ * ------------------------------------------------------------------------- */
+typedef struct frg_diff_plan frg_diff_plan;
+
+/* Plan flags.
+ * FRG_DIFF_TORCH_ORDER: the torch backend's within-pixel order, du and dv of
+ *   a moving pixel both from the old values: a Jacobi step on the 2x2 pixel
+ *   block, which diverges with omega = 1.95 wherever |A12| / sqrt(A11 A22)
+ *   > 2 / omega - 1 (most data-dominated pixels of a gradient-constancy
+ *   tensor).  Without it (default) dv is taken from the new du, the numba
+ *   solver's order (core/level_solver.py:355-364): the sweep is then SOR on a
+ *   symmetric positive definite system and converges for omega < 2.
+ * FRG_DIFF_STORE_SWEEPS: the forward keeps the pixels moved by every
+ *   half-sweep (2 * iterations * F * h * ceil(w / 2) * 2 elements per level)
+ *   and the backward reads them; without it the forward keeps the state at
+ *   each psi tick only and the backward recomputes each window. */
+#define FRG_DIFF_TORCH_ORDER 1
+#define FRG_DIFF_STORE_SWEEPS 2
+/* Backward flag FRG_DIFF_LAGGED_PSI: hold psi fixed at each tick (the adjoint
+ * of the lagged-nonlinearity system); without it the gradient also runs
+ * through psi = a (E + 1e-6)^(a - 1), whose slope near E = 0 (~1e9) makes it
+ * exact but stiff. */
+#define FRG_DIFF_LAGGED_PSI 1
+/* Backward flag FRG_DIFF_IMPLICIT: per level, hold psi at its last tick and
+ * differentiate the fixed point of the level system M x = b (M symmetric
+ * positive definite, the operator the sweeps iterate) instead of the
+ * unrolled iterations: lam = M^-1 dL/dx by one red-black SOR solve of
+ * `iterations` sweeps on the same operator, then dL/db = lam and
+ * dL/dM = -lam x^T with x the level's final state.  Exact for a converged
+ * forward; an approximation of the unrolled gradient otherwise. */
+#define FRG_DIFF_IMPLICIT 2
+
+int frg_diff_plan_create(const frg_params* params, int height, int width, int channels, int max_frames, int flags,
+                         frg_diff_plan** out);
+void frg_diff_plan_destroy(frg_diff_plan* plan);
+size_t frg_diff_plan_device_bytes(const frg_diff_plan* plan);
+int frg_diff_plan_num_levels(const frg_diff_plan* plan);
+/* Replaces the tap tables of one level (same layout as frg_plan_set_level_tables). */
+int frg_diff_set_level_tables(frg_diff_plan* plan, int level, int kind, int taps, const int* ix, const float* wx,
+                              const int* iy, const float* wy);
+/* weight: (K, H, W) device array of the plan's element type. */
+int frg_diff_set_weight(frg_diff_plan* plan, const void* weight, void* stream);
+/* flow_out (F, 2, H, W); uv_init (F, 2, H, W) or NULL for zero.  alpha_x,
+ * alpha_y override the plan's (the values the backward differentiates at). */
+int frg_diff_forward(frg_diff_plan* plan, int n_frames, double alpha_x, double alpha_y, const void* fixed,
+                     const void* moving, const void* uv_init, void* flow_out, void* stream);
+/* Gradient of a loss L given g_flow = dL/dflow (F, 2, H, W) for the last
+ * frg_diff_forward: g_fixed, g_moving (F, K, H, W) are overwritten;
+ * g_alpha (F, 2) device doubles are overwritten with dL/d(alpha_x, alpha_y)
+ * per frame.  Any of the outputs may be NULL. */
+int frg_diff_backward(frg_diff_plan* plan, const void* g_flow, void* g_fixed, void* g_moving, double* g_alpha,
+                      int flags, void* stream);
+/* Continuous compensation warp out = src(x + flow) with out-of-bounds pixels
+ * from fill (motion_correction/parallelization/sequential.py:300-307), and its
+ * adjoint (g_src, g_fill, g_flow overwritten; any may be NULL except g_src).
+ * precision selects float (FRG_FP32) or double (FRG_FP64_REFERENCE). */
+int frg_diff_warp(int precision, int n_frames, int channels, int height, int width, const void* src,
+                  const void* flow, const void* fill, void* out, void* stream);
+int frg_diff_warp_backward(int precision, int n_frames, int channels, int height, int width, const void* src,
+                           const void* flow, const void* g_out, void* g_src, void* g_fill, void* g_flow,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

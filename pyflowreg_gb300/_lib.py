@@ -99,6 +99,16 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_resize", I, [I, I, I, P, I, I, P, P])
         _sig(lib, "frg_motion_tensor", I, [I, I, P, P, D, D, I, P, P])
         _sig(lib, "frg_median5", I, [I, I, P, P, P])
+        _sig(lib, "frg_diff_plan_create", I, [pP, I, I, I, I, I, ctypes.POINTER(P)])
+        _sig(lib, "frg_diff_plan_destroy", None, [P])
+        _sig(lib, "frg_diff_plan_device_bytes", S, [P])
+        _sig(lib, "frg_diff_plan_num_levels", I, [P])
+        _sig(lib, "frg_diff_set_level_tables", I, [P, I, I, I, pI, pF, pI, pF])
+        _sig(lib, "frg_diff_set_weight", I, [P, P, P])
+        _sig(lib, "frg_diff_forward", I, [P, I, D, D, P, P, P, P, P])
+        _sig(lib, "frg_diff_backward", I, [P, P, P, P, P, I, P])
+        _sig(lib, "frg_diff_warp", I, [I, I, I, I, I, P, P, P, P, P])
+        _sig(lib, "frg_diff_warp_backward", I, [I, I, I, I, I, P, P, P, P, P, P, P])
         _lib = lib
         return lib
 

@@ -1227,3 +1227,18 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream)
 }
 
 }  // extern "C"
+
+// Host helpers shared with frg_diff_api.cu (declared in frg_internal.h).
+namespace frg {
+int host_fail(int code, const std::string& msg) { return fail(code, msg); }
+void host_count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int host_warping_depth(double eta, int levels, int m, int n) { return warping_depth(eta, levels, m, n); }
+double host_resize_sigma(int ih, int iw, int oh, int ow) { return resize_sigma(ih, iw, oh, ow); }
+int host_make_tables(int in_len, int out_len, double sigma, std::vector<int32_t>& idx, std::vector<float>& wt)
+{
+    HostTables t = make_tables(in_len, out_len, sigma);
+    idx = std::move(t.idx);
+    wt = std::move(t.wt);
+    return t.P;
+}
+}  // namespace frg

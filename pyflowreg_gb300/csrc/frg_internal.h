@@ -5,6 +5,9 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
+#include <vector>
+
 namespace frg {
 
 constexpr int kMaxK = 8;        // channels per frame handled by one plan
@@ -116,5 +119,86 @@ cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, in
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
+
+// Host helpers of frg_api.cu shared with the differentiable mode's C ABI
+// (frg_diff_api.cu).
+int host_fail(int code, const std::string& msg);
+void host_count_launches(long long n);
+int host_warping_depth(double eta, int levels, int m, int n);
+double host_resize_sigma(int ih, int iw, int oh, int ow);
+// Tap tables of the fused Gauss-cubic resize (util/resize_util.py:194-229).
+int host_make_tables(int in_len, int out_len, double sigma, std::vector<int32_t>& idx, std::vector<float>& wt);
+
+namespace diff {
+
+// Inverse (CSR) form of a resize tap table: for each source index a, the
+// entries ptr[a] .. ptr[a+1]-1 list the output indices idx[e] whose taps
+// read a, with weight w[e].
+struct Csr {
+    const int32_t* ptr;
+    const int32_t* idx;
+    const float* w;
+};
+
+// Differentiable-mode launchers (frg_diff.cu), T = float or double.  Arrays
+// are planar row-major: images (F, K, h, w), flows / solver states (F, 2, h, w),
+// J (F, 6, K, h, w), coefficients (F, 5, h, w).
+template <typename T>
+cudaError_t resize(const T* src, long long planes, int ih, int iw, int oh, int ow, const int32_t* ix, const float* wx,
+                   int Px, const int32_t* iy, const float* wy, int Py, T* tmp, T* dst, cudaStream_t st);
+template <typename T>
+cudaError_t resize_t(const T* gdst, long long planes, int oh, int ow, int ih, int iw, const Csr& cx, const Csr& cy,
+                     T* tmp, T* gsrc, int accumulate, cudaStream_t st);
+template <typename T>
+cudaError_t warp(const T* f2, const T* f1, const T* uv, int F, int K, int h, int w, double hcol, double hrow, T* out,
+                 cudaStream_t st);
+template <typename T>
+cudaError_t warp_adj(const T* f2, const T* uv, const T* gout, int F, int K, int h, int w, double hcol, double hrow,
+                     T* gf2, T* gf1, T* guv, cudaStream_t st);
+template <typename T>
+cudaError_t tensor(const T* f1, const T* f2, int F, int K, int h, int w, double hy, double hx, T* J, cudaStream_t st);
+template <typename T>
+cudaError_t tensor_adj(const T* f1, const T* f2, const T* gJ, int F, int K, int h, int w, double hy, double hx, T* G,
+                       T* gf1, T* gf2, int accumulate_f1, cudaStream_t st);
+// Solver: coefficients (F, 5, h, w) = max(A11, eps), max(A22, eps), A12, B1e,
+// B2e with the input flow's Laplacian folded into B1e, B2e.  States are full
+// (F, 2, h, w) arrays; a half-sweep's moved pixels can also be stored
+// compressed (F, 2, h, (w + 1) / 2).  gs = 1: dv of a moving pixel from its
+// new du (numba's within-pixel order); gs = 0: from the old du (torch backend).
+template <typename T>
+cudaError_t tick(const T* J, const T* W, const T* stt, const T* uv, int F, int K, int h, int w, const double* a_data,
+                 double eps, double ax, double ay, T* coef, T* ck, cudaStream_t st);
+// rhs (F, 2, h, w) or NULL: with it the sweep solves M lam = rhs (B1e, B2e
+// replaced by -rhs) for the level's symmetric operator M.
+template <typename T>
+cudaError_t rb_sweep(int color, const T* coef, const T* rhs, T* state, T* store, int F, int h, int w, double ax,
+                     double ay, double omega, double eps, int gs, cudaStream_t st);
+// Implicit adjoint assembly: gcoef (overwritten) and galpha from lam = M^-1 g
+// and the level's final state x.
+template <typename T>
+cudaError_t implicit_assemble(const T* lam, const T* x, int F, int h, int w, T* gcoef, double sx, double sy,
+                              double* galpha, cudaStream_t st);
+// Adjoint of half-sweep j (colour `color`) over the pixels it moves: first
+// their gather of w * aprev (the (au, av) of step j + 1, compressed; NULL for
+// the window's last half-sweep), then their own step, writing anext.  pre
+// state: per colour a compressed array (pre_c0 / pre_c1) or, when that is
+// NULL, the full array pre_full (NULL: zero).  galpha (F, 2) += (sx, sy) *
+// d/d(ax, ay).  rb_adj_gather closes a window (the gather of step 0).
+template <typename T>
+cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pre_c0, const T* pre_c1, T* lam,
+                        const T* aprev, T* anext, int F, int h, int w, double ax, double ay, double omega, double eps,
+                        int gs, T* gcoef, double sx, double sy, double* galpha, cudaStream_t st);
+template <typename T>
+cudaError_t rb_adj_gather(int color, T* lam, const T* aprev, int F, int h, int w, double ax, double ay,
+                          cudaStream_t st);
+template <typename T>
+cudaError_t tick_adj(const T* J, const T* W, const T* stt, const T* uv, const T* gcoef, int F, int K, int h, int w,
+                     const double* a_data, double eps, double ax, double ay, int lagged, T* gJ, T* lam, T* guv,
+                     double sx, double sy, double* galpha, cudaStream_t st);
+template <typename T>
+cudaError_t median_add(const T* d, const T* uv_in, T* uv_out, int F, int h, int w, int median, cudaStream_t st);
+template <typename T>
+cudaError_t median_adj(const T* d, const T* g, int32_t* am, int F, int h, int w, T* gd, cudaStream_t st);
+}  // namespace diff
 
 }  // namespace frg

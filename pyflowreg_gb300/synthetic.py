@@ -209,6 +209,20 @@ class TorchVideo:
             out[i] = self.frame(t0 + i)
         return out
 
+    def truth(self, t: int):
+        """(unwarped noise-free frame (h, w, K) at frame t's mean count, true
+        flow (h, w, 2) with moving(x + flow(x)) = unwarped(x))."""
+        torch = self.torch
+        rng = np.random.default_rng(1000 * self.seed + t)
+        shift = rng.normal(0.0, self.shift_std, 2)
+        lam = float(rng.uniform(50.0, 2000.0))
+        phase = 2.0 * np.pi * t / self.period
+        img = torch.stack([lam * torch.clamp(self._blobs(k, self.yy, self.xx) / 2.0, min=0.0) for k in range(self.K)],
+                          dim=2)
+        u, v = self._field(self.yy, self.xx, phase)
+        flow = torch.stack([u + float(shift[0]), v + float(shift[1])], dim=2)
+        return img, flow
+
 
 def preprocess_torch(frames, ref_raw, sigma=1.0, truncate=4.0):
     """Normalise by the raw reference's joint min/max and blur each channel with
