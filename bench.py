@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--diff-frames", type=int, default=64,
                     help="frames of the differentiation workload (512x512x1); 0 skips it")
+    ap.add_argument("--diff-modes", default="implicit,unrolled,unrolled_store_sweeps",
+                    help="gradient modes timed in the differentiation workload")
+    ap.add_argument("--only-diff", action="store_true",
+                    help="run only the differentiation workload (for profiling); prints its JSON object")
     return ap.parse_args()
 
 
@@ -104,9 +108,11 @@ def run_diff(args, dev):
     opts = {k: OPTIONS[k] for k in ("levels", "eta", "iterations", "update_lag")}
     stream = torch.cuda.current_stream()
     modes = {}
-    for name, kw in (("implicit", dict(checkpoint="ticks", gradient="implicit")),
-                     ("unrolled", dict(checkpoint="ticks", gradient="unrolled")),
-                     ("unrolled_store_sweeps", dict(checkpoint="sweeps", gradient="unrolled"))):
+    all_modes = {"implicit": dict(checkpoint="ticks", gradient="implicit"),
+                 "unrolled": dict(checkpoint="ticks", gradient="unrolled"),
+                 "unrolled_store_sweeps": dict(checkpoint="sweeps", gradient="unrolled")}
+    for name in args.diff_modes.split(","):
+        kw = all_modes[name]
         plan = diff.DiffPlan(H, W, 1, F, dtype=torch.float32, **kw, **opts)
         plan.set_weight([1.0])
         fwd_ms, bwd_ms, loss_v = [], [], None
@@ -133,12 +139,14 @@ def run_diff(args, dev):
         plan.close()
         del plan
         torch.cuda.empty_cache()
-    head = modes["implicit"]
+    head = modes.get("unrolled") or next(iter(modes.values()))
     return {"workload": f"{F} x 512x512x1 photon-count frames, registration loss (lambda 0.1)",
             "dtype": "f32", "pixel_order": "gauss_seidel",
-            "headline": "implicit: per level one red-black SOR solve of M lam = dL/dx on the level's operator "
-                        "(psi held at its last tick); checkpoints per level (resized frames, input flow, "
-                        "solver state at each psi tick), the last window and J recomputed",
+            "headline": "unrolled: the exact gradient (every half-sweep reversed, psi ticks differentiated); "
+                        "checkpoints per level (resized frames, input flow, solver state at each psi tick), "
+                        "each tick window and J recomputed in the backward.  'implicit' holds psi at its last "
+                        "tick and differentiates the level's fixed point with one SOR solve on the same "
+                        "operator: cheaper, but at a_data = 0.45 it misses most of the exact derivative",
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
 
 
@@ -492,6 +500,12 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.only_diff:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_diff(args, torch.device("cuda", 0))))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
