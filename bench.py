@@ -56,6 +56,10 @@ def parse():
                     help="frames of the differentiation workload (512x512x1); 0 skips it")
     ap.add_argument("--diff-modes", default="implicit,unrolled,unrolled_store_sweeps",
                     help="gradient modes timed in the differentiation workload")
+    ap.add_argument("--uneven-frames", type=int, default=256,
+                    help="frames of the uneven-size batch (sizes 256^2, 512^2, 796x512, 1024^2; 1-2 channels); 0 skips")
+    ap.add_argument("--stream-frames", type=int, default=128,
+                    help="frames of the 2048x2048x2 streaming workload (batches of 32); 0 skips")
     ap.add_argument("--only-diff", action="store_true",
                     help="run only the differentiation workload (for profiling); prints its JSON object")
     return ap.parse_args()
@@ -148,6 +152,130 @@ def run_diff(args, dev):
                         "tick and differentiates the level's fixed point with one SOR solve on the same "
                         "operator: cheaper, but at a_data = 0.45 it misses most of the exact derivative",
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
+
+
+def run_uneven(args, dev):
+    """Uneven-size batch: frames drawn uniformly from {256^2, 512^2, 796x512,
+    1024^2} x {1, 2} channels, each size/channel pair a video of its own
+    registered to the mean of its first 50 frames; one register() call for all
+    frames (groups on 4 streams, launch sequences replayed as CUDA graphs)."""
+    import torch
+
+    from pyflowreg_gb300.batch import UnevenBatch
+    from pyflowreg_gb300.synthetic import TorchVideo, preprocess_torch
+
+    sizes = [(256, 256), (512, 512), (796, 512), (1024, 1024)]
+    rng = np.random.default_rng(2)
+    draws = [(sizes[rng.integers(4)], int(rng.integers(1, 3))) for _ in range(args.uneven_frames)]
+    refs, frames = {}, []
+    with torch.no_grad():
+        for bi, ((h, w), k) in enumerate(sorted(set(draws))):
+            vid = TorchVideo(seed=20 + bi, h=h, w=w, K=k, device=dev)
+            ref_raw = vid.frames(0, 50).mean(0)
+            refs[(h, w, k)] = (vid, ref_raw, preprocess_torch(ref_raw, ref_raw).contiguous())
+        counters = {}
+        for (hw, k) in draws:
+            key = (hw[0], hw[1], k)
+            vid, ref_raw, _ = refs[key]
+            t = 50 + counters.get(key, 0)
+            counters[key] = counters.get(key, 0) + 1
+            frames.append(preprocess_torch(vid.frame(t), ref_raw).contiguous())
+    opts = dict(OPTIONS)
+    opts.pop("min_level", None)
+    ub = UnevenBatch({k: v[2] for k, v in refs.items()}, graphs=True, **opts)
+    ub.register(frames)  # plans, graph capture
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(args.steps, 1)
+    e0.record(stream)
+    for _ in range(reps):
+        ub.register(frames)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ub.close()
+    counts = {f"{k[0]}x{k[1]}x{k[2]}": v for k, v in sorted(counters.items())}
+    return {"workload": f"{len(frames)} frames of mixed size and channels, one register() call",
+            "frames_per_size": counts, "ms_per_batch": ms, "frames_per_s": len(frames) / (ms / 1e3),
+            "graphs": True, "streams": 4}
+
+
+def run_stream(args, dev):
+    """Large-frame stream: 2048x2048x2 frames registered in batches of 32
+    through StreamRegistrar (pinned host buffers, copies on a side stream
+    overlapping compute).  The frames are the reference (3000 blobs per
+    channel) warped by a rigid drift of up to 20 px plus a sinusoid field,
+    with Poisson counts; they are rendered before the timed region into pinned
+    host memory, which the source hands over without a copy."""
+    import time
+
+    import torch
+    import torch.nn.functional as Fnn
+
+    from pyflowreg_gb300.stream import StreamRegistrar
+    from pyflowreg_gb300.synthetic import preprocess_torch
+
+    Hs = Ws = 2048
+    Ks, N, B = 2, args.stream_frames, 32
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    yy, xx = torch.meshgrid(torch.arange(Hs, device=dev, dtype=torch.float32),
+                            torch.arange(Ws, device=dev, dtype=torch.float32), indexing="ij")
+    ref = torch.full((Ks, Hs, Ws), 0.05, device=dev)
+    with torch.no_grad():
+        for k in range(Ks):
+            n = 3000
+            cy, cx = torch.rand(n, generator=g, device=dev) * Hs, torch.rand(n, generator=g, device=dev) * Ws
+            sg = 2 + 4 * torch.rand(n, generator=g, device=dev)
+            am = 0.3 + 0.7 * torch.rand(n, generator=g, device=dev)
+            for i0 in range(0, n, 100):
+                sl = slice(i0, i0 + 100)
+                # each blob on a 49 x 49 window around its centre
+                oy = torch.arange(-24, 25, device=dev, dtype=torch.float32)
+                py = (cy[sl, None].floor() + oy[None]).long()
+                px = (cx[sl, None].floor() + oy[None]).long()
+                gy = torch.exp(-(py.float() - cy[sl, None]) ** 2 / (2 * sg[sl, None] ** 2))
+                gx = torch.exp(-(px.float() - cx[sl, None]) ** 2 / (2 * sg[sl, None] ** 2))
+                vals = am[sl, None, None] * gy[:, :, None] * gx[:, None, :]
+                ok = (py[:, :, None] >= 0) & (py[:, :, None] < Hs) & (px[:, None, :] >= 0) & (px[:, None, :] < Ws)
+                idx = (py[:, :, None] * Ws + px[:, None, :])
+                ref[k].view(-1).index_add_(0, idx[ok], vals[ok])
+        host = torch.empty((N, Hs, Ws, Ks), dtype=torch.float32).pin_memory()
+        frames_raw = []
+        for t in range(N):
+            drift = 20.0 * min(1.0, t / max(N - 1, 1))
+            ph = 2 * np.pi * t / 250.0
+            u = drift * 0.8 + 2.0 * torch.sin(2 * np.pi * yy / 300.0 + ph)
+            v = drift * 0.6 + 2.0 * torch.cos(2 * np.pi * xx / 260.0 + ph)
+            grid = torch.stack([(xx - u) / (Ws - 1) * 2 - 1, (yy - v) / (Hs - 1) * 2 - 1], dim=-1)[None]
+            mov = Fnn.grid_sample(ref[None], grid, mode="bicubic", padding_mode="border", align_corners=True)[0]
+            lam = 50.0 + 1950.0 * float(torch.rand((), generator=g, device=dev))
+            cnt = torch.poisson(lam * mov.clamp(min=0) / 2.0, generator=g)
+            frames_raw.append(cnt.permute(1, 2, 0))
+        ref_raw = torch.stack(frames_raw[:min(50, N)]).mean(0)
+        for t in range(N):
+            host[t].copy_(preprocess_torch(frames_raw[t], ref_raw))
+        refp = preprocess_torch(ref_raw, ref_raw).contiguous()
+        del frames_raw
+    opts = dict(OPTIONS)
+    opts.pop("min_level", None)
+    sr = StreamRegistrar(refp, batch=B, **opts)
+    sink_count = [0]
+
+    def sink(t0, flows):
+        sink_count[0] += len(flows)
+
+    sr.run(lambda t0, n: host[t0:t0 + n], min(N, 2 * B), sink)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    info = sr.run(lambda t0, n: host[t0:t0 + n], N, sink)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    sr.close()
+    return {"workload": f"{N} x 2048x2048x2 frames, batches of {B}, pinned host in/out, copies on a side stream",
+            "frames_per_s": N / dt, "seconds": dt, "h2d_bytes": info["h2d_bytes"], "d2h_bytes": info["d2h_bytes"],
+            "timing": "wall clock around StreamRegistrar.run after a warm-up run"}
 
 
 def weight_tensor(device):
@@ -371,6 +499,8 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, parity = cpu_baseline(args, ref, frames, out)
     backward = run_diff(args, dev) if (rank == 0 and args.diff_frames > 0) else None
+    uneven = run_uneven(args, dev) if (rank == 0 and args.uneven_frames > 0) else None
+    stream_2048 = run_stream(args, dev) if (rank == 0 and args.stream_frames > 0) else None
 
     if rank == 0:
         line = {
@@ -400,6 +530,8 @@ def run_gb300(args):
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
             "bwd_fwd_ratio": backward["ratio"] if backward else None,
             "backward": backward,
+            "uneven_batch": uneven,
+            "stream_2048": stream_2048,
             "clocks": clocks,
             "cpu_baseline": cpu,
             "parity": parity,

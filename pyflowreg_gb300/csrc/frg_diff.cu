@@ -381,10 +381,11 @@ struct AData {
 //   nu = -(B1e + A12 dv_c) + ax (du_L + du_R) + ay (du_T + du_B)
 // which is the reference's -sum_k W psi (J13 + J12 dv) + sum_n w_n (u_n + du_n - u_c).
 
-// Sums (va, vb) over the block into dst[0], dst[1]: the reduction runs in T,
-// one double atomic per block and value.  Every thread of the block calls it.
+// Sums (va, vb) over the block and adds them to slot[0], slot[1], a pair
+// owned by this block (no atomics: launches on one stream run in order and no
+// other block of a launch writes the slot).  Every thread of the block calls it.
 template <typename T>
-__device__ __forceinline__ void block_add2(T va, T vb, double* dst)
+__device__ __forceinline__ void block_add2(T va, T vb, double* slot)
 {
     for (int o = 16; o > 0; o >>= 1) {
         va += __shfl_down_sync(0xffffffffu, va, o);
@@ -406,11 +407,47 @@ __device__ __forceinline__ void block_add2(T va, T vb, double* dst)
             vb += __shfl_down_sync(0xffffffffu, vb, o);
         }
         if (lane == 0) {
-            if (va != (T)0) atomicAdd(dst, (double)va);
-            if (vb != (T)0) atomicAdd(dst + 1, (double)vb);
+            slot[0] += (double)va;
+            slot[1] += (double)vb;
         }
     }
     __syncthreads();
+}
+
+// The slot of this block in a per-launch-shape partial buffer: one pair per
+// (frame, row, block column).
+__device__ __forceinline__ double* block_slot(double* part)
+{
+    return part + ((((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x) + blockIdx.x) * 2;
+}
+
+// galpha(f, :) += sum of frame f's n_slots pairs, which are then cleared.
+__global__ void kd_reduce_slots(double* __restrict__ part, long long n_slots, double* __restrict__ galpha)
+{
+    const long long f = blockIdx.x;
+    double* p = part + f * n_slots * 2;
+    double a = 0, b = 0;
+    for (long long i = threadIdx.x; i < n_slots; i += blockDim.x) {
+        a += p[2 * i];
+        b += p[2 * i + 1];
+        p[2 * i] = 0;
+        p[2 * i + 1] = 0;
+    }
+    __shared__ double ra[256], rb[256];
+    ra[threadIdx.x] = a;
+    rb[threadIdx.x] = b;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            ra[threadIdx.x] += ra[threadIdx.x + st];
+            rb[threadIdx.x] += rb[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        galpha[2 * f] += ra[0];
+        galpha[2 * f + 1] += rb[0];
+    }
 }
 
 // Solver state before a half-sweep: the values of each colour either from a
@@ -593,7 +630,7 @@ __global__ void kd_rb_adj_step(int color, const T* __restrict__ coef, StateSrc<T
         gax = (au * Xdu + av * Xdv - rr) * (T)sx;
         gay = (au * Ydu + av * Ydv - rr) * (T)sy;
     }
-    block_add2(gax, gay, galpha + f * 2);
+    block_add2(gax, gay, block_slot(galpha));
 }
 
 // The closing gather of a window: pixels of colour `color` (which did not move
@@ -650,7 +687,7 @@ __global__ void kd_implicit_assemble(const T* __restrict__ lam, const T* __restr
         gax = -(lu * ((T)2 * duc - du[pL] - du[pR]) + lv * ((T)2 * dvc - dv[pL] - dv[pR])) * (T)sx;
         gay = -(lu * ((T)2 * duc - du[pT] - du[pB]) + lv * ((T)2 * dvc - dv[pT] - dv[pB])) * (T)sy;
     }
-    block_add2(gax, gay, galpha + f * 2);
+    block_add2(gax, gay, block_slot(galpha));
 }
 
 // Adjoint of a psi tick and of the folded input flow, once per window:
@@ -751,7 +788,7 @@ __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, co
         gax = -(gb1 * lxu + gb2 * lxv) * (T)sx;
         gay = -(gb1 * lyu + gb2 * lyv) * (T)sy;
     }
-    block_add2(gax, gay, galpha + f * 2);
+    block_add2(gax, gay, block_slot(galpha));
 }
 
 // ------------------------------------------------------------------ median
@@ -949,6 +986,12 @@ cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pr
     kd_rb_adj_step<T><<<grid_rows((w + 1) / 2, h, F), 128, 0, st>>>(color, coef, pre, lam, aprev, anext, h, w, (T)ax,
                                                                     (T)ay, (T)omega, (T)eps, gs, gcoef, sx, sy,
                                                                     galpha);
+    return cudaGetLastError();
+}
+
+cudaError_t reduce_slots(double* part, int F, long long n_slots, double* galpha, cudaStream_t st)
+{
+    kd_reduce_slots<<<F, 256, 0, st>>>(part, n_slots, galpha);
     return cudaGetLastError();
 }
 

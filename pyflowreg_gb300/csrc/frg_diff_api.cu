@@ -129,6 +129,8 @@ struct frg_diff_plan {
     void* gcoef = nullptr;   // (F, 5, hw)
     void* guv = nullptr;     // (F, 2, hw)
     void* galpha = nullptr;  // (F, 2) doubles, when the caller passes none
+    double* partA = nullptr; // per-block alpha partials of the half-sweep adjoints (F, H, ceil(ceil(W/2)/128), 2)
+    double* partB = nullptr; // per-block alpha partials of the per-pixel adjoints (F, H, ceil(W/128), 2)
     void* gJ = nullptr;      // (F, 6, K, hw)
     void* G = nullptr;       // (F, K, 5, hw)
     void* gf1 = nullptr;     // (F, K, hw)
@@ -289,6 +291,9 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
     if (g_moving) DCUDA(cudaMemsetAsync(g_moving, 0, (size_t)F * K * H * W * es, st));
     double* galpha = g_alpha ? g_alpha : (double*)pl->galpha;
     DCUDA(cudaMemsetAsync(galpha, 0, (size_t)F * 2 * sizeof(double), st));
+    const int W2 = (W + 1) / 2;
+    DCUDA(cudaMemsetAsync(pl->partA, 0, (size_t)F * H * ((W2 + 127) / 128) * 2 * sizeof(double), st));
+    DCUDA(cudaMemsetAsync(pl->partB, 0, (size_t)F * H * ((W + 127) / 128) * 2 * sizeof(double), st));
     int go = 0;
     DCUDA(cudaMemcpyAsync(pl->gout[go], g_flow, (size_t)F * 2 * H * W * es, cudaMemcpyDeviceToDevice, st));
     for (int li = (int)pl->levels.size() - 1; li >= 0; --li) {
@@ -344,9 +349,9 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
             for (int it = 0; it < I; ++it)
                 for (int c = 0; c < 2; ++c)
                     DLAUNCH(1, rb_sweep<T>(c, coef, g, lam, (T*)nullptr, F, h, w, L.ax, L.ay, om, kEps, 1, st));
-            DLAUNCH(1, implicit_assemble<T>(lam, fin, F, h, w, gcoef, sx, sy, galpha, st));
+            DLAUNCH(1, implicit_assemble<T>(lam, fin, F, h, w, gcoef, sx, sy, pl->partB, st));
             DLAUNCH(1, tick_adj<T>(J, Wl, s0, uv, gcoef, F, K, h, w, pl->a_data, kEps, L.ax, L.ay, 1, gJ, (T*)nullptr,
-                                   guv, sx, sy, galpha, st));
+                                   guv, sx, sy, pl->partB, st));
         }
         for (int k = implicit ? -1 : pl->n_ticks - 1; k >= 0; --k) {
             const int start = k * lag, n_it = std::min(lag, I - start), n_half = 2 * n_it;
@@ -385,13 +390,15 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
                 const T* c1 = c == 0 ? oth : own;
                 T* anext = abuf[j & 1];
                 DLAUNCH(1, rb_adj_step<T>(c, coef, s0, c0, c1, lam, aprev, anext, F, h, w, L.ax, L.ay, om, kEps,
-                                          pl->gs, gcoef, sx, sy, galpha, st));
+                                          pl->gs, gcoef, sx, sy, pl->partA, st));
                 aprev = anext;
             }
             DLAUNCH(1, rb_adj_gather<T>(1, lam, aprev, F, h, w, L.ax, L.ay, st));
             DLAUNCH(1, tick_adj<T>(J, Wl, s0, uv, gcoef, F, K, h, w, pl->a_data, kEps, L.ax, L.ay, lagged, gJ,
-                                   s0 ? lam : (T*)nullptr, guv, sx, sy, galpha, st));
+                                   s0 ? lam : (T*)nullptr, guv, sx, sy, pl->partB, st));
         }
+        DLAUNCH(1, reduce_slots(pl->partA, F, (long long)h * (((w + 1) / 2 + 127) / 128), galpha, st));
+        DLAUNCH(1, reduce_slots(pl->partB, F, (long long)h * ((w + 127) / 128), galpha, st));
         T* gf1 = (T*)pl->gf1;
         T* gf2w = (T*)pl->gf2w;
         DLAUNCH(2, tensor_adj<T>(f1, f2w, gJ, F, K, h, w, L.h_row, L.h_col, (T*)pl->G, gf1, gf2w, 0, st));
@@ -514,7 +521,9 @@ int frg_diff_plan_create(const frg_params* params, int height, int width, int ch
          (rc = dalloc(pl, &pl->abuf[0], F * 2 * height * ((width + 1) / 2) * es)) ||
          (rc = dalloc(pl, &pl->abuf[1], F * 2 * height * ((width + 1) / 2) * es)) ||
          (rc = dalloc(pl, &pl->gcoef, F * 5 * hw * es)) || (rc = dalloc(pl, &pl->guv, F * 2 * hw * es)) ||
-         (rc = dalloc(pl, &pl->galpha, F * 2 * sizeof(double))) || (rc = dalloc(pl, &pl->gJ, F * 6 * K * hw * es)) ||
+         (rc = dalloc(pl, &pl->galpha, F * 2 * sizeof(double))) ||
+         (rc = dalloc_t(pl, &pl->partA, F * height * (size_t)(((width + 1) / 2 + 127) / 128) * 2)) ||
+         (rc = dalloc_t(pl, &pl->partB, F * height * (size_t)((width + 127) / 128) * 2)) || (rc = dalloc(pl, &pl->gJ, F * 6 * K * hw * es)) ||
          (rc = dalloc(pl, &pl->G, F * 5 * K * hw * es)) || (rc = dalloc(pl, &pl->gf1, F * K * hw * es)) ||
          (rc = dalloc(pl, &pl->gf2w, F * K * hw * es)) || (rc = dalloc(pl, &pl->gf2l, F * K * hw * es)) ||
          (rc = dalloc(pl, &pl->gout[0], F * 2 * hw * es)) || (rc = dalloc(pl, &pl->gout[1], F * 2 * hw * es)) ||

@@ -178,6 +178,11 @@ cudaError_t rb_sweep(int color, const T* coef, const T* rhs, T* state, T* store,
 template <typename T>
 cudaError_t implicit_assemble(const T* lam, const T* x, int F, int h, int w, T* gcoef, double sx, double sy,
                               double* galpha, cudaStream_t st);
+// The adjoint kernels add their alpha gradients to per-block partial pairs
+// (galpha arguments below): (F, h, ceil(n / 128), 2) doubles for a launch over
+// n pixels of each row.  reduce_slots adds frame f's n_slots pairs to galpha
+// (F, 2) and clears them.
+cudaError_t reduce_slots(double* part, int F, long long n_slots, double* galpha, cudaStream_t st);
 // Adjoint of half-sweep j (colour `color`) over the pixels it moves: first
 // their gather of w * aprev (the (au, av) of step j + 1, compressed; NULL for
 // the window's last half-sweep), then their own step, writing anext.  pre

@@ -1,0 +1,79 @@
+"""Uneven batches (frames of several sizes in one call, optionally replayed as
+CUDA graphs) and streaming registration with overlapped copies: both must give
+exactly the flows of direct per-group calls."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+OPTS = dict(alpha=(1.5, 1.5), levels=100, eta=0.8, iterations=20, update_lag=5, a_data=0.45)
+
+
+def _frames(key, n, seed):
+    from pyflowreg_gb300.synthetic import TorchVideo, preprocess_torch
+
+    H, W, K = key
+    vid = TorchVideo(seed=seed, h=H, w=W, K=K, n_blobs=12, device="cuda")
+    raw = vid.frames(0, n + 4)
+    ref_raw = raw[:4].mean(0)
+    return preprocess_torch(ref_raw, ref_raw).contiguous(), preprocess_torch(raw[4:], ref_raw).contiguous()
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_uneven_batch_equals_per_group_calls(graphs):
+    from pyflowreg_gb300 import api
+    from pyflowreg_gb300.batch import UnevenBatch
+
+    shapes = [(64, 64, 1), (80, 96, 2), (128, 112, 1), (72, 48, 2)]
+    counts = [5, 3, 4, 2]
+    refs, frames, keys = {}, [], []
+    for i, (key, n) in enumerate(zip(shapes, counts)):
+        ref, fr = _frames(key, n, 10 + i)
+        refs[key] = ref
+        frames += [fr[j] for j in range(n)]
+        keys += [key] * n
+    order = np.random.default_rng(0).permutation(len(frames))
+    frames = [frames[i] for i in order]
+    keys = [keys[i] for i in order]
+    ub = UnevenBatch(refs, graphs=graphs, **OPTS)
+    for _ in range(2):  # the second call replays the captured graphs
+        got = ub.register(frames)
+    torch.cuda.synchronize()
+    for key in shapes:
+        idx = [i for i, k in enumerate(keys) if k == key]
+        plan = api.Plan(api.make_params(K=key[2], **OPTS), *key, len(idx))
+        plan.set_reference(refs[key])
+        ref = plan.displacement(torch.stack([frames[i] for i in idx]))
+        torch.cuda.synchronize()
+        for j, i in enumerate(idx):
+            assert torch.equal(got[i], ref[j]), key
+        plan.close()
+    ub.close()
+
+
+def test_stream_registrar_equals_batch_loop():
+    from pyflowreg_gb300 import api
+    from pyflowreg_gb300.stream import StreamRegistrar
+
+    key = (96, 80, 2)
+    ref, fr = _frames(key, 45, 3)
+    host = fr.cpu().numpy()
+    out = np.zeros((45, key[0], key[1], 2), np.float32)
+
+    def sink(t0, flows):
+        out[t0:t0 + len(flows)] = flows
+
+    sr = StreamRegistrar(ref, batch=16, **OPTS)
+    info = sr.run(lambda t0, n: host[t0:t0 + n], 45, sink)
+    sr.close()
+    assert info["frames"] == 45
+    plan = api.Plan(api.make_params(K=2, **OPTS), *key, 16)
+    plan.set_reference(ref)
+    w = torch.zeros((key[0], key[1], 2), dtype=torch.float32, device="cuda")
+    for t0 in range(0, 45, 16):
+        n = min(16, 45 - t0)
+        f = plan.displacement(fr[t0:t0 + n].contiguous(), w)
+        np.testing.assert_array_equal(out[t0:t0 + n], f.cpu().numpy())
+        w = f[max(0, n - 20):n].mean(0).contiguous()
+    plan.close()
