@@ -60,6 +60,8 @@ def parse():
                     help="frames of the uneven-size batch (sizes 256^2, 512^2, 796x512, 1024^2; 1-2 channels); 0 skips")
     ap.add_argument("--stream-frames", type=int, default=128,
                     help="frames of the 2048x2048x2 streaming workload (batches of 32); 0 skips")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default SOR launch shape instead of tuning it on the workload first")
     ap.add_argument("--only-diff", action="store_true",
                     help="run only the differentiation workload (for profiling); prints its JSON object")
     return ap.parse_args()
@@ -396,6 +398,12 @@ def run_gb300(args):
         if world > 1:
             dist.barrier()
 
+    tuning = None
+    if not args.no_autotune:
+        # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
+        chosen = plan.autotune(frames, n_levels=4, reps=1)
+        tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)": {"G": g, "threads": t}
+                  for i, (g, t, _) in chosen.items()}
     for _ in range(max(args.warmup, 3)):
         plan.displacement(frames, None, out)
     torch.cuda.synchronize()
@@ -521,7 +529,8 @@ def run_gb300(args):
                        "channels": K, "options": {**OPTIONS, "alpha": list(OPTIONS["alpha"]),
                                                   "weight": list(WEIGHT)},
                        "l2": "inputs larger than L2 (%.0f MB per step)" % (T * H * W * K * 4 / 1e6),
-                       "parallelism": f"frames sharded over {world} GPU(s)"},
+                       "parallelism": f"frames sharded over {world} GPU(s)",
+                       "sor_launch_tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": T * H * W * K * 4,
                     "d2h_bytes_per_step": T * H * W * 2 * 4},
             "gpu_launches": int(launches),

@@ -113,6 +113,15 @@ int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double*
 int frg_plan_set_level_tables(frg_plan* plan, int level, int kind, int taps, const int* ix, const float* wx,
                               const int* iy, const float* wy);
 
+/* Tuning of one level's fused SOR launches (no reference counterpart; the
+ * results do not change, only the launch shape): sor_G iterations per
+ * wavefront pass (0: the most the shared-memory ring holds, reported as gmax)
+ * and sor_threads threads per CTA (0: the level's rows rounded up to 32,
+ * reported as rows; else a multiple of 32 in [rows, 1024]).  Levels that do
+ * not use the fused kernel report gmax 0 and accept only (0, 0). */
+int frg_plan_set_level_tuning(frg_plan* plan, int level, int sor_G, int sor_threads);
+int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_threads, int* gmax, int* rows);
+
 /* Reference (fixed) frame (height, width, channels) float32 and the per-pixel
  * channel weight (height, width, channels) float32 (NULL: 1/channels), as
  * get_displacement receives them after its input normalisation

@@ -221,6 +221,61 @@ class Plan:
         _lib.check(self.lib.frg_plan_profile(self.handle, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
         return n.value, ms.value, b.value
 
+    def level_tuning(self):
+        """[(sor_G, sor_threads, gmax, rows)] per level, coarsest first (gmax 0:
+        the level does not use the fused SOR kernel)."""
+        out = []
+        for i in range(self.lib.frg_plan_num_levels(self.handle)):
+            v = [ctypes.c_int() for _ in range(4)]
+            _lib.check(self.lib.frg_plan_level_tuning(self.handle, i, *[ctypes.byref(x) for x in v]))
+            out.append(tuple(x.value for x in v))
+        return out
+
+    def set_level_tuning(self, level: int, sor_G: int = 0, sor_threads: int = 0) -> None:
+        _lib.check(self.lib.frg_plan_set_level_tuning(self.handle, level, sor_G, sor_threads),
+                   "frg_plan_set_level_tuning")
+
+    def autotune(self, moving_t, n_levels: int = 5, reps: int = 2):
+        """Picks, for the `n_levels` finest levels that use the fused SOR kernel,
+        the iterations per wavefront pass and the threads per CTA that make
+        full calls on `moving_t` (a representative device batch) fastest:
+        coordinate descent from the finest level, each candidate timed with
+        CUDA events (best of `reps`).  The flows do not depend on the choice.
+        Returns {level: (sor_G, sor_threads, ms)}."""
+        tun = self.level_tuning()
+        out_t = torch.empty((moving_t.shape[0], self.H, self.W, 2), dtype=torch.float32, device=moving_t.device)
+
+        def timed():
+            best = float("inf")
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self.displacement(moving_t, None, out_t)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            return best
+
+        self.displacement(moving_t, None, out_t)
+        torch.cuda.synchronize()
+        chosen = {}
+        levels = [i for i in range(len(tun) - 1, -1, -1) if tun[i][2] > 0][:n_levels]
+        for i in levels:
+            _, _, gmax, rows = tun[i]
+            # every pass length: short passes free shared memory for a second CTA per SM
+            gs = list(range(gmax, 0, -1))
+            ths = sorted({t for t in (rows, ((rows * 3 // 2) + 31) // 32 * 32, 1024) if rows <= t <= 1024})
+            best = None
+            for g in gs:
+                for t in ths:
+                    self.set_level_tuning(i, g, t)
+                    ms = timed()
+                    if best is None or ms < best[2]:
+                        best = (g, t, ms)
+            self.set_level_tuning(i, best[0], best[1])
+            chosen[i] = best
+        return chosen
+
     def set_reference(self, fixed_t, weight_t=None, stream=None, key=None):
         """fixed_t (H, W, K) float32 CUDA tensor; weight_t the same shape or None."""
         if key is not None and key == self._ref_key:

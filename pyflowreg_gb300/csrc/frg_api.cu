@@ -269,6 +269,8 @@ struct LevelPlan {
     float* ref = nullptr;    // (K, h, w) reference level
     float* wdiag = nullptr;  // (K, D*P) weight level, diagonal-major
     double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
+    int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
+    int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
 };
 
 // Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
@@ -436,11 +438,13 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
                 long long W_fs, const float* lap, long long lap_fs, float* du, float* dv,
                 long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
                 const float* a_data, float wx, float wy, float omega, cudaStream_t st,
-                SorProfile* prof = nullptr, float* rm_du = nullptr, float* rm_dv = nullptr, long long rm_fs = 0)
+                SorProfile* prof = nullptr, float* rm_du = nullptr, float* rm_dv = nullptr, long long rm_fs = 0,
+                int tune_G = 0, int tune_threads = 0)
 {
     const SorKind kind = sor_kind(K, g);
     const bool fused = kind == kSorFused;
-    const int gmax = kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag);
+    int gmax = kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag);
+    if (fused && tune_G > 0 && tune_G < gmax) gmax = tune_G;
     const std::vector<Pass> passes = make_passes(iterations, update_lag, gmax);
     for (size_t pi = 0; pi < passes.size(); ++pi) {
         const Pass& ps = passes[pi];
@@ -458,7 +462,7 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
             FRG_LAUNCH(launch_sor_fused(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, T, K, g, ps.G,
                                         ps.fold_mode, (ps.fold_mode >= 0 && continued) ? 1 : 0, a_data, wx, wy,
                                         omega, st, final_pass ? rm_du : nullptr, final_pass ? rm_dv : nullptr,
-                                        rm_fs));
+                                        rm_fs, tune_threads));
         } else if (kind == kSorRows) {
             // thread index runs along rows: rows are the a-direction (weight wy)
             FRG_LAUNCH(launch_sor(coef, coef_fs, du, dv, st_fs, T, g, ps.G, wy, wx, omega, st));
@@ -764,6 +768,35 @@ int frg_plan_level_info(const frg_plan* plan, int level, int* h, int* w, double*
     return FRG_OK;
 }
 
+int frg_plan_set_level_tuning(frg_plan* plan, int level, int sor_G, int sor_threads)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    LevelPlan& L = plan->levels[level];
+    if (sor_kind(plan->K, L.g) != kSorFused) {
+        if (sor_G != 0 || sor_threads != 0) return fail(FRG_EINVAL, "this level does not use the fused SOR kernel");
+        return FRG_OK;
+    }
+    const int gmax = sor_fused_gmax(L.g.P);
+    if (sor_G < 0 || sor_G > gmax) return fail(FRG_EINVAL, "sor_G out of range for this level");
+    if (sor_threads != 0 && (sor_threads < L.g.P || sor_threads > 2 * kMaxLane || (sor_threads & 31)))
+        return fail(FRG_EINVAL, "sor_threads must be 0 or a multiple of 32 in [rows rounded up to 32, 1024]");
+    L.sor_G = sor_G;
+    L.sor_threads = sor_threads;
+    return FRG_OK;
+}
+
+int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_threads, int* gmax, int* rows)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    const LevelPlan& L = plan->levels[level];
+    const bool fused = sor_kind(plan->K, L.g) == kSorFused;
+    if (sor_G) *sor_G = L.sor_G;
+    if (sor_threads) *sor_threads = L.sor_threads;
+    if (gmax) *gmax = fused ? sor_fused_gmax(L.g.P) : 0;
+    if (rows) *rows = L.g.P;
+    return FRG_OK;
+}
+
 int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, void* stream)
 {
     if (!pl || !fixed) return fail(FRG_EINVAL, "plan or fixed is NULL");
@@ -868,7 +901,7 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         const bool fused = sor_kind(K, L.g) == kSorFused;
         int rc = solve_level(pl->p.iterations, pl->p.update_lag, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du,
                              pl->dv, dp, pl->coef, 5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st,
-                             &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw);
+                             &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw, L.sor_G, L.sor_threads);
         if (rc) return rc;
         // 6. median + accumulate (core/optical_flow.py:607-611)
         const int do_median = std::min(h, w) > 5 ? 1 : 0;

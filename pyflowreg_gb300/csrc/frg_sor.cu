@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(MAXT) k_sor_fused(SorArgs A)
 constexpr int kSmemLimit = 232448;  // 227 KB of dynamic shared memory per CTA
 
 template <int K, int PF, int MAXT>
-cudaError_t run_fused_t(const SorArgs& A, int n_frames, cudaStream_t st)
+cudaError_t run_fused_t(const SorArgs& A, int n_frames, int threads, cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
@@ -286,16 +286,18 @@ cudaError_t run_fused_t(const SorArgs& A, int n_frames, cudaStream_t st)
         attr = true;
     }
     const size_t smem = (size_t)(2 * A.G + 3) * 7 * A.g.P * sizeof(float);
-    k_sor_fused<K, PF, MAXT><<<n_frames, A.g.P, smem, st>>>(A);
+    k_sor_fused<K, PF, MAXT><<<n_frames, threads, smem, st>>>(A);
     return cudaGetLastError();
 }
 
-// up to 512 rows: registers for 512 threads; 513..1024 rows: 1024 threads
+// threads per CTA: at least the rows of the longest diagonal (P), at most
+// 1024.  Up to 512 threads: the variant with registers for 512 threads and
+// the deeper prefetch; above: the 1024-thread variant.
 template <int K, int PF>
-cudaError_t run_fused(const SorArgs& A, int n_frames, cudaStream_t st)
+cudaError_t run_fused(const SorArgs& A, int n_frames, int threads, cudaStream_t st)
 {
-    if (A.g.P <= kMaxLane) return run_fused_t<K, PF, kMaxLane>(A, n_frames, st);
-    return run_fused_t<K, 1, 2 * kMaxLane>(A, n_frames, st);
+    if (threads <= kMaxLane) return run_fused_t<K, PF, kMaxLane>(A, n_frames, threads, st);
+    return run_fused_t<K, 1, 2 * kMaxLane>(A, n_frames, threads, st);
 }
 
 }  // namespace
@@ -314,9 +316,11 @@ cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, lon
                              long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
                              int n_frames, int K, DiagGeom g, int G, int mode, int store_coef, const float* a_data,
                              float wx, float wy, float omega, cudaStream_t st, float* out_du, float* out_dv,
-                             long long out_fs)
+                             long long out_fs, int threads)
 {
     if (G < 1 || G > sor_fused_gmax(g.P) || (g.P & 31) || !sor_fused_supports(K)) return cudaErrorInvalidValue;
+    if (threads <= 0) threads = g.P;
+    if (threads < g.P || threads > 2 * kMaxLane || (threads & 31)) return cudaErrorInvalidValue;
     SorArgs A;
     A.J = J;
     A.J_fs = J_fs;
@@ -342,10 +346,10 @@ cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, lon
     A.omega = omega;
     for (int k = 0; k < kMaxK; ++k) A.a_data[k] = k < K ? a_data[k] : 0.0f;
     switch (K) {
-        case 1: return run_fused<1, 2>(A, n_frames, st);
-        case 2: return run_fused<2, 2>(A, n_frames, st);
-        case 3: return run_fused<3, 1>(A, n_frames, st);
-        default: return run_fused<4, 1>(A, n_frames, st);
+        case 1: return run_fused<1, 2>(A, n_frames, threads, st);
+        case 2: return run_fused<2, 2>(A, n_frames, threads, st);
+        case 3: return run_fused<3, 1>(A, n_frames, threads, st);
+        default: return run_fused<4, 1>(A, n_frames, threads, st);
     }
 }
 

@@ -77,3 +77,23 @@ def test_stream_registrar_equals_batch_loop():
         np.testing.assert_array_equal(out[t0:t0 + n], f.cpu().numpy())
         w = f[max(0, n - 20):n].mean(0).contiguous()
     plan.close()
+
+
+def test_autotuned_plan_gives_identical_flows():
+    """The launch-shape tuning (iterations per wavefront pass, threads per CTA)
+    changes no result bit."""
+    from pyflowreg_gb300 import api
+
+    key = (200, 168, 2)
+    ref, fr = _frames(key, 6, 5)
+    plan = api.Plan(api.make_params(K=2, **OPTS), *key, 6)
+    plan.set_reference(ref)
+    base = plan.displacement(fr).clone()
+    chosen = plan.autotune(fr, n_levels=3, reps=1)
+    assert chosen
+    tuned = plan.displacement(fr)
+    assert torch.equal(base, tuned)
+    for i, (g, t, ms) in chosen.items():
+        plan.set_level_tuning(i, max(1, g - 1), 1024)
+    assert torch.equal(base, plan.displacement(fr))
+    plan.close()
