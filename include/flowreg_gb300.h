@@ -209,6 +209,34 @@ int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy,
 /* 5x5 median with mirror boundary of one plane (h, w), h, w >= 3. */
 int frg_median5(int h, int w, const float* src, float* dst, void* stream);
 
+/* Preprocessing of frames before the flow, as compensate_recording does it
+ * (motion_correction/compensate_recording.py:521-561, normalize and
+ * apply_gaussian_filter in util/image_processing.py:12-165): out =
+ * gaussian(normalise(raw)) with normalise(x) = (x - lo[k]) / den[k] and a
+ * separable Gaussian in axis order time, rows, columns, scipy's "reflect"
+ * mode and scipy's symmetric correlation order.  raw, out (n_frames, height,
+ * width, channels) float32 on the device; lo, den host arrays (channels);
+ * rt, ry, rx host arrays of the radius per channel; wt, wy, wx device
+ * arrays of taps w[0..r_k] per channel, stored with stride (max_k r_k + 1);
+ * f32_norm: normalise in float32 (numpy's result for float32 frames and
+ * reference), else float64; f32_storage: keep the normalised values and each
+ * pass's output in float32 (joint normalisation of float32 data), else
+ * float64 (per-channel normalisation writes into a float64 array); tmp holds
+ * n_frames * channels * height * width values of the storage type. */
+int frg_preprocess(int n_frames, int height, int width, int channels, const float* raw, const double* lo,
+                   const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                   const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, void* stream);
+
+/* Post-registration pass over flows (n_frames, height, width, 2) float32:
+ * valid (n_frames, height, width) uint8 0/255 masks of the backward warp
+ * (core/warping.py:14-60, compute_batch_valid_masks; may be NULL) and stats
+ * (n_frames, 4) float64 on the device: mean |w|, max |w|, mean divergence
+ * (np.gradient), |mean w| (motion_correction/compensate_recording.py:808-821).
+ * workspace: frg_flow_post_workspace bytes of device memory. */
+size_t frg_flow_post_workspace(int n_frames, int height, int width);
+int frg_flow_post(int n_frames, int height, int width, const float* flow, unsigned char* valid, void* workspace,
+                  double* stats, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Differentiable mode.
  *

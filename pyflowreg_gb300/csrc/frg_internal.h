@@ -122,6 +122,14 @@ cudaError_t launch_x_median_accum(const double* du, const double* dv, const doub
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
 
+// Preprocessing and post-registration statistics (frg_prep.cu).
+// taps w[k][0 .. r] stored with stride (max_k r + 1); radii per channel (host arrays)
+cudaError_t launch_preprocess(const float* raw, int T, int H, int W, int K, const double* lo, const double* den,
+                              const double* wt, const int* rt, const double* wy, const int* ry, const double* wx,
+                              const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, cudaStream_t st);
+cudaError_t launch_flow_post(const float* flow, int T, int H, int W, uint8_t* valid, double* part, double* stats,
+                             cudaStream_t st);
+
 // Host helpers of frg_api.cu shared with the differentiable mode's C ABI
 // (frg_diff_api.cu).
 int host_fail(int code, const std::string& msg);
