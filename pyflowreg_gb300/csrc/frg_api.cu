@@ -350,6 +350,11 @@ struct frg_plan {
     int32_t* up_sy = nullptr;
     float* up_wy = nullptr;
     double* xtmp = nullptr;   // fp64 width-pass buffer (T, 2, h_min, W)
+    // a_smooth != 1 runs on the reference-order kernels in both precisions
+    bool xpath = false;       // precision == FRG_FP64_REFERENCE or a_smooth != 1
+    double* xpsis = nullptr;  // (T, m*n) smoothness weights
+    double* xsnap = nullptr;  // (T, 2, m*n) state snapshot for the psi_s border
+    double* xflow = nullptr;  // (T, H, W, 2) fp64 flow of an fp32 plan on this path
 };
 
 namespace {
@@ -487,8 +492,7 @@ int check_params(const frg_params* p, int K)
     if (p->iterations < 1) return fail(FRG_EINVAL, "iterations must be >= 1");
     if (p->update_lag < 1) return fail(FRG_EINVAL, "update_lag must be >= 1");
     if (p->min_level < 0) return fail(FRG_EINVAL, "min_level must be >= 0");
-    if (p->a_smooth != 1.0)
-        return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
+    if (!(p->a_smooth > 0.0)) return fail(FRG_EINVAL, "a_smooth must be > 0");
     if (p->const_assumption != 0 && p->const_assumption != 1)
         return fail(FRG_EUNSUPPORTED, "only the 'gc' and 'gray' constancy assumptions are supported");
     for (int k = 0; k < K; ++k)
@@ -497,6 +501,8 @@ int check_params(const frg_params* p, int K)
         return fail(FRG_EINVAL, "precision must be FRG_FP32 or FRG_FP64_REFERENCE");
     return FRG_OK;
 }
+
+int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out, cudaStream_t st);
 
 }  // namespace
 
@@ -562,6 +568,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     pl->K = channels;
     pl->max_T = max_frames;
     for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
+    pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0;
 
     // schedule: core/optical_flow.py:494-518
     const int m = height, n = width;
@@ -605,7 +612,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         HostTables fx = make_tables(L.fw, L.w, sigf), fy = make_tables(L.fh, L.h, sigf);
         if ((rc = upload_tables(pl, fx, L.w, fy, L.h, &L.flow))) { frg_plan_destroy(pl); return rc; }
         if ((rc = dev_alloc(pl, &L.ref, (size_t)channels * L.h * L.w))) { frg_plan_destroy(pl); return rc; }
-        if (params->precision == FRG_FP64_REFERENCE)
+        if (pl->xpath)
             rc = dev_alloc(pl, &L.wpad64, (size_t)channels * (L.h + 2) * (L.w + 2));
         else
             rc = dev_alloc(pl, &L.wdiag, (size_t)channels * L.g.D * L.g.P);
@@ -636,7 +643,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             frg_plan_destroy(pl);
             return fail(FRG_ECUDA, cudaGetErrorString(e));
         }
-        if (params->precision == FRG_FP64_REFERENCE &&
+        if (pl->xpath &&
             (rc = dev_alloc(pl, &pl->xtmp, (size_t)max_frames * 2 * Lm.h * width))) {
             frg_plan_destroy(pl);
             return rc;
@@ -651,7 +658,17 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         frg_plan_destroy(pl);
         return rc;
     }
-    if (params->precision == FRG_FP64_REFERENCE) {
+    if (pl->xpath) {
+        if (params->a_smooth != 1.0 &&
+            ((rc = dev_alloc(pl, &pl->xpsis, T * max_pad)) || (rc = dev_alloc(pl, &pl->xsnap, T * 2 * max_pad)))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
+        if (params->precision == FRG_FP32 &&
+            (rc = dev_alloc(pl, &pl->xflow, T * 2 * (size_t)height * width))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
         if ((rc = dev_alloc(pl, &pl->xJ, T * 6 * K * max_pad)) || (rc = dev_alloc(pl, &pl->xwp, T * K * max_pad)) ||
             (rc = dev_alloc(pl, &pl->xdu, T * max_pad)) || (rc = dev_alloc(pl, &pl->xdv, T * max_pad)) ||
             (rc = dev_alloc(pl, &pl->xuv, T * 2 * max_pad)) || (rc = dev_alloc(pl, &pl->xacc[0], T * 2 * max_hw)) ||
@@ -803,7 +820,7 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
     cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
     const float* wsrc = weight ? weight : pl->ones;
-    if (pl->p.precision == FRG_FP64_REFERENCE) {
+    if (pl->xpath) {
         for (LevelPlan& L : pl->levels) {
             const long long hw = (long long)L.h * L.w, mn = (long long)(L.h + 2) * (L.w + 2);
             FRG_LAUNCH(launch_x_resize_h_f(fixed, 0, 1, (long long)W * K, K, 1, K, H, pl->tmp, L.w, L.img.ix,
@@ -846,6 +863,13 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         return fail(FRG_EINVAL, "this plan computes in fp64: use frg_get_displacement_f64");
     cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
+    if (pl->xpath) {
+        // a_smooth != 1: the reference-order kernels, rounded to float32 at the end
+        int rc = run_xpath(pl, T, moving, uv_init, pl->xflow, st);
+        if (rc) return rc;
+        FRG_LAUNCH(launch_x_to_float(pl->xflow, (long long)T * H * W * 2, flow_out, st));
+        return FRG_OK;
+    }
     const long long fsz = (long long)H * W * K;
     int cur = 0;
     const LevelPlan* prev = nullptr;
@@ -932,15 +956,14 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
     return FRG_OK;
 }
 
-int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out,
-                             void* stream)
+}  // extern "C"
+
+namespace {
+
+// The reference-order level loop (float64 solver), for FP64 plans and for
+// a_smooth != 1 in either precision.
+int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out, cudaStream_t st)
 {
-    if (!pl || !moving || !flow_out) return fail(FRG_EINVAL, "NULL argument");
-    if (!pl->has_ref) return fail(FRG_EINVAL, "frg_set_reference has not been called");
-    if (T < 1 || T > pl->max_T) return fail(FRG_EINVAL, "n_frames out of range for this plan");
-    if (pl->p.precision != FRG_FP64_REFERENCE)
-        return fail(FRG_EINVAL, "this plan computes in fp32: use frg_get_displacement");
-    cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
     const long long fsz = (long long)H * W * K;
     int cur = 0;
@@ -982,9 +1005,19 @@ int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const flo
         }
         FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1, pl->p.const_assumption,
                                    pl->xJ, st));
-        FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv, pl->xwp, T, K, h, w,
-                                L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations, pl->p.update_lag,
-                                pl->a_data64, pl->p.omega, st));
+        if (pl->p.a_smooth == 1.0) {
+            FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv, pl->xwp, T, K,
+                                    h, w, L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations,
+                                    pl->p.update_lag, pl->a_data64, pl->p.omega, st));
+        } else {
+            long long n_launch = 0;
+            cudaError_t e = launch_x_sor_smooth(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv,
+                                                pl->xwp, pl->xpsis, pl->xsnap, T, K, h, w, L.alpha_x, L.alpha_y,
+                                                L.h_col, L.h_row, pl->p.iterations, pl->p.update_lag, pl->a_data64,
+                                                pl->p.a_smooth, pl->p.omega, st, &n_launch);
+            g_launches.fetch_add(n_launch, std::memory_order_relaxed);
+            if (e != cudaSuccess) return fail(FRG_ECUDA, std::string("launch_x_sor_smooth: ") + cudaGetErrorString(e));
+        }
         const int do_median = std::min(h, w) > 5 ? 1 : 0;
         const bool last = (li + 1 == pl->levels.size());
         if (last && pl->min_level == 0) {
@@ -1004,6 +1037,21 @@ int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const flo
                                            pl->up_sy, pl->up_wy, st));
     }
     return FRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out,
+                             void* stream)
+{
+    if (!pl || !moving || !flow_out) return fail(FRG_EINVAL, "NULL argument");
+    if (!pl->has_ref) return fail(FRG_EINVAL, "frg_set_reference has not been called");
+    if (T < 1 || T > pl->max_T) return fail(FRG_EINVAL, "n_frames out of range for this plan");
+    if (pl->p.precision != FRG_FP64_REFERENCE)
+        return fail(FRG_EINVAL, "this plan computes in fp32: use frg_get_displacement");
+    return run_xpath(pl, T, moving, uv_init, flow_out, (cudaStream_t)stream);
 }
 
 int frg_imregister(int n_frames, int height, int width, int channels, const float* frames, const float* flow,

@@ -405,6 +405,242 @@ cudaError_t launch_x_sor(const double* J, const double* W, const double* u, cons
 }
 
 // ---------------------------------------------------------------------------
+// a_smooth != 1 (core/level_solver.py:69-155, 229-255, 309-340).  The
+// smoothness weights psi_s need every pixel's u + du at the start of a tick
+// iteration, so the wavefront is cut at the ticks: kx_smooth_tick computes the
+// data weights W psi and psi_s over the whole padded grid, kx_sor_range runs
+// the iterations up to the next tick.  psi_s reads the border of du, dv as
+// set_boundary_2d last left it: at the start of the previous iteration, i.e.
+// the interior values then, taken at clamped coordinates.  kx_sor_range
+// snapshots every pixel's value before its update in the range's last
+// iteration for that purpose.
+// ---------------------------------------------------------------------------
+__global__ void kx_smooth_init(const double* __restrict__ W, double* __restrict__ wp, double* __restrict__ psi_s,
+                               double* __restrict__ snap, int K, long long mn)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long f = blockIdx.y;
+    if (i >= mn) return;
+    for (int k = 0; k < K; ++k) wp[(f * K + k) * mn + i] = W[(long long)k * mn + i];
+    psi_s[f * mn + i] = 1.0;
+    snap[f * 2 * mn + i] = 0.0;
+    snap[f * 2 * mn + mn + i] = 0.0;
+}
+
+__global__ void kx_smooth_tick(const double* __restrict__ J, const double* __restrict__ W,
+                               const double* __restrict__ u, const double* __restrict__ v, long long uv_fs,
+                               const double* __restrict__ du_g, const double* __restrict__ dv_g,
+                               const double* __restrict__ snap, double* __restrict__ wp_g, double* __restrict__ psi_g,
+                               int K, int h, int w, double hx, double hy, XAData ad, double a_s)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // column of the padded grid
+    const int j = blockIdx.y;                              // row of the padded grid
+    const long long f = blockIdx.z;
+    const int n = w + 2, m = h + 2;
+    if (i >= n) return;
+    const long long mn = (long long)m * n, o = (long long)j * n + i;
+    const double* du = du_g + f * mn;
+    const double* dv = dv_g + f * mn;
+    const double* sn = snap + f * 2 * mn;
+    const double* uf = u + f * uv_fs;
+    const double* vf = v + f * uv_fs;
+    const bool interior = j >= 1 && j <= m - 2 && i >= 1 && i <= n - 2;
+    if (interior) {
+        // data weights (core/level_solver.py:230-246), as kx_sor computes them
+        const double duc = du[o], dvc = dv[o];
+        const double* Jf = J + f * 6 * K * mn;
+        const long long qs = (long long)K * mn;
+        for (int k = 0; k < K; ++k) {
+            const long long ok = (long long)k * mn + o;
+            double val = dmul(dmul(Jf[ok], duc), duc);
+            val = dadd(val, dmul(dmul(Jf[qs + ok], dvc), dvc));
+            val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
+            val = dadd(val, dmul(dmul(dmul(2.0, Jf[3 * qs + ok]), duc), dvc));
+            val = dadd(val, dmul(dmul(2.0, Jf[4 * qs + ok]), duc));
+            val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
+            val = dadd(val, Jf[2 * qs + ok]);
+            if (val < 0.0) val = 0.0;
+            const double psi = dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0)));
+            wp_g[(f * K + k) * mn + o] = dmul(W[ok], psi);
+        }
+    }
+    // u + du at padded (jj, ii): the interior now, the border as set_boundary_2d left it
+    auto full = [&](int jj, int ii, int plane) {
+        const long long q = (long long)jj * n + ii;
+        const bool in = jj >= 1 && jj <= m - 2 && ii >= 1 && ii <= n - 2;
+        double d;
+        if (in)
+            d = plane ? dv[q] : du[q];
+        else
+            d = sn[(long long)plane * mn + (long long)xclamp(jj, 1, m - 2) * n + xclamp(ii, 1, n - 2)];
+        return dadd(plane ? vf[q] : uf[q], d);
+    };
+    double ux = 0.0, vx = 0.0, uy = 0.0, vy = 0.0;
+    if (n > 1) {
+        if (i == 0) {
+            ux = ddiv(dsub(full(j, i + 1, 0), full(j, i, 0)), hx);
+            vx = ddiv(dsub(full(j, i + 1, 1), full(j, i, 1)), hx);
+        } else if (i == n - 1) {
+            ux = ddiv(dsub(full(j, i, 0), full(j, i - 1, 0)), hx);
+            vx = ddiv(dsub(full(j, i, 1), full(j, i - 1, 1)), hx);
+        } else {
+            ux = ddiv(dsub(full(j, i + 1, 0), full(j, i - 1, 0)), dmul(2.0, hx));
+            vx = ddiv(dsub(full(j, i + 1, 1), full(j, i - 1, 1)), dmul(2.0, hx));
+        }
+    }
+    if (m > 1) {
+        if (j == 0) {
+            uy = ddiv(dsub(full(j + 1, i, 0), full(j, i, 0)), hy);
+            vy = ddiv(dsub(full(j + 1, i, 1), full(j, i, 1)), hy);
+        } else if (j == m - 1) {
+            uy = ddiv(dsub(full(j, i, 0), full(j - 1, i, 0)), hy);
+            vy = ddiv(dsub(full(j, i, 1), full(j - 1, i, 1)), hy);
+        } else {
+            uy = ddiv(dsub(full(j + 1, i, 0), full(j - 1, i, 0)), dmul(2.0, hy));
+            vy = ddiv(dsub(full(j + 1, i, 1), full(j - 1, i, 1)), dmul(2.0, hy));
+        }
+    }
+    double tmp = dadd(dadd(dadd(dmul(ux, ux), dmul(uy, uy)), dmul(vx, vx)), dmul(vy, vy));
+    if (tmp < 0.0) tmp = 0.0;
+    psi_g[f * mn + o] = dmul(a_s, pow(dadd(tmp, 0.00001), dsub(a_s, 1.0)));
+}
+
+// Iterations [t0, t1) of the lexicographic SOR as one wavefront (pixel (r, c)
+// of iteration t at step r + c + 2 (t - t0)) with the weights of the last tick
+// and the smoothness weights 0.5 (psi_s[c] + psi_s[n]) alpha / h^2.
+__global__ void kx_sor_range(const double* __restrict__ J, const double* __restrict__ u,
+                             const double* __restrict__ v, long long uv_fs, double* du_g, double* dv_g,
+                             const double* __restrict__ wp_g, const double* __restrict__ psi_g,
+                             double* __restrict__ snap, int K, int h, int w, double alpha_x, double alpha_y, double hx,
+                             double hy, int t0, int t1, double omega)
+{
+    const int f = blockIdx.x;
+    const int n = w + 2, m = h + 2;
+    const long long mn = (long long)m * n;
+    const double* Jf = J + (long long)f * 6 * K * mn;
+    const double* uf = u + f * uv_fs;
+    const double* vf = v + f * uv_fs;
+    double* du = du_g + (long long)f * mn;
+    double* dv = dv_g + (long long)f * mn;
+    const double* wp = wp_g + (long long)f * K * mn;
+    const double* ps = psi_g + (long long)f * mn;
+    double* sn = snap + (long long)f * 2 * mn;
+    const long long qs = (long long)K * mn;
+    const double ax = ddiv(alpha_x, dmul(hx, hx));
+    const double ay = ddiv(alpha_y, dmul(hy, hy));
+    const double one_m_omega = dsub(1.0, omega);
+    const int nit = t1 - t0;
+    const int nsteps = (h - 1) + (w - 1) + 2 * (nit - 1) + 1;
+    for (int s = 0; s < nsteps; ++s) {
+        for (int r = threadIdx.x; r < h; r += blockDim.x) {
+            for (int tl = 0; tl < nit; ++tl) {
+                const int c = s - r - 2 * tl;
+                if (c < 0) break;
+                if (c >= w) continue;
+                const long long o = (long long)(r + 1) * n + (c + 1);
+                const double duc = du[o], dvc = dv[o];
+                if (tl == nit - 1) {
+                    sn[o] = duc;
+                    sn[mn + o] = dvc;
+                }
+                const double duL = c > 0 ? du[o - 1] : duc, dvL = c > 0 ? dv[o - 1] : dvc;
+                const double duR = c < w - 1 ? du[o + 1] : duc, dvR = c < w - 1 ? dv[o + 1] : dvc;
+                const double duD = r < h - 1 ? du[o + n] : duc, dvD = r < h - 1 ? dv[o + n] : dvc;
+                const double duU = r > 0 ? du[o - n] : duc, dvU = r > 0 ? dv[o - n] : dvc;
+                const double uc = uf[o], vc = vf[o], pc = ps[o];
+                double num_u = 0.0, num_v = 0.0, den_u = 0.0, den_v = 0.0, t;
+                // left, right, down, up (core/level_solver.py:272-307)
+                t = dmul(dmul(0.5, dadd(pc, ps[o - 1])), ax);
+                num_u = dadd(num_u, dmul(t, dsub(dadd(uf[o - 1], duL), uc)));
+                num_v = dadd(num_v, dmul(t, dsub(dadd(vf[o - 1], dvL), vc)));
+                den_u = dadd(den_u, t);
+                den_v = dadd(den_v, t);
+                t = dmul(dmul(0.5, dadd(pc, ps[o + 1])), ax);
+                num_u = dadd(num_u, dmul(t, dsub(dadd(uf[o + 1], duR), uc)));
+                num_v = dadd(num_v, dmul(t, dsub(dadd(vf[o + 1], dvR), vc)));
+                den_u = dadd(den_u, t);
+                den_v = dadd(den_v, t);
+                t = dmul(dmul(0.5, dadd(pc, ps[o + n])), ay);
+                num_u = dadd(num_u, dmul(t, dsub(dadd(uf[o + n], duD), uc)));
+                num_v = dadd(num_v, dmul(t, dsub(dadd(vf[o + n], dvD), vc)));
+                den_u = dadd(den_u, t);
+                den_v = dadd(den_v, t);
+                t = dmul(dmul(0.5, dadd(pc, ps[o - n])), ay);
+                num_u = dadd(num_u, dmul(t, dsub(dadd(uf[o - n], duU), uc)));
+                num_v = dadd(num_v, dmul(t, dsub(dadd(vf[o - n], dvU), vc)));
+                den_u = dadd(den_u, t);
+                den_v = dadd(den_v, t);
+                for (int k = 0; k < K; ++k) {
+                    const long long ok = (long long)k * mn + o;
+                    const double wpk = wp[ok];
+                    num_u = dsub(num_u, dmul(wpk, dadd(Jf[4 * qs + ok], dmul(Jf[3 * qs + ok], dvc))));
+                    den_u = dadd(den_u, dmul(wpk, Jf[ok]));
+                    den_v = dadd(den_v, dmul(wpk, Jf[qs + ok]));
+                }
+                const double du_kp1 = den_u != 0.0 ? ddiv(num_u, den_u) : 0.0;
+                const double dun = dadd(dmul(one_m_omega, duc), dmul(omega, du_kp1));
+                double num_v2 = num_v;
+                for (int k = 0; k < K; ++k) {
+                    const long long ok = (long long)k * mn + o;
+                    num_v2 = dsub(num_v2, dmul(wp[ok], dadd(Jf[5 * qs + ok], dmul(Jf[3 * qs + ok], dun))));
+                }
+                const double dv_kp1 = den_v != 0.0 ? ddiv(num_v2, den_v) : 0.0;
+                const double dvn = dadd(dmul(one_m_omega, dvc), dmul(omega, dv_kp1));
+                du[o] = dun;
+                dv[o] = dvn;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
+                                double* du, double* dv, double* wp, double* psi_s, double* snap, int n_frames, int K,
+                                int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
+                                int update_lag, const double* a_data, double a_smooth, double omega, cudaStream_t st,
+                                long long* launches)
+{
+    XAData ad;
+    for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0;
+    const long long mn = (long long)(h + 2) * (w + 2);
+    cudaError_t e = cudaMemsetAsync(du, 0, sizeof(double) * n_frames * mn, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dv, 0, sizeof(double) * n_frames * mn, st);
+    if (e != cudaSuccess) return e;
+    kx_smooth_init<<<dim3((unsigned)((mn + 255) / 256), (unsigned)n_frames), 256, 0, st>>>(W, wp, psi_s, snap, K, mn);
+    ++*launches;
+    const int threads = h >= 512 ? 512 : ((h + 31) / 32) * 32;
+    int t = 0;
+    while (t < iterations) {
+        if ((t + 1) % update_lag == 0) {
+            kx_smooth_tick<<<dim3((unsigned)((w + 2 + 127) / 128), (unsigned)(h + 2), (unsigned)n_frames), 128, 0, st>>>(
+                J, W, u, v, uv_fs, du, dv, snap, wp, psi_s, K, h, w, hx, hy, ad, a_smooth);
+            ++*launches;
+        }
+        int t1 = t + 1;
+        while (t1 < iterations && (t1 + 1) % update_lag != 0) ++t1;
+        kx_sor_range<<<n_frames, threads, 0, st>>>(J, u, v, uv_fs, du, dv, wp, psi_s, snap, K, h, w, alpha_x, alpha_y,
+                                                   hx, hy, t, t1, omega);
+        ++*launches;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        t = t1;
+    }
+    return cudaSuccess;
+}
+
+__global__ void kx_to_float(const double* __restrict__ src, long long n, float* __restrict__ dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st)
+{
+    kx_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, n, dst);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Median (scipy "mirror", exact selection) and accumulate in float64
 // (core/optical_flow.py:607-611).  du, dv, u, v: padded (m, n) planes; output
 // u + du, v + dv interiors with strides (frame, row, col) in elements.

@@ -112,6 +112,15 @@ cudaError_t launch_x_sor(const double* J, const double* W, const double* u, cons
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
                          double alpha_y, double hx, double hy, int iterations, int update_lag,
                          const double* a_data, double omega, cudaStream_t st);
+// a_smooth != 1: the SOR cut at the psi ticks (ticks recompute W psi and
+// psi_s over the padded grid).  psi_s (T, m*n) and snap (T, 2, m*n) are
+// workspace; *launches is incremented per kernel launched.
+cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
+                                double* du, double* dv, double* wp, double* psi_s, double* snap, int n_frames, int K,
+                                int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
+                                int update_lag, const double* a_data, double a_smooth, double omega, cudaStream_t st,
+                                long long* launches);
+cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st);
 // cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
 // (oh, ow): width pass into tmp, height pass into the strided dst view.
 template <typename T>
