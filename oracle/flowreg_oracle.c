@@ -238,10 +238,98 @@ static void repad_d(double *p, int h, int w)
     }
 }
 
+/* Census tensor (core/optical_flow.py:231-345) with numpy's dtypes: f1 is float64; f2 is
+ * float32 when f2_is_f32, and then the directional difference, the smoothed Heaviside and its
+ * gradient are float32 (Python-float constants cast to float32); the J sums are float64. */
+static int census_tensor(const double *f1, const double *f2, int h, int w, double hy, double hx,
+                         int f2_is_f32, double *J11, double *J22, double *J33, double *J12,
+                         double *J13, double *J23)
+{
+    const double eps = 0.1 / 255.0, eps2 = eps * eps;
+    const int H2 = h + 2, W2 = w + 2;
+    const size_t N = (size_t)H2 * W2;
+    double *f1p = malloc(N * sizeof(double)), *f2p = malloc(N * sizeof(double));
+    double *s1p = malloc(N * sizeof(double)), *s2p = malloc(N * sizeof(double));
+    float *s2pf = malloc(N * sizeof(float));
+    if (!f1p || !f2p || !s1p || !s2p || !s2pf) {
+        free(f1p); free(f2p); free(s1p); free(s2p); free(s2pf);
+        return ORC_ENOMEM;
+    }
+    pad1_d(f1, h, w, f1p);
+    pad1_d(f2, h, w, f2p);
+    memset(J11, 0, N * sizeof(double)); memset(J22, 0, N * sizeof(double));
+    memset(J33, 0, N * sizeof(double)); memset(J12, 0, N * sizeof(double));
+    memset(J13, 0, N * sizeof(double)); memset(J23, 0, N * sizeof(double));
+    const float eps2f = (float)eps2, h2x_f = (float)(2.0 * hx), h2y_f = (float)(2.0 * hy);
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            if (dy == 0 && dx == 0) continue;
+            const double dist = sqrt((hy * dy) * (hy * dy) + (hx * dx) * (hx * dx));
+            const float dist_f = (float)dist;
+            /* core values s(y, x), y < h, x < w, written edge-padded into s1p / s2p */
+            for (int y = 0; y < h; ++y)
+                for (int x = 0; x < w; ++x) {
+                    const size_t c = (size_t)(y + 1) * W2 + (x + 1);
+                    const size_t nb = (size_t)(y + 1 + dy) * W2 + (x + 1 + dx);
+                    const double r1 = (f1p[nb] - f1p[c]) / dist;
+                    const double s1 = 0.5 * (1.0 + r1 / sqrt(r1 * r1 + eps2));
+                    double s2;
+                    if (f2_is_f32) {
+                        const float d = (float)f2p[nb] - (float)f2p[c];
+                        const float r2 = d / dist_f;
+                        const float q = sqrtf(r2 * r2 + eps2f);
+                        s2 = (double)(0.5f * (1.0f + r2 / q));
+                    } else {
+                        const double r2 = (f2p[nb] - f2p[c]) / dist;
+                        s2 = 0.5 * (1.0 + r2 / sqrt(r2 * r2 + eps2));
+                    }
+                    s1p[c] = s1;
+                    s2p[c] = s2;
+                }
+            for (int y = 0; y < H2; ++y)
+                for (int x = 0; x < W2; ++x) {
+                    const size_t o = (size_t)y * W2 + x;
+                    const size_t src = (size_t)clampi(y, 1, h) * W2 + clampi(x, 1, w);
+                    s1p[o] = s1p[src];
+                    s2p[o] = s2p[src];
+                }
+            for (size_t i = 0; i < N; ++i) s2pf[i] = (float)s2p[i];
+            for (int y = 1; y <= h; ++y)
+                for (int x = 1; x <= w; ++x) {
+                    const size_t o = (size_t)y * W2 + x;
+                    const double sx1 = (s1p[o + 1] - s1p[o - 1]) / (2.0 * hx);
+                    const double sy1 = (s1p[o + W2] - s1p[o - W2]) / (2.0 * hy);
+                    double sx2, sy2;
+                    if (f2_is_f32) {
+                        sx2 = (double)((s2pf[o + 1] - s2pf[o - 1]) / h2x_f);
+                        sy2 = (double)((s2pf[o + W2] - s2pf[o - W2]) / h2y_f);
+                    } else {
+                        sx2 = (s2p[o + 1] - s2p[o - 1]) / (2.0 * hx);
+                        sy2 = (s2p[o + W2] - s2p[o - W2]) / (2.0 * hy);
+                    }
+                    const double sx = 0.5 * (sx1 + sx2), sy = 0.5 * (sy1 + sy2);
+                    const double st = s2p[o] - s1p[o];
+                    J11[o] += sx * sx; J22[o] += sy * sy; J33[o] += st * st;
+                    J12[o] += sx * sy; J13[o] += sx * st; J23[o] += sy * st;
+                }
+        }
+    const double scale = 2.0 / 8.0;
+    for (int y = 1; y <= h; ++y)
+        for (int x = 1; x <= w; ++x) {
+            const size_t o = (size_t)y * W2 + x;
+            J11[o] *= scale; J22[o] *= scale; J33[o] *= scale;
+            J12[o] *= scale; J13[o] *= scale; J23[o] *= scale;
+        }
+    free(f1p); free(f2p); free(s1p); free(s2p); free(s2pf);
+    return ORC_OK;
+}
+
 int orc_motion_tensor(const double *f1, const double *f2, int h, int w, double hy, double hx,
                       int f2_is_f32, int gray, double *J11, double *J22, double *J33,
                       double *J12, double *J13, double *J23)
 {
+    if (gray == 2)
+        return census_tensor(f1, f2, h, w, hy, hx, f2_is_f32, J11, J22, J33, J12, J13, J23);
     int H2 = h + 2, W2 = w + 2;
     size_t N = (size_t)H2 * W2;
     double *f1p = malloc(N * sizeof(double));
@@ -531,7 +619,7 @@ typedef struct {
 typedef struct {
     int iterations, update_lag;
     double a_smooth;
-    int gray;                    /* 0: gradient constancy, 1: gray-value constancy */
+    int gray;                    /* 0: gradient constancy, 1: gray-value constancy, 2: census */
     int order;                   /* 0 lexicographic (numba), 1 red-black */
     double omega;
     int acc_f32;                 /* resize accumulator: 0 float64 (numba), 1 float32 (plain Python) */

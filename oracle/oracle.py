@@ -258,8 +258,18 @@ def warp(f2: np.ndarray, u: np.ndarray, v: np.ndarray, f1: np.ndarray, cubic: bo
     return out[:, :, 0] if squeeze and C == 1 else out
 
 
+def _const_mode(const_assumption) -> int:
+    """0 gradient constancy, 1 gray value, 2 census (core/optical_flow.py:466-473)."""
+    key = str(getattr(const_assumption, "value", const_assumption)).strip().lower()
+    modes = {"gc": 0, "gradient": 0, "gray": 1, "brightness": 1, "cs": 2, "census": 2}
+    if key not in modes:
+        raise ValueError(f"oracle: unsupported constancy assumption '{const_assumption}'")
+    return modes[key]
+
+
 def motion_tensor(f1, f2, hy, hx, f2_is_f32=False, gray=False):
-    """get_motion_tensor_gc / _gray (core/optical_flow.py:73-228) on one channel."""
+    """get_motion_tensor_gc / _gray / _cs (core/optical_flow.py:73-345) on one channel;
+    gray: False/0 gradient constancy, True/1 gray value, 2 census."""
     f1 = np.ascontiguousarray(f1, dtype=np.float64)
     f2 = np.ascontiguousarray(f2, dtype=np.float64)
     h, w = f1.shape
@@ -405,14 +415,11 @@ def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, m
     "python" reproduces the reference source run without numba (see
     resize_tables), which is what the committed golden vectors hold.
     """
-    key = str(getattr(const_assumption, "value", const_assumption)).strip().lower()
-    if key not in ("gc", "gradient", "gray", "brightness"):
-        raise ValueError(f"oracle: unsupported constancy assumption '{const_assumption}'")
+    mode = _const_mode(const_assumption)
     fixed, moving, weight, a_data_arr = normalize_inputs(fixed, moving, weight, a_data)
     m, n, K = fixed.shape
     plan = _Plan(m, n, _alpha_pair(alpha), levels, eta, min_level, semantics)
-    prm = _Params(int(iterations), int(update_lag), float(a_smooth),
-                  1 if key in ("gray", "brightness") else 0, int(order), float(omega),
+    prm = _Params(int(iterations), int(update_lag), float(a_smooth), mode, int(order), float(omega),
                   1 if semantics == "python" else 0)
     uvd = None if uv is None else np.ascontiguousarray(np.asarray(uv, dtype=np.float64)[:, :, :2])
     oh, ow = plan.out_hw
@@ -437,10 +444,9 @@ def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), u
     m, n, K = fixed3.shape
     T = moving_frames.shape[0]
     mov = np.ascontiguousarray(moving_frames.astype(np.float64).reshape(T, m, n, K))
-    key = str(getattr(const_assumption, "value", const_assumption)).strip().lower()
     plan = _Plan(m, n, _alpha_pair(alpha), levels, eta, min_level)
-    prm = _Params(int(iterations), int(update_lag), float(a_smooth),
-                  1 if key in ("gray", "brightness") else 0, int(order), float(omega), 0)
+    prm = _Params(int(iterations), int(update_lag), float(a_smooth), _const_mode(const_assumption),
+                  int(order), float(omega), 0)
     uvd = None if uv is None else np.ascontiguousarray(np.asarray(uv, dtype=np.float64)[:, :, :2])
     oh, ow = plan.out_hw
     out = np.empty((T, oh, ow, 2), np.float64)

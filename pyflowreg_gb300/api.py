@@ -59,8 +59,6 @@ def resolve_const_assumption(const_assumption) -> int:
         raise ValueError(
             f"Unknown constancy assumption: '{const_assumption}'. Supported values are: '{supported}'."
         )
-    if _CONST[key] == 2:
-        raise NotImplementedError("the census data term ('cs') is not implemented by the GB300 backend")
     return _CONST[key]
 
 
@@ -373,7 +371,7 @@ def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_l
     m, n = fixed.shape[:2]
     w = normalize_weight(weight, m, n, K)
     params = make_params(alpha, update_lag, iterations, min_level, levels, eta, a_smooth, a_data,
-                         ["gc", "gray"][const], K, precision=precision)
+                         ["gc", "gray", "cs"][const], K, precision=precision)
     return fixed, moving, w, params, m, n, K
 
 

@@ -350,8 +350,8 @@ struct frg_plan {
     int32_t* up_sy = nullptr;
     float* up_wy = nullptr;
     double* xtmp = nullptr;   // fp64 width-pass buffer (T, 2, h_min, W)
-    // a_smooth != 1 runs on the reference-order kernels in both precisions
-    bool xpath = false;       // precision == FRG_FP64_REFERENCE or a_smooth != 1
+    // a_smooth != 1 and the census data term run on the reference-order kernels in both precisions
+    bool xpath = false;       // precision == FRG_FP64_REFERENCE, a_smooth != 1 or census
     double* xpsis = nullptr;  // (T, m*n) smoothness weights
     double* xsnap = nullptr;  // (T, 2, m*n) state snapshot for the psi_s border
     double* xflow = nullptr;  // (T, H, W, 2) fp64 flow of an fp32 plan on this path
@@ -493,8 +493,8 @@ int check_params(const frg_params* p, int K)
     if (p->update_lag < 1) return fail(FRG_EINVAL, "update_lag must be >= 1");
     if (p->min_level < 0) return fail(FRG_EINVAL, "min_level must be >= 0");
     if (!(p->a_smooth > 0.0)) return fail(FRG_EINVAL, "a_smooth must be > 0");
-    if (p->const_assumption != 0 && p->const_assumption != 1)
-        return fail(FRG_EUNSUPPORTED, "only the 'gc' and 'gray' constancy assumptions are supported");
+    if (p->const_assumption < 0 || p->const_assumption > 2)
+        return fail(FRG_EINVAL, "const_assumption must be 0 (gc), 1 (gray) or 2 (census)");
     for (int k = 0; k < K; ++k)
         if (!(p->a_data[k] > 0.0)) return fail(FRG_EINVAL, "a_data must be > 0");
     if (p->precision != FRG_FP32 && p->precision != FRG_FP64_REFERENCE)
@@ -568,7 +568,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     pl->K = channels;
     pl->max_T = max_frames;
     for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
-    pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0;
+    pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0 || params->const_assumption == 2;
 
     // schedule: core/optical_flow.py:494-518
     const int m = height, n = width;
@@ -864,7 +864,7 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
     cudaStream_t st = (cudaStream_t)stream;
     const int H = pl->H, W = pl->W, K = pl->K;
     if (pl->xpath) {
-        // a_smooth != 1: the reference-order kernels, rounded to float32 at the end
+        // a_smooth != 1 or census: the reference-order kernels, rounded to float32 at the end
         int rc = run_xpath(pl, T, moving, uv_init, pl->xflow, st);
         if (rc) return rc;
         FRG_LAUNCH(launch_x_to_float(pl->xflow, (long long)T * H * W * 2, flow_out, st));
@@ -1266,6 +1266,8 @@ int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy,
 {
     if (!f1 || !f2 || !out || h < 1 || w < 1) return fail(FRG_EINVAL, "bad argument");
     if (h > 4096 || w > 4096) return fail(FRG_EINVAL, "plane too large");
+    if (gray != 0 && gray != 1)
+        return fail(FRG_EUNSUPPORTED, "frg_motion_tensor computes gc or gray; census runs inside a plan");
     cudaStream_t st = (cudaStream_t)stream;
     DiagGeom g = make_geom(h, w);
     const long long dp = (long long)g.D * g.P;

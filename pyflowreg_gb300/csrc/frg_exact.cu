@@ -226,7 +226,60 @@ __global__ void kx_tensor(const float* __restrict__ f1, const float* __restrict_
             return dsub((double)Bf(yy, xx), A(yy, xx));
         };
         double j11, j22, j33, j12, j13, j23;
-        if (gray) {
+        if (gray == 2) {
+            // census (core/optical_flow.py:231-345): per neighbour offset the smoothed
+            // Heaviside of the directional difference, s = 0.5 (1 + r / sqrt(r^2 + eps^2)),
+            // edge-padded, differentiated centrally; float32 arithmetic on f2 when
+            // f2_f32 (Python-float constants cast to float32), float64 otherwise
+            const double eps = 0.1 / 255.0, eps2 = dmul(eps, eps);
+            const float eps2f = (float)eps2;
+            j11 = j22 = j33 = j12 = j13 = j23 = 0.0;
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    if (dy == 0 && dx == 0) continue;
+                    const double ty = dmul(hy, (double)dy), tx = dmul(hx, (double)dx);
+                    const double dist = __dsqrt_rn(dadd(dmul(ty, ty), dmul(tx, tx)));
+                    const float dist_f = (float)dist;
+                    // s at padded (yy, xx), the edge pad of the core (clamped into [1, h] x [1, w])
+                    auto s1 = [&](int yy, int xx) {
+                        yy = xclamp(yy, 1, h);
+                        xx = xclamp(xx, 1, w);
+                        const double r = ddiv(dsub(A(yy + dy, xx + dx), A(yy, xx)), dist);
+                        return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
+                    };
+                    auto s2 = [&](int yy, int xx) {
+                        yy = xclamp(yy, 1, h);
+                        xx = xclamp(xx, 1, w);
+                        if (f2_f32) {
+                            const float r = __fdiv_rn(__fsub_rn(Bf(yy + dy, xx + dx), Bf(yy, xx)), dist_f);
+                            const float q = __fsqrt_rn(__fadd_rn(__fmul_rn(r, r), eps2f));
+                            return (double)__fmul_rn(0.5f, __fadd_rn(1.0f, __fdiv_rn(r, q)));
+                        }
+                        const double r = ddiv(dsub((double)Bf(yy + dy, xx + dx), (double)Bf(yy, xx)), dist);
+                        return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
+                    };
+                    const double sx1 = ddiv(dsub(s1(yo, xo + 1), s1(yo, xo - 1)), h2x);
+                    const double sy1 = ddiv(dsub(s1(yo + 1, xo), s1(yo - 1, xo)), h2y);
+                    double sx2, sy2;
+                    if (f2_f32) {
+                        sx2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo, xo + 1), (float)s2(yo, xo - 1)), h2x_f);
+                        sy2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo + 1, xo), (float)s2(yo - 1, xo)), h2y_f);
+                    } else {
+                        sx2 = ddiv(dsub(s2(yo, xo + 1), s2(yo, xo - 1)), h2x);
+                        sy2 = ddiv(dsub(s2(yo + 1, xo), s2(yo - 1, xo)), h2y);
+                    }
+                    const double sx = dmul(0.5, dadd(sx1, sx2)), sy = dmul(0.5, dadd(sy1, sy2));
+                    const double st = dsub(s2(yo, xo), s1(yo, xo));
+                    j11 = dadd(j11, dmul(sx, sx));
+                    j22 = dadd(j22, dmul(sy, sy));
+                    j33 = dadd(j33, dmul(st, st));
+                    j12 = dadd(j12, dmul(sx, sy));
+                    j13 = dadd(j13, dmul(sx, st));
+                    j23 = dadd(j23, dmul(sy, st));
+                }
+            j11 = dmul(j11, 0.25); j22 = dmul(j22, 0.25); j33 = dmul(j33, 0.25);
+            j12 = dmul(j12, 0.25); j13 = dmul(j13, 0.25); j23 = dmul(j23, 0.25);
+        } else if (gray) {
             const double fxv = FX(yo, xo);
             const double fyv = dmul(0.5, dadd(gy1(yo, xo), gy2(yo, xo)));
             const double ftv = FT(yo, xo);

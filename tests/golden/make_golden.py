@@ -124,6 +124,9 @@ def main():
     mt["gc_f32"] = np.stack(of.get_motion_tensor_gc(f1, f2.astype(np.float32), 1.3, 1.7))
     mt["gray"] = np.stack(of.get_motion_tensor_gray(f1, f2, 1.3, 1.7))
     mt["gray_f32"] = np.stack(of.get_motion_tensor_gray(f1, f2.astype(np.float32), 1.3, 1.7))
+    # census (core/optical_flow.py:231-345)
+    mt["cs"] = np.stack(of.get_motion_tensor_cs(f1, f2, 1.3, 1.7))
+    mt["cs_f32"] = np.stack(of.get_motion_tensor_cs(f1, f2.astype(np.float32), 1.3, 1.7))
     out["tensor"] = mt
 
     # 4) level solver (core/level_solver.py:158-369)
@@ -166,6 +169,10 @@ def main():
     full["d_flow"] = of.get_displacement(fx, mv, const_assumption="gray", iterations=12, eta=0.7)
     # min_level > 0: the finest levels are skipped and the flow is upsampled by cv2.resize (cubic)
     full["e_flow"] = of.get_displacement(fx, mv, alpha=(1.5, 1.5), min_level=2, iterations=10)
+    # census data term and a graduated non-convexity schedule (core/optical_flow.py:620-770, 887-929)
+    full["f_flow"] = of.get_displacement(fx, mv, const_assumption="cs", iterations=12)
+    full["g_flow"] = of.get_displacement(fx, mv, alpha=(1.5, 1.5), gnc_schedule=(0.0, 0.5, 1.0), warping_steps=2,
+                                         iterations=6, a_smooth=0.7)
     out["full"] = full
 
     for name, d in out.items():

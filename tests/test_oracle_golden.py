@@ -36,7 +36,8 @@ def test_warp(oracle, golden_dir):
     np.testing.assert_array_equal(oracle.warp(g["f2_3c"], g["u"], g["v"], g["f1_3c"], True), g["cubic_2c"])
 
 
-@pytest.mark.parametrize("name,f32,gray", [("gc", 0, 0), ("gc_f32", 1, 0), ("gray", 0, 1), ("gray_f32", 1, 1)])
+@pytest.mark.parametrize("name,f32,gray", [("gc", 0, 0), ("gc_f32", 1, 0), ("gray", 0, 1), ("gray_f32", 1, 1),
+                                           ("cs", 0, 2), ("cs_f32", 1, 2)])
 def test_motion_tensor(oracle, golden_dir, name, f32, gray):
     g = load(golden_dir, "tensor")
     f2 = g["f2"].astype(np.float32).astype(np.float64) if f32 else g["f2"]
@@ -68,6 +69,8 @@ def test_full_displacement(oracle, golden_dir):
     e = oracle.get_displacement(f["b_fixed"], f["b_moving"], alpha=(1.5, 1.5), min_level=2, iterations=10,
                                 semantics="python")
     np.testing.assert_array_equal(e, f["e_flow"])
+    cs = oracle.get_displacement(f["b_fixed"], f["b_moving"], const_assumption="cs", iterations=12, semantics="python")
+    np.testing.assert_array_equal(cs, f["f_flow"])
     an = oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
     assert np.abs(an - f["a_flow"]).max() < 1e-4
 
