@@ -38,7 +38,8 @@ extern "C" {
 #define FRG_EUNSUPPORTED 4    /* option not implemented by this backend */
 
 #define FRG_MAX_CHANNELS 8
-#define FRG_ABI_VERSION 1
+#define FRG_MAX_GNC_STAGES 16
+#define FRG_ABI_VERSION 2
 
 /* Optical-flow options, the subset of OFOptions.to_dict()
  * (motion_correction/OF_options.py:1084-1101) that get_displacement uses. */
@@ -51,9 +52,17 @@ typedef struct frg_params {
     int update_lag;                       /* iterations between nonlinearity updates */
     double a_smooth;                      /* smoothness Charbonnier exponent (1.0 only) */
     double a_data[FRG_MAX_CHANNELS];      /* data-term exponent per channel */
-    int const_assumption;                 /* 0: gradient constancy "gc", 1: gray value "gray" */
+    int const_assumption;                 /* 0: gradient constancy "gc", 1: gray value "gray", 2: census "cs" */
     double omega;                         /* SOR relaxation factor (reference: 1.95) */
     int precision;                        /* FRG_FP32 (default) or FRG_FP64_REFERENCE */
+    /* Graduated non-convexity (get_displacement's gnc_schedule / warping_steps,
+     * core/optical_flow.py:620-770, 887-929): gnc_stages = 0 runs the plain
+     * pyramid; otherwise gnc_stages (2..FRG_MAX_GNC_STAGES) betas, nondecreasing
+     * from 0 to 1, each stage re-running the pyramid from the previous stage's
+     * flow with warping_steps warp / relinearise rounds per level. */
+    int gnc_stages;
+    double gnc_schedule[FRG_MAX_GNC_STAGES];
+    int warping_steps;
 } frg_params;
 
 /* precision: FRG_FP32 is the fast path (float32 arithmetic, folded SOR

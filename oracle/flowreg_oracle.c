@@ -513,12 +513,17 @@ static inline void relax_pixel(int j, int i, int m, int n, int K, const double *
     dv[c] = (1.0 - omega) * dv[c] + omega * dv_kp1;
 }
 
+/* gnc_beta < 0: compute_flow (core/level_solver.py:158-369); gnc_beta in [0, 1]:
+ * compute_flow_gnc (core/level_solver.py:372-555), which mixes psi and psi_s with the
+ * quadratic penalty, (1 - beta) + beta * robust, where the exponent lies in (0, 1). */
 int orc_compute_flow(const double *J11, const double *J22, const double *J33, const double *J12,
                      const double *J13, const double *J23, const double *wgt, const double *u,
                      const double *v, int m, int n, int K, double alpha_x, double alpha_y,
                      int iterations, int update_lag, const double *a_data, double a_smooth,
-                     double hx, double hy, int order, double omega, double *du, double *dv)
+                     double hx, double hy, int order, double omega, double gnc_beta, double *du, double *dv)
 {
+    const int gnc = gnc_beta >= 0.0;
+    const double mix_quadratic = 1.0 - gnc_beta;
     size_t N = (size_t)m * n;
     double *psi = malloc(N * K * sizeof(double));
     double *psi_s = malloc(N * sizeof(double));
@@ -539,11 +544,15 @@ int orc_compute_flow(const double *J11, const double *J22, const double *J33, co
                     double val = J11[ck] * a * a + J22[ck] * b * b + J23[ck] * b
                                + 2.0 * J12[ck] * a * b + 2.0 * J13[ck] * a + J23[ck] * b + J33[ck];
                     if (val < 0.0) val = 0.0;
-                    psi[ck] = a_data[k] * pow(val + 0.00001, a_data[k] - 1.0);
+                    const double robust = a_data[k] * pow(val + 0.00001, a_data[k] - 1.0);
+                    const int mix = gnc && 0.0 < a_data[k] && a_data[k] < 1.0 && gnc_beta < 1.0;
+                    psi[ck] = mix ? mix_quadratic + gnc_beta * robust : robust;
                 }
-            if (smooth_nl)
+            if (smooth_nl) {
                 nonlinearity_smoothness_2d(psi_s, u, du, v, dv, m, n, a_smooth, hx, hy, scratch);
-            else
+                if (gnc && 0.0 < a_smooth && a_smooth < 1.0 && gnc_beta < 1.0)
+                    for (size_t c = 0; c < N; ++c) psi_s[c] = mix_quadratic + gnc_beta * psi_s[c];
+            } else
                 for (size_t c = 0; c < N; ++c) psi_s[c] = 1.0;
         }
         set_boundary_2d(du, m, n);
@@ -623,6 +632,8 @@ typedef struct {
     int order;                   /* 0 lexicographic (numba), 1 red-black */
     double omega;
     int acc_f32;                 /* resize accumulator: 0 float64 (numba), 1 float32 (plain Python) */
+    double gnc_beta;             /* < 0: plain stage; else one GNC stage with this beta */
+    int warping_steps;           /* warp / relinearise steps per level of a GNC stage */
 } orc_params;
 
 /* resize an (H, W, K) double array, channel by channel, to (h, w, K) */
@@ -753,7 +764,7 @@ int orc_displacement(int H, int W, int K, const double *fixed, const double *mov
             rc = orc_compute_flow(J, J + mn * K, J + 2 * mn * K, J + 3 * mn * K, J + 4 * mn * K,
                                   J + 5 * mn * K, wpad, un, vn, m, n, K, L->alpha_x, L->alpha_y,
                                   prm->iterations, prm->update_lag, a_data, prm->a_smooth,
-                                  h_col, h_row, prm->order, prm->omega, du, dv);
+                                  h_col, h_row, prm->order, prm->omega, -1.0, du, dv);
         }
         if (rc == ORC_OK) {
             /* median on the interiors (lines 607-609), then accumulate (610-611) */
@@ -768,6 +779,135 @@ int orc_displacement(int H, int W, int K, const double *fixed, const double *mov
                 }
             }
             for (size_t i = 0; i < mn; ++i) { un[i] += du[i]; vn[i] += dv[i]; }
+            free(u); free(v);
+            u = un; v = vn; un = NULL; vn = NULL;
+            ph = h; pw = w;
+        }
+        free(f1); free(f2); free(wl); free(ur); free(vr); free(un); free(vn); free(tmp); free(J);
+        free(Jc); free(wpad); free(du); free(dv); free(plane1); free(plane2); free(uw); free(vw);
+        free(wf); free(med); free(medo);
+    }
+    if (rc == ORC_OK) {
+        for (int y = 0; y < ph; ++y)
+            for (int x = 0; x < pw; ++x) {
+                w_out[((size_t)y * pw + x) * 2 + 0] = u[(size_t)(y + 1) * (pw + 2) + x + 1];
+                w_out[((size_t)y * pw + x) * 2 + 1] = v[(size_t)(y + 1) * (pw + 2) + x + 1];
+            }
+    }
+    free(u); free(v); free(u_init); free(v_init);
+    return rc;
+}
+
+/* One GNC stage (core/optical_flow.py:620-770): per level, warping_steps rounds of
+ * warp (every level, the top one included, so the warped frame is always float32),
+ * tensor, compute_flow_gnc from du = dv = 0, u += du, and a 5x5 median of u itself. */
+int orc_displacement_gnc(int H, int W, int K, const double *fixed, const double *moving,
+                         const double *weight, const double *uv, int n_levels,
+                         const orc_level *levels, const double *a_data, const orc_params *prm,
+                         double *w_out)
+{
+    int rc = ORC_OK;
+    double *u = NULL, *v = NULL;
+    int ph = 0, pw = 0;
+    size_t full = (size_t)H * W;
+    double *u_init = malloc(full * sizeof(double)), *v_init = malloc(full * sizeof(double));
+    if (!u_init || !v_init) { free(u_init); free(v_init); return ORC_ENOMEM; }
+    for (size_t i = 0; i < full; ++i) {
+        u_init[i] = uv ? uv[i * 2 + 0] : 0.0;
+        v_init[i] = uv ? uv[i * 2 + 1] : 0.0;
+    }
+    for (int li = 0; li < n_levels && rc == ORC_OK; ++li) {
+        const orc_level *L = &levels[li];
+        int h = L->h, w = L->w, m = h + 2, n = w + 2;
+        size_t hw = (size_t)h * w, mn = (size_t)m * n;
+        double *f1 = malloc(hw * K * sizeof(double)), *f2 = malloc(hw * K * sizeof(double));
+        double *wl = malloc(hw * K * sizeof(double));
+        double *ur = malloc(hw * sizeof(double)), *vr = malloc(hw * sizeof(double));
+        double *un = malloc(mn * sizeof(double)), *vn = malloc(mn * sizeof(double));
+        double *tmp = malloc(hw * K * sizeof(double));
+        double *J = malloc(6 * mn * K * sizeof(double));
+        double *Jc = malloc(6 * mn * sizeof(double));
+        double *wpad = malloc(mn * K * sizeof(double));
+        double *du = malloc(mn * sizeof(double)), *dv = malloc(mn * sizeof(double));
+        double *plane1 = malloc(hw * sizeof(double)), *plane2 = malloc(hw * sizeof(double));
+        double *uw = malloc(hw * sizeof(double)), *vw = malloc(hw * sizeof(double));
+        float *wf = malloc(hw * sizeof(float));
+        double *med = malloc(hw * sizeof(double)), *medo = malloc(hw * sizeof(double));
+        if (!f1 || !f2 || !wl || !ur || !vr || !un || !vn || !tmp || !J || !Jc || !wpad || !du ||
+            !dv || !plane1 || !plane2 || !uw || !vw || !wf || !med || !medo)
+            rc = ORC_ENOMEM;
+        if (rc == ORC_OK)
+            rc = resize_hwk(fixed, H, W, K, f1, h, w, L->ix_img, L->wx_img, L->iy_img, L->wy_img, L->p_img, prm->acc_f32);
+        if (rc == ORC_OK)
+            rc = resize_hwk(moving, H, W, K, f2, h, w, L->ix_img, L->wx_img, L->iy_img, L->wy_img, L->p_img, prm->acc_f32);
+        double h_row = (double)H / h, h_col = (double)W / w;
+        if (rc == ORC_OK) {
+            const double *su = L->top ? u_init : NULL, *sv = L->top ? v_init : NULL;
+            double *iu = NULL, *iv = NULL;
+            if (!L->top) {
+                iu = malloc((size_t)ph * pw * sizeof(double));
+                iv = malloc((size_t)ph * pw * sizeof(double));
+                if (!iu || !iv) rc = ORC_ENOMEM;
+                else {
+                    for (int y = 0; y < ph; ++y)
+                        for (int x = 0; x < pw; ++x) {
+                            iu[(size_t)y * pw + x] = u[(size_t)(y + 1) * (pw + 2) + x + 1];
+                            iv[(size_t)y * pw + x] = v[(size_t)(y + 1) * (pw + 2) + x + 1];
+                        }
+                    su = iu; sv = iv;
+                }
+            }
+            if (rc == ORC_OK) rc = resize_hwk(su, L->fh, L->fw, 1, ur, h, w, L->ix_flow, L->wx_flow, L->iy_flow, L->wy_flow, L->p_flow, prm->acc_f32);
+            if (rc == ORC_OK) rc = resize_hwk(sv, L->fh, L->fw, 1, vr, h, w, L->ix_flow, L->wx_flow, L->iy_flow, L->wy_flow, L->p_flow, prm->acc_f32);
+            free(iu); free(iv);
+        }
+        if (rc == ORC_OK) {
+            add_boundary(ur, h, w, un);
+            add_boundary(vr, h, w, vn);
+            rc = resize_hwk(weight, H, W, K, wl, h, w, L->ix_img, L->wx_img, L->iy_img, L->wy_img, L->p_img, prm->acc_f32);
+            memset(wpad, 0, mn * K * sizeof(double));
+            for (int y = 0; y < h; ++y)
+                for (int x = 0; x < w; ++x)
+                    for (int k = 0; k < K; ++k)
+                        wpad[((size_t)(y + 1) * n + x + 1) * K + k] = wl[((size_t)y * w + x) * K + k];
+        }
+        for (int ws = 0; ws < prm->warping_steps && rc == ORC_OK; ++ws) {
+            for (size_t i = 0; i < hw; ++i) {
+                int y = (int)(i / w), x = (int)(i % w);
+                uw[i] = un[(size_t)(y + 1) * n + x + 1] / h_col;
+                vw[i] = vn[(size_t)(y + 1) * n + x + 1] / h_row;
+            }
+            for (int k = 0; k < K; ++k) {
+                for (size_t i = 0; i < hw; ++i) { plane1[i] = f1[i * K + k]; plane2[i] = f2[i * K + k]; }
+                orc_warp_plane(plane2, plane1, uw, vw, h, w, 1, wf);
+                for (size_t i = 0; i < hw; ++i) tmp[i * K + k] = (double)wf[i];
+            }
+            for (int k = 0; k < K && rc == ORC_OK; ++k) {
+                for (size_t i = 0; i < hw; ++i) { plane1[i] = f1[i * K + k]; plane2[i] = tmp[i * K + k]; }
+                rc = orc_motion_tensor(plane1, plane2, h, w, h_row, h_col, 1, prm->gray,
+                                       Jc, Jc + mn, Jc + 2 * mn, Jc + 3 * mn, Jc + 4 * mn, Jc + 5 * mn);
+                for (int q = 0; q < 6; ++q)
+                    for (size_t i = 0; i < mn; ++i) J[(size_t)q * mn * K + i * K + k] = Jc[(size_t)q * mn + i];
+            }
+            if (rc == ORC_OK)
+                rc = orc_compute_flow(J, J + mn * K, J + 2 * mn * K, J + 3 * mn * K, J + 4 * mn * K,
+                                      J + 5 * mn * K, wpad, un, vn, m, n, K, L->alpha_x, L->alpha_y,
+                                      prm->iterations, prm->update_lag, a_data, prm->a_smooth,
+                                      h_col, h_row, prm->order, prm->omega, prm->gnc_beta, du, dv);
+            if (rc == ORC_OK) {
+                for (size_t i = 0; i < mn; ++i) { un[i] += du[i]; vn[i] += dv[i]; }
+                if ((h < w ? h : w) > 5) {
+                    for (int pass = 0; pass < 2; ++pass) {
+                        double *d = pass == 0 ? un : vn;
+                        for (int y = 0; y < h; ++y)
+                            for (int x = 0; x < w; ++x) med[(size_t)y * w + x] = d[(size_t)(y + 1) * n + x + 1];
+                        orc_median5_plane(med, h, w, medo);
+                        add_boundary(medo, h, w, d);
+                    }
+                }
+            }
+        }
+        if (rc == ORC_OK) {
             free(u); free(v);
             u = un; v = vn; un = NULL; vn = NULL;
             ph = h; pw = w;

@@ -64,7 +64,8 @@ class _Params(ctypes.Structure):
         ("iterations", ctypes.c_int), ("update_lag", ctypes.c_int),
         ("a_smooth", ctypes.c_double), ("gray", ctypes.c_int),
         ("order", ctypes.c_int), ("omega", ctypes.c_double),
-        ("acc_f32", ctypes.c_int),
+        ("acc_f32", ctypes.c_int), ("gnc_beta", ctypes.c_double),
+        ("warping_steps", ctypes.c_int),
     ]
 
 
@@ -76,6 +77,7 @@ def lib():
         P = ctypes.c_void_p
         I, D = ctypes.c_int, ctypes.c_double
         _lib.orc_displacement.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
+        _lib.orc_displacement_gnc.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
         _lib.orc_displacement_batch.argtypes = [I, I, I, I, P, P, P, P, I, P, P, P, I, I, P, I]
         _lib.orc_resize_plane.argtypes = [P, I, I, P, I, I, P, P, I, P, P, I, P, I]
         _lib.orc_resize_plane.restype = None
@@ -83,7 +85,7 @@ def lib():
         _lib.orc_warp_plane.restype = None
         _lib.orc_motion_tensor.argtypes = [P, P, I, I, D, D, I, I, P, P, P, P, P, P]
         _lib.orc_compute_flow.argtypes = [P, P, P, P, P, P, P, P, P, I, I, I, D, D, I, I, P, D,
-                                          D, D, I, D, P, P]
+                                          D, D, I, D, D, P, P]
         _lib.orc_median5_plane.argtypes = [P, I, I, P]
         _lib.orc_median5_plane.restype = None
         _lib.orc_cubic_table.argtypes = [P]
@@ -282,8 +284,10 @@ def motion_tensor(f1, f2, hy, hx, f2_is_f32=False, gray=False):
 
 
 def compute_flow(J11, J22, J33, J12, J13, J23, weight, u, v, alpha_x, alpha_y, iterations,
-                 update_lag, a_data, a_smooth, hx, hy, order=ORDER_LEXICOGRAPHIC, omega=1.95):
-    """compute_flow (core/level_solver.py:158-369); returns (m, n, 2)."""
+                 update_lag, a_data, a_smooth, hx, hy, order=ORDER_LEXICOGRAPHIC, omega=1.95,
+                 gnc_beta=None):
+    """compute_flow (core/level_solver.py:158-369), or compute_flow_gnc
+    (core/level_solver.py:372-555) when gnc_beta is given; returns (m, n, 2)."""
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (J11, J22, J33, J12, J13, J23, weight)]
     if arrs[0].ndim == 2:
         arrs = [a[:, :, None] for a in arrs]
@@ -296,7 +300,7 @@ def compute_flow(J11, J22, J33, J12, J13, J23, weight, u, v, alpha_x, alpha_y, i
     rc = lib().orc_compute_flow(*[_p(a) for a in arrs], _p(u), _p(v), m, n, K, float(alpha_x),
                                 float(alpha_y), int(iterations), int(update_lag), _p(ad),
                                 float(a_smooth), float(hx), float(hy), int(order), float(omega),
-                                _p(du), _p(dv))
+                                -1.0 if gnc_beta is None else float(gnc_beta), _p(du), _p(dv))
     if rc:
         raise MemoryError("oracle level solver")
     return np.stack([du, dv], axis=2)
@@ -405,33 +409,62 @@ def _upsample_final(w, m, n):
     return mod.resize(w, (n, m), interpolation=mod.INTER_CUBIC)
 
 
+def gnc_stages(gnc_schedule, warping_steps):
+    """normalize_gnc_schedule / normalize_warping_steps (core/optical_flow.py:414-443)
+    and the default of 10 steps (core/optical_flow.py:911): (betas or None, steps)."""
+    if gnc_schedule is None:
+        return None, None
+    sched = np.asarray(gnc_schedule, dtype=np.float64)
+    if sched.ndim != 1:
+        raise ValueError("gnc_schedule must be a 1D sequence of stage weights")
+    if sched.size < 2:
+        raise ValueError("gnc_schedule must contain at least two stages")
+    if np.any(sched < 0.0) or np.any(sched > 1.0):
+        raise ValueError("gnc_schedule entries must lie in [0, 1]")
+    if not np.all(np.diff(sched) >= 0.0):
+        raise ValueError("gnc_schedule must be monotone nondecreasing")
+    if not np.isclose(sched[0], 0.0) or not np.isclose(sched[-1], 1.0):
+        raise ValueError("gnc_schedule must start at 0.0 and end at 1.0")
+    steps = 10 if warping_steps is None else int(warping_steps)
+    if steps < 1:
+        raise ValueError("warping_steps must be a positive integer")
+    return [float(b) for b in sched], steps
+
+
 def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, min_level=0,
                      levels=50, eta=0.8, a_smooth=1.0, a_data=0.45, const_assumption="gc",
                      uv=None, weight=None, order=ORDER_LEXICOGRAPHIC, omega=1.95,
-                     semantics="numba"):
-    """Oracle of pyflowreg.core.optical_flow.get_displacement (no GNC).
+                     semantics="numba", gnc_schedule=None, warping_steps=None):
+    """Oracle of pyflowreg.core.optical_flow.get_displacement
+    (core/optical_flow.py:773-929), GNC stages included (620-770).
 
     semantics="numba" follows the deployed (numba-compiled) reference;
     "python" reproduces the reference source run without numba (see
     resize_tables), which is what the committed golden vectors hold.
     """
     mode = _const_mode(const_assumption)
+    betas, steps = gnc_stages(gnc_schedule, warping_steps)
     fixed, moving, weight, a_data_arr = normalize_inputs(fixed, moving, weight, a_data)
     m, n, K = fixed.shape
     plan = _Plan(m, n, _alpha_pair(alpha), levels, eta, min_level, semantics)
-    prm = _Params(int(iterations), int(update_lag), float(a_smooth), mode, int(order), float(omega),
-                  1 if semantics == "python" else 0)
-    uvd = None if uv is None else np.ascontiguousarray(np.asarray(uv, dtype=np.float64)[:, :, :2])
     oh, ow = plan.out_hw
-    out = np.empty((oh, ow, 2), np.float64)
-    rc = lib().orc_displacement(m, n, K, _p(np.ascontiguousarray(fixed)), _p(np.ascontiguousarray(moving)),
-                                _p(weight), None if uvd is None else _p(uvd), len(plan.sched),
-                                ctypes.byref(plan.levels), _p(a_data_arr), ctypes.byref(prm), _p(out))
-    if rc:
-        raise RuntimeError(f"oracle failed with status {rc}")
-    if plan.min_level > 0:
-        out = _upsample_final(out, m, n)
-    return out
+    flow = uv
+    for beta in (betas if betas is not None else [None]):
+        prm = _Params(int(iterations), int(update_lag), float(a_smooth), mode, int(order), float(omega),
+                      1 if semantics == "python" else 0, -1.0 if beta is None else beta,
+                      0 if steps is None else steps)
+        uvd = None if flow is None else np.ascontiguousarray(np.asarray(flow, dtype=np.float64)[:, :, :2])
+        out = np.empty((oh, ow, 2), np.float64)
+        fn = lib().orc_displacement if beta is None else lib().orc_displacement_gnc
+        rc = fn(m, n, K, _p(np.ascontiguousarray(fixed)), _p(np.ascontiguousarray(moving)),
+                _p(weight), None if uvd is None else _p(uvd), len(plan.sched),
+                ctypes.byref(plan.levels), _p(a_data_arr), ctypes.byref(prm), _p(out))
+        if rc:
+            raise RuntimeError(f"oracle failed with status {rc}")
+        if plan.min_level > 0:
+            out = _upsample_final(out, m, n)
+        flow = out
+    return flow
 
 
 def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), update_lag=5,

@@ -19,6 +19,7 @@ FRG_ENOMEM = 2
 FRG_ECUDA = 3
 FRG_EUNSUPPORTED = 4
 FRG_MAX_CHANNELS = 8
+FRG_MAX_GNC_STAGES = 16
 
 _lock = threading.Lock()
 _lib = None
@@ -38,6 +39,9 @@ class FrgParams(ctypes.Structure):
         ("const_assumption", ctypes.c_int),
         ("omega", ctypes.c_double),
         ("precision", ctypes.c_int),
+        ("gnc_stages", ctypes.c_int),
+        ("gnc_schedule", ctypes.c_double * FRG_MAX_GNC_STAGES),
+        ("warping_steps", ctypes.c_int),
     ]
 
 

@@ -63,7 +63,7 @@ def resolve_const_assumption(const_assumption) -> int:
 
 
 def normalize_gnc_schedule(gnc_schedule):
-    """Validation of core/optical_flow.py:414-432 (the backend then rejects GNC)."""
+    """Validation of core/optical_flow.py:414-432."""
     if gnc_schedule is None:
         return None
     schedule = np.asarray(gnc_schedule, dtype=np.float64)
@@ -129,10 +129,12 @@ PRECISIONS = {"fp32": _lib.FRG_FP32, "fp64": _lib.FRG_FP64_REFERENCE}
 
 def make_params(alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
                 a_smooth=1.0, a_data=0.45, const_assumption="gc", K=1, omega=1.95,
-                precision="fp32") -> "_lib.FrgParams":
+                precision="fp32", gnc_schedule=None, warping_steps=None) -> "_lib.FrgParams":
     """Options as a frg_params struct.  precision "fp32" is the fast path;
     "fp64" computes in the reference's precision and operation order (the
-    parity mode)."""
+    parity mode).  gnc_schedule / warping_steps select the graduated
+    non-convexity stages (core/optical_flow.py:887-929; 10 warping steps
+    per level when warping_steps is None)."""
     if K > _lib.FRG_MAX_CHANNELS:
         raise ValueError(f"at most {_lib.FRG_MAX_CHANNELS} channels are supported")
     if precision not in PRECISIONS:
@@ -153,12 +155,22 @@ def make_params(alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=5
         p.a_data[k] = float(ad[k])
     p.const_assumption = resolve_const_assumption(const_assumption)
     p.omega = float(omega)
+    sched = normalize_gnc_schedule(gnc_schedule)
+    steps = normalize_warping_steps(warping_steps)
+    if sched is not None:
+        if sched.size > _lib.FRG_MAX_GNC_STAGES:
+            raise ValueError(f"at most {_lib.FRG_MAX_GNC_STAGES} GNC stages are supported")
+        p.gnc_stages = int(sched.size)
+        for i, b in enumerate(sched):
+            p.gnc_schedule[i] = float(b)
+        p.warping_steps = 10 if steps is None else steps
     return p
 
 
 def _params_key(p) -> tuple:
     return (p.alpha_x, p.alpha_y, p.eta, p.levels, p.min_level, p.iterations, p.update_lag, p.a_smooth,
-            tuple(p.a_data), p.const_assumption, p.omega, p.precision)
+            tuple(p.a_data), p.const_assumption, p.omega, p.precision, p.gnc_stages,
+            tuple(p.gnc_schedule[:p.gnc_stages]), p.warping_steps)
 
 
 # --------------------------------------------------------------------------
@@ -360,9 +372,6 @@ def clear_plans():
 def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_level, levels, eta, a_smooth,
              const_assumption, gnc_schedule, warping_steps, level_solver_backend, precision="fp32"):
     const = resolve_const_assumption(const_assumption)
-    if normalize_gnc_schedule(gnc_schedule) is not None:
-        raise NotImplementedError("graduated non-convexity (gnc_schedule) is not implemented by the GB300 backend")
-    normalize_warping_steps(warping_steps)
     if level_solver_backend is not None:
         raise NotImplementedError("the GB300 backend runs its own level solver; level_solver_backend must be None")
     fixed = np.asarray(fixed)
@@ -371,7 +380,8 @@ def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_l
     m, n = fixed.shape[:2]
     w = normalize_weight(weight, m, n, K)
     params = make_params(alpha, update_lag, iterations, min_level, levels, eta, a_smooth, a_data,
-                         ["gc", "gray", "cs"][const], K, precision=precision)
+                         ["gc", "gray", "cs"][const], K, precision=precision, gnc_schedule=gnc_schedule,
+                         warping_steps=warping_steps)
     return fixed, moving, w, params, m, n, K
 
 

@@ -350,8 +350,8 @@ struct frg_plan {
     int32_t* up_sy = nullptr;
     float* up_wy = nullptr;
     double* xtmp = nullptr;   // fp64 width-pass buffer (T, 2, h_min, W)
-    // a_smooth != 1 and the census data term run on the reference-order kernels in both precisions
-    bool xpath = false;       // precision == FRG_FP64_REFERENCE, a_smooth != 1 or census
+    // a_smooth != 1, the census data term and GNC stages run on the reference-order kernels in both precisions
+    bool xpath = false;       // precision == FRG_FP64_REFERENCE, a_smooth != 1, census or GNC
     double* xpsis = nullptr;  // (T, m*n) smoothness weights
     double* xsnap = nullptr;  // (T, 2, m*n) state snapshot for the psi_s border
     double* xflow = nullptr;  // (T, H, W, 2) fp64 flow of an fp32 plan on this path
@@ -499,6 +499,22 @@ int check_params(const frg_params* p, int K)
         if (!(p->a_data[k] > 0.0)) return fail(FRG_EINVAL, "a_data must be > 0");
     if (p->precision != FRG_FP32 && p->precision != FRG_FP64_REFERENCE)
         return fail(FRG_EINVAL, "precision must be FRG_FP32 or FRG_FP64_REFERENCE");
+    if (p->gnc_stages != 0) {
+        // normalize_gnc_schedule / normalize_warping_steps (core/optical_flow.py:414-443)
+        if (p->gnc_stages < 2 || p->gnc_stages > FRG_MAX_GNC_STAGES)
+            return fail(FRG_EINVAL, "gnc_stages must be 0 or in [2, FRG_MAX_GNC_STAGES]");
+        for (int s = 0; s < p->gnc_stages; ++s) {
+            const double b = p->gnc_schedule[s];
+            if (!(b >= 0.0 && b <= 1.0)) return fail(FRG_EINVAL, "gnc_schedule entries must lie in [0, 1]");
+            if (s > 0 && !(b >= p->gnc_schedule[s - 1]))
+                return fail(FRG_EINVAL, "gnc_schedule must be monotone nondecreasing");
+        }
+        // np.isclose(x, target) with rtol 1e-5, atol 1e-8
+        if (!(std::fabs(p->gnc_schedule[0]) <= 1e-8)) return fail(FRG_EINVAL, "gnc_schedule must start at 0.0");
+        if (!(std::fabs(p->gnc_schedule[p->gnc_stages - 1] - 1.0) <= 1e-8 + 1e-5))
+            return fail(FRG_EINVAL, "gnc_schedule must end at 1.0");
+        if (p->warping_steps < 1) return fail(FRG_EINVAL, "warping_steps must be a positive integer");
+    }
     return FRG_OK;
 }
 
@@ -568,7 +584,8 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     pl->K = channels;
     pl->max_T = max_frames;
     for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
-    pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0 || params->const_assumption == 2;
+    pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0 ||
+                params->const_assumption == 2 || params->gnc_stages != 0;
 
     // schedule: core/optical_flow.py:494-518
     const int m = height, n = width;
@@ -960,10 +977,103 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
 
 namespace {
 
+// GNC stages (core/optical_flow.py:620-770, 909-929) on the reference-order
+// kernels.  Each stage re-runs the pyramid from the previous stage's flow
+// (flow_out, written by the stage before, read by the next stage's top-level
+// resize); each level runs warping_steps rounds of warp (the top level too, so
+// the warped frame is float32 everywhere), tensor, compute_flow_gnc from
+// du = dv = 0, and the state update u = [median5](u + du) with its border
+// rebuilt.  The state is per frame from the start (it changes in place).
+int run_xpath_gnc(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out, cudaStream_t st)
+{
+    const int H = pl->H, W = pl->W, K = pl->K;
+    const long long fsz = (long long)H * W * K;
+    for (int stage = 0; stage < pl->p.gnc_stages; ++stage) {
+        const double beta = pl->p.gnc_schedule[stage];
+        int cur = 0;
+        const LevelPlan* prev = nullptr;
+        for (size_t li = 0; li < pl->levels.size(); ++li) {
+            const LevelPlan& L = pl->levels[li];
+            const int h = L.h, w = L.w;
+            const long long hw = (long long)h * w, mn = (long long)(h + 2) * (w + 2);
+            FRG_LAUNCH(launch_x_resize_h_f(moving, fsz, 1, (long long)W * K, K, T, K, H, pl->tmp, w, L.img.ix,
+                                           L.img.wx, L.img.P, st));
+            FRG_LAUNCH(launch_x_resize_v_f(pl->tmp, T, K, H, w, pl->f2, K * hw, hw, w, h, 0, L.img.iy, L.img.wy,
+                                           L.img.P, st));
+            if (L.top) {
+                if (stage > 0) {
+                    FRG_LAUNCH(launch_x_resize_h_d(flow_out, (long long)H * W * 2, 1, (long long)W * 2, 2, T, 2, H,
+                                                   pl->tmp, w, L.flow.ix, L.flow.wx, L.flow.P, st));
+                } else if (uv_init) {
+                    FRG_LAUNCH(launch_x_resize_h_f(uv_init, 0, 1, (long long)W * 2, 2, T, 2, H, pl->tmp, w, L.flow.ix,
+                                                   L.flow.wx, L.flow.P, st));
+                } else {
+                    FRG_CUDA(cudaMemsetAsync(pl->xuv, 0, sizeof(double) * T * 2 * mn, st));
+                }
+                if (stage > 0 || uv_init)
+                    FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, T, 2, H, w, pl->xuv, 2 * mn, mn, w + 2, h, 1, L.flow.iy,
+                                                   L.flow.wy, L.flow.P, st));
+            } else {
+                const long long phw = (long long)prev->h * prev->w;
+                FRG_LAUNCH(launch_x_resize_h_d(pl->xacc[cur], 2 * phw, phw, prev->w, 1, T, 2, prev->h, pl->tmp, w,
+                                               L.flow.ix, L.flow.wx, L.flow.P, st));
+                FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, T, 2, prev->h, w, pl->xuv, 2 * mn, mn, w + 2, h, 1,
+                                               L.flow.iy, L.flow.wy, L.flow.P, st));
+            }
+            const bool last = (li + 1 == pl->levels.size());
+            const bool direct = last && pl->min_level == 0;  // the finest level writes flow_out itself
+            const int nxt = cur ^ 1;
+            double* ou = direct ? flow_out : pl->xacc[nxt];
+            double* ov = direct ? flow_out + 1 : pl->xacc[nxt] + hw;
+            const long long o_fs = direct ? (long long)H * W * 2 : 2 * hw;
+            const long long o_rs = direct ? (long long)W * 2 : w;
+            const long long o_cs = direct ? 2 : 1;
+            const int do_median = std::min(h, w) > 5 ? 1 : 0;
+            for (int ws = 0; ws < pl->p.warping_steps; ++ws) {
+                FRG_LAUNCH(launch_x_warp(pl->f2, L.ref, pl->xuv, pl->xuv + mn, 2 * mn, T, K, h, w, L.h_col, L.h_row,
+                                         pl->warped, st));
+                FRG_LAUNCH(launch_x_tensor(L.ref, pl->warped, T, K, h, w, L.h_row, L.h_col, 1,
+                                           pl->p.const_assumption, pl->xJ, st));
+                if (pl->p.a_smooth == 1.0) {
+                    FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, 2 * mn, pl->xdu, pl->xdv,
+                                            pl->xwp, T, K, h, w, L.alpha_x, L.alpha_y, L.h_col, L.h_row,
+                                            pl->p.iterations, pl->p.update_lag, pl->a_data64, pl->p.omega, beta, st));
+                } else {
+                    long long n_launch = 0;
+                    cudaError_t e = launch_x_sor_smooth(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, 2 * mn, pl->xdu,
+                                                        pl->xdv, pl->xwp, pl->xpsis, pl->xsnap, T, K, h, w,
+                                                        L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations,
+                                                        pl->p.update_lag, pl->a_data64, pl->p.a_smooth, pl->p.omega,
+                                                        beta, st, &n_launch);
+                    g_launches.fetch_add(n_launch, std::memory_order_relaxed);
+                    if (e != cudaSuccess)
+                        return fail(FRG_ECUDA, std::string("launch_x_sor_smooth: ") + cudaGetErrorString(e));
+                }
+                // the padded state is needed again unless this is the level's last step
+                const int write_ring = ws + 1 < pl->p.warping_steps ? 1 : 0;
+                cudaError_t e = launch_x_gnc_update(pl->xdu, pl->xdv, pl->xuv, pl->xuv + mn, 2 * mn, T, h, w,
+                                                    do_median, ou, ov, o_fs, o_rs, o_cs, write_ring, st);
+                g_launches.fetch_add(1 + write_ring, std::memory_order_relaxed);
+                if (e != cudaSuccess)
+                    return fail(FRG_ECUDA, std::string("launch_x_gnc_update: ") + cudaGetErrorString(e));
+            }
+            cur = nxt;
+            prev = &L;
+        }
+        if (pl->min_level > 0) {
+            FRG_LAUNCH(launch_cubic_up<double>(pl->xacc[cur], T, 2, prev->h, prev->w, pl->xtmp, flow_out,
+                                               (long long)H * W * 2, 1, (long long)W * 2, 2, H, W, pl->up_sx,
+                                               pl->up_wx, pl->up_sy, pl->up_wy, st));
+        }
+    }
+    return FRG_OK;
+}
+
 // The reference-order level loop (float64 solver), for FP64 plans and for
-// a_smooth != 1 in either precision.
+// a_smooth != 1, census and GNC stages in either precision.
 int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, double* flow_out, cudaStream_t st)
 {
+    if (pl->p.gnc_stages > 0) return run_xpath_gnc(pl, T, moving, uv_init, flow_out, st);
     const int H = pl->H, W = pl->W, K = pl->K;
     const long long fsz = (long long)H * W * K;
     int cur = 0;
@@ -1008,13 +1118,13 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
         if (pl->p.a_smooth == 1.0) {
             FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv, pl->xwp, T, K,
                                     h, w, L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations,
-                                    pl->p.update_lag, pl->a_data64, pl->p.omega, st));
+                                    pl->p.update_lag, pl->a_data64, pl->p.omega, -1.0, st));
         } else {
             long long n_launch = 0;
             cudaError_t e = launch_x_sor_smooth(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv,
                                                 pl->xwp, pl->xpsis, pl->xsnap, T, K, h, w, L.alpha_x, L.alpha_y,
                                                 L.h_col, L.h_row, pl->p.iterations, pl->p.update_lag, pl->a_data64,
-                                                pl->p.a_smooth, pl->p.omega, st, &n_launch);
+                                                pl->p.a_smooth, pl->p.omega, -1.0, st, &n_launch);
             g_launches.fetch_add(n_launch, std::memory_order_relaxed);
             if (e != cudaSuccess) return fail(FRG_ECUDA, std::string("launch_x_sor_smooth: ") + cudaGetErrorString(e));
         }

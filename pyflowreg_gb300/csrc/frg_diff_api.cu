@@ -443,6 +443,8 @@ int frg_diff_plan_create(const frg_params* params, int height, int width, int ch
         return host_fail(FRG_EUNSUPPORTED, "the differentiable mode supports a_smooth = 1 only");
     if (params->const_assumption != 0)
         return host_fail(FRG_EUNSUPPORTED, "the differentiable mode supports gradient constancy only");
+    if (params->gnc_stages != 0)
+        return host_fail(FRG_EUNSUPPORTED, "the differentiable mode has no GNC stages");
     if (params->precision != FRG_FP32 && params->precision != FRG_FP64_REFERENCE)
         return host_fail(FRG_EINVAL, "precision must be FRG_FP32 or FRG_FP64_REFERENCE");
 

@@ -347,10 +347,49 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
 // ---------------------------------------------------------------------------
 struct XAData { double a[kMaxK]; };
 
+// compute_flow_gnc (core/level_solver.py:408-446): with a stage weight beta in
+// [0, 1) (beta < 0: no GNC) an exponent a in (0, 1) gives (1 - beta) + beta * robust.
+__device__ __forceinline__ double gnc_mix(double robust, double a, double beta)
+{
+    if (beta >= 0.0 && beta < 1.0 && a > 0.0 && a < 1.0) return dadd(dsub(1.0, beta), dmul(beta, robust));
+    return robust;
+}
+
+// set_boundary_2d (core/level_solver.py:46-67) at the start of the last
+// iteration leaves every border cell of du, dv holding, at clamped
+// coordinates, the interior value of that moment: the border-adjacent pixel
+// (r, c) writes its pre-update value to the cells that clamp to it.  The
+// sweep itself never reads the border (the Neumann copy is the pixel's own
+// value), so only what follows the solve sees it.
+__device__ __forceinline__ void ring_snapshot(double* du, double* dv, int r, int c, int h, int w, double duc,
+                                              double dvc)
+{
+    const long long n = w + 2;
+    const int ys[2] = {r == 0 ? 0 : -1, r == h - 1 ? h + 1 : -1};
+    const int xs[2] = {c == 0 ? 0 : -1, c == w - 1 ? w + 1 : -1};
+    for (int a = 0; a < 2; ++a) {
+        if (ys[a] < 0) continue;
+        const long long q = (long long)ys[a] * n + c + 1;
+        du[q] = duc;
+        dv[q] = dvc;
+        for (int b = 0; b < 2; ++b) {
+            if (xs[b] < 0) continue;
+            du[(long long)ys[a] * n + xs[b]] = duc;
+            dv[(long long)ys[a] * n + xs[b]] = dvc;
+        }
+    }
+    for (int b = 0; b < 2; ++b) {
+        if (xs[b] < 0) continue;
+        const long long q = (long long)(r + 1) * n + xs[b];
+        du[q] = duc;
+        dv[q] = dvc;
+    }
+}
+
 __global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ W, const double* __restrict__ u,
                        const double* __restrict__ v, long long uv_fs, double* du_g, double* dv_g, double* wp_g,
                        int K, int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
-                       int update_lag, XAData ad, double omega)
+                       int update_lag, XAData ad, double omega, double gnc_beta)
 {
     const int f = blockIdx.x;
     const int n = w + 2, m = h + 2;
@@ -380,6 +419,8 @@ __global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ 
                 if (c >= w) continue;
                 const long long o = (long long)(r + 1) * n + (c + 1);
                 const double duc = du[o], dvc = dv[o];
+                if (t == iterations - 1 && (r == 0 || r == h - 1 || c == 0 || c == w - 1))
+                    ring_snapshot(du, dv, r, c, h, w, duc, dvc);
                 if ((t + 1) % update_lag == 0) {
                     // core/level_solver.py:230-246 (J23*dv appears twice, as in the reference)
                     for (int k = 0; k < K; ++k) {
@@ -392,7 +433,8 @@ __global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ 
                         val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
                         val = dadd(val, Jf[2 * qs + ok]);
                         if (val < 0.0) val = 0.0;
-                        const double psi = dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0)));
+                        const double psi =
+                            gnc_mix(dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0))), ad.a[k], gnc_beta);
                         wp[ok] = dmul(W[ok], psi);
                     }
                 }
@@ -447,13 +489,13 @@ __global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ 
 cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
                          double alpha_y, double hx, double hy, int iterations, int update_lag,
-                         const double* a_data, double omega, cudaStream_t st)
+                         const double* a_data, double omega, double gnc_beta, cudaStream_t st)
 {
     XAData ad;
     for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0;
     const int threads = h >= 512 ? 512 : ((h + 31) / 32) * 32;
     kx_sor<<<n_frames, threads, 0, st>>>(J, W, u, v, uv_fs, du, dv, wp, K, h, w, alpha_x, alpha_y, hx, hy,
-                                         iterations, update_lag, ad, omega);
+                                         iterations, update_lag, ad, omega, gnc_beta);
     return cudaGetLastError();
 }
 
@@ -484,7 +526,7 @@ __global__ void kx_smooth_tick(const double* __restrict__ J, const double* __res
                                const double* __restrict__ u, const double* __restrict__ v, long long uv_fs,
                                const double* __restrict__ du_g, const double* __restrict__ dv_g,
                                const double* __restrict__ snap, double* __restrict__ wp_g, double* __restrict__ psi_g,
-                               int K, int h, int w, double hx, double hy, XAData ad, double a_s)
+                               int K, int h, int w, double hx, double hy, XAData ad, double a_s, double gnc_beta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;  // column of the padded grid
     const int j = blockIdx.y;                              // row of the padded grid
@@ -513,7 +555,8 @@ __global__ void kx_smooth_tick(const double* __restrict__ J, const double* __res
             val = dadd(val, dmul(Jf[5 * qs + ok], dvc));
             val = dadd(val, Jf[2 * qs + ok]);
             if (val < 0.0) val = 0.0;
-            const double psi = dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0)));
+            const double psi =
+                gnc_mix(dmul(ad.a[k], pow(dadd(val, 0.00001), dsub(ad.a[k], 1.0))), ad.a[k], gnc_beta);
             wp_g[(f * K + k) * mn + o] = dmul(W[ok], psi);
         }
     }
@@ -555,7 +598,7 @@ __global__ void kx_smooth_tick(const double* __restrict__ J, const double* __res
     }
     double tmp = dadd(dadd(dadd(dmul(ux, ux), dmul(uy, uy)), dmul(vx, vx)), dmul(vy, vy));
     if (tmp < 0.0) tmp = 0.0;
-    psi_g[f * mn + o] = dmul(a_s, pow(dadd(tmp, 0.00001), dsub(a_s, 1.0)));
+    psi_g[f * mn + o] = gnc_mix(dmul(a_s, pow(dadd(tmp, 0.00001), dsub(a_s, 1.0))), a_s, gnc_beta);
 }
 
 // Iterations [t0, t1) of the lexicographic SOR as one wavefront (pixel (r, c)
@@ -595,6 +638,7 @@ __global__ void kx_sor_range(const double* __restrict__ J, const double* __restr
                 if (tl == nit - 1) {
                     sn[o] = duc;
                     sn[mn + o] = dvc;
+                    if (r == 0 || r == h - 1 || c == 0 || c == w - 1) ring_snapshot(du, dv, r, c, h, w, duc, dvc);
                 }
                 const double duL = c > 0 ? du[o - 1] : duc, dvL = c > 0 ? dv[o - 1] : dvc;
                 const double duR = c < w - 1 ? du[o + 1] : duc, dvR = c < w - 1 ? dv[o + 1] : dvc;
@@ -650,8 +694,8 @@ __global__ void kx_sor_range(const double* __restrict__ J, const double* __restr
 cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                                 double* du, double* dv, double* wp, double* psi_s, double* snap, int n_frames, int K,
                                 int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
-                                int update_lag, const double* a_data, double a_smooth, double omega, cudaStream_t st,
-                                long long* launches)
+                                int update_lag, const double* a_data, double a_smooth, double omega, double gnc_beta,
+                                cudaStream_t st, long long* launches)
 {
     XAData ad;
     for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0;
@@ -666,7 +710,7 @@ cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* 
     while (t < iterations) {
         if ((t + 1) % update_lag == 0) {
             kx_smooth_tick<<<dim3((unsigned)((w + 2 + 127) / 128), (unsigned)(h + 2), (unsigned)n_frames), 128, 0, st>>>(
-                J, W, u, v, uv_fs, du, dv, snap, wp, psi_s, K, h, w, hx, hy, ad, a_smooth);
+                J, W, u, v, uv_fs, du, dv, snap, wp, psi_s, K, h, w, hx, hy, ad, a_smooth, gnc_beta);
             ++*launches;
         }
         int t1 = t + 1;
@@ -773,6 +817,92 @@ cudaError_t launch_x_median_accum(const double* du, const double* dv, const doub
 {
     dim3 blk(128), grd((w + 127) / 128, h, n_frames);
     kx_median_accum<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// GNC warping step update (core/optical_flow.py:745-755): u = u + du over the
+// padded grid, then, when min(h, w) > 5, u = add_boundary(median5(u interior)).
+// kx_gnc_median writes the new interior (strides o_fs, o_rs, o_cs) from the
+// padded u, du; kx_gnc_ring then rewrites the padded u from it: the interior,
+// and the border as the edge copy (median) or as u + du (no median).
+// ---------------------------------------------------------------------------
+__global__ void kx_gnc_median(const double* __restrict__ du, const double* __restrict__ dv,
+                              const double* __restrict__ u, const double* __restrict__ v, long long uv_fs, int h, int w,
+                              int do_median, double* ou, double* ov, long long o_fs, long long o_rs, long long o_cs)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int f = blockIdx.z;
+    if (x >= w) return;
+    const long long n = w + 2, mn = (long long)(h + 2) * n;
+    const double* duf = du + (long long)f * mn;
+    const double* dvf = dv + (long long)f * mn;
+    const double* uf = u + f * uv_fs;
+    const double* vf = v + f * uv_fs;
+    double mu, mv;
+    if (do_median) {
+        double a[25], b[25];
+        int q = 0;
+        for (int dy = -2; dy <= 2; ++dy) {
+            int yy = y + dy;
+            if (yy < 0) yy = -yy;
+            if (yy >= h) yy = 2 * (h - 1) - yy;
+            for (int dx = -2; dx <= 2; ++dx) {
+                int xx = x + dx;
+                if (xx < 0) xx = -xx;
+                if (xx >= w) xx = 2 * (w - 1) - xx;
+                const long long o = (long long)(yy + 1) * n + xx + 1;
+                a[q] = dadd(uf[o], duf[o]);
+                b[q] = dadd(vf[o], dvf[o]);
+                ++q;
+            }
+        }
+        mu = median25d(a);
+        mv = median25d(b);
+    } else {
+        const long long o = (long long)(y + 1) * n + x + 1;
+        mu = dadd(uf[o], duf[o]);
+        mv = dadd(vf[o], dvf[o]);
+    }
+    ou[f * o_fs + y * o_rs + x * o_cs] = mu;
+    ov[f * o_fs + y * o_rs + x * o_cs] = mv;
+}
+
+__global__ void kx_gnc_ring(const double* __restrict__ au, const double* __restrict__ av, long long a_fs,
+                            long long a_rs, long long a_cs, const double* __restrict__ du,
+                            const double* __restrict__ dv, double* u, double* v, long long uv_fs, int h, int w,
+                            int do_median)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // padded column
+    const int j = blockIdx.y;                              // padded row
+    const int f = blockIdx.z;
+    const int n = w + 2;
+    if (i >= n) return;
+    const long long mn = (long long)(h + 2) * n, q = (long long)j * n + i;
+    const bool interior = j >= 1 && j <= h && i >= 1 && i <= w;
+    double* uf = u + f * uv_fs;
+    double* vf = v + f * uv_fs;
+    if (interior || do_median) {
+        const long long a = f * a_fs + (long long)(xclamp(j, 1, h) - 1) * a_rs + (long long)(xclamp(i, 1, w) - 1) * a_cs;
+        uf[q] = au[a];
+        vf[q] = av[a];
+    } else {
+        uf[q] = dadd(uf[q], du[(long long)f * mn + q]);
+        vf[q] = dadd(vf[q], dv[(long long)f * mn + q]);
+    }
+}
+
+cudaError_t launch_x_gnc_update(const double* du, const double* dv, double* u, double* v, long long uv_fs,
+                                int n_frames, int h, int w, int do_median, double* ou, double* ov, long long o_fs,
+                                long long o_rs, long long o_cs, int write_ring, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
+    kx_gnc_median<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !write_ring) return e;
+    dim3 grd2((w + 2 + 127) / 128, h + 2, n_frames);
+    kx_gnc_ring<<<grd2, blk, 0, st>>>(ou, ov, o_fs, o_rs, o_cs, du, dv, u, v, uv_fs, h, w, do_median);
     return cudaGetLastError();
 }
 

@@ -111,15 +111,16 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
 cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
                          double alpha_y, double hx, double hy, int iterations, int update_lag,
-                         const double* a_data, double omega, cudaStream_t st);
+                         const double* a_data, double omega, double gnc_beta, cudaStream_t st);
 // a_smooth != 1: the SOR cut at the psi ticks (ticks recompute W psi and
 // psi_s over the padded grid).  psi_s (T, m*n) and snap (T, 2, m*n) are
-// workspace; *launches is incremented per kernel launched.
+// workspace; *launches is incremented per kernel launched.  gnc_beta < 0: compute_flow;
+// else compute_flow_gnc with that stage weight (both solvers).
 cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                                 double* du, double* dv, double* wp, double* psi_s, double* snap, int n_frames, int K,
                                 int h, int w, double alpha_x, double alpha_y, double hx, double hy, int iterations,
-                                int update_lag, const double* a_data, double a_smooth, double omega, cudaStream_t st,
-                                long long* launches);
+                                int update_lag, const double* a_data, double a_smooth, double omega, double gnc_beta,
+                                cudaStream_t st, long long* launches);
 cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st);
 // cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
 // (oh, ow): width pass into tmp, height pass into the strided dst view.
@@ -130,6 +131,12 @@ cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, in
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
+// One GNC warping step's state update (two kernels, the second only when
+// write_ring): (ou, ov) = [median5](u + du) interiors, then the padded u, v
+// rebuilt from them.  Counts 1 + write_ring launches.
+cudaError_t launch_x_gnc_update(const double* du, const double* dv, double* u, double* v, long long uv_fs,
+                                int n_frames, int h, int w, int do_median, double* ou, double* ov, long long o_fs,
+                                long long o_rs, long long o_cs, int write_ring, cudaStream_t st);
 
 // Preprocessing and post-registration statistics (frg_prep.cu).
 // taps w[k][0 .. r] stored with stride (max_k r + 1); radii per channel (host arrays)

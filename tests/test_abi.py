@@ -25,7 +25,7 @@ def test_library_builds_and_exports_all_symbols():
     assert len(names) >= 15
     for name in names:
         assert hasattr(lib, name), f"{name} declared in the header but not exported"
-    assert lib.frg_version() == 1
+    assert lib.frg_version() == 2
 
 
 def test_symbols_are_plain_c():

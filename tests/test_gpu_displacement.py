@@ -252,7 +252,7 @@ def test_deterministic():
 def test_unsupported_options_raise():
     fixed, moving, _ = pair_256(4, h=32, w=32)
     with pytest.raises(NotImplementedError):
-        G.get_displacement(fixed, moving, gnc_schedule=(0.0, 1.0))
+        G.get_displacement(fixed, moving, level_solver_backend=lambda *a, **k: None)
     with pytest.raises(ValueError):
         G.get_displacement(fixed, moving, const_assumption="nope")
     with pytest.raises(ValueError):

@@ -71,7 +71,11 @@ def test_full_displacement(oracle, golden_dir):
     np.testing.assert_array_equal(e, f["e_flow"])
     cs = oracle.get_displacement(f["b_fixed"], f["b_moving"], const_assumption="cs", iterations=12, semantics="python")
     np.testing.assert_array_equal(cs, f["f_flow"])
-    an = oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
+    # graduated non-convexity: three stages, two warping steps per level
+    gnc = oracle.get_displacement(f["b_fixed"], f["b_moving"], alpha=(1.5, 1.5), gnc_schedule=(0.0, 0.5, 1.0),
+                                  warping_steps=2, iterations=6, a_smooth=0.7, semantics="python")
+    np.testing.assert_array_equal(gnc, f["g_flow"])
+    an =oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
     assert np.abs(an - f["a_flow"]).max() < 1e-4
 
 
