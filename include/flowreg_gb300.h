@@ -16,6 +16,8 @@
  *   frg_level_solve  replaces compute_flow via the level_solver_backend seam
  *                                                        core/optical_flow.py:348-411, 584-606
  *                                                        core/level_solver.py:158-369
+ *   frg_level_solve_f64 replaces compute_flow / compute_flow_gnc at that seam
+ *                    in float64                          core/level_solver.py:158-555
  *   frg_imregister   replaces imregister_wrapper          core/warping.py:160-234
  *   frg_resize       replaces imresize_fused_gauss_cubic  util/resize_util.py:232-254
  *   frg_motion_tensor replaces get_motion_tensor_gc/_gray core/optical_flow.py:73-228
@@ -203,6 +205,19 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
                             int update_lag, const double* a_data, double a_smooth, double hx, double hy,
                             double omega, float* du, float* dv, void* stream);
 size_t frg_level_solve_noalloc_capacity(void);
+
+/* The level solver in the reference's own precision and operation order, for
+ * the level_solver_backend seam fed with the reference's float64 arrays
+ * (core/optical_flow.py:348-411): compute_flow (core/level_solver.py:158-369)
+ * when gnc_beta < 0, compute_flow_gnc (core/level_solver.py:372-555) with
+ * that stage weight when gnc_beta is in [0, 1]; any a_smooth > 0.  Layouts as
+ * frg_level_solve, all arrays double on the device; du, dv receive the whole
+ * (m, n) result, their rings as set_boundary_2d left them at the start of the
+ * last iteration.  Allocates its scratch with cudaMallocAsync on `stream`. */
+int frg_level_solve_f64(int m, int n, int K, const double* J, const double* weight, const double* u,
+                        const double* v, double alpha_x, double alpha_y, int iterations, int update_lag,
+                        const double* a_data, double a_smooth, double hx, double hy, double omega,
+                        double gnc_beta, double* du, double* dv, void* stream);
 
 /* Fused Gauss-cubic resize of n_planes planes (n_planes, ih, iw) to
  * (n_planes, oh, ow), sigma = 0.6 / min(oh/ih, ow/iw) when that is < 1. */

@@ -102,6 +102,7 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_level_solve", I, [I, I, I, P, P, P, P, D, D, I, I, pD, D, D, D, D, P, P, P])
         _sig(lib, "frg_level_solve_noalloc", I, [I, I, I, P, P, P, P, D, D, I, I, pD, D, D, D, D, P, P, P])
         _sig(lib, "frg_level_solve_noalloc_capacity", S, [])
+        _sig(lib, "frg_level_solve_f64", I, [I, I, I, P, P, P, P, D, D, I, I, pD, D, D, D, D, D, P, P, P])
         _sig(lib, "frg_resize", I, [I, I, I, P, I, I, P, P])
         _sig(lib, "frg_motion_tensor", I, [I, I, P, P, D, D, I, P, P])
         _sig(lib, "frg_median5", I, [I, I, P, P, P])

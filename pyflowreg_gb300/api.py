@@ -497,15 +497,22 @@ def imregister_wrapper(f2_level, u, v, f1_level, interpolation_method="cubic"):
 # level_solver seam (core/optical_flow.py:348-411)
 # --------------------------------------------------------------------------
 def level_solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag, verbose, a_data,
-                 a_smooth, hx, hy, gnc_beta=None):
-    """GPU level solver with the positional signature of ``level_solver_backend``.
+                 a_smooth, hx, hy, gnc_beta=None, precision="fp32"):
+    """GPU level solver with the signature of ``level_solver_backend``
+    (core/optical_flow.py:348-411).
 
-    Runs compute_flow's exact update order on the device in float32 and
-    returns (du, dv) as float64 (m, n) arrays.
+    Runs compute_flow's exact update order on the device and returns (du, dv)
+    as float64 (m, n) arrays.  precision "fp32" is the fast solver
+    (a_smooth = 1, no GNC); "fp64" -- taken as well whenever a_smooth != 1 or
+    gnc_beta is given -- computes in the reference's float64 arithmetic,
+    compute_flow_gnc when gnc_beta is not None.
     """
     _require_cuda()
-    if gnc_beta is not None:
-        raise NotImplementedError("GNC stages are not implemented by the GB300 backend")
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+    if precision == "fp64" or gnc_beta is not None or float(a_smooth) != 1.0:
+        return _level_solver_f64(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag,
+                                 a_data, a_smooth, hx, hy, gnc_beta)
     J = np.stack([np.asarray(a, dtype=np.float32) for a in (J11, J22, J33, J12, J13, J23)])
     if J.ndim == 3:
         J = J[..., None]
@@ -530,6 +537,37 @@ def level_solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, 
                                    _stream_ptr()), "frg_level_solve")
     torch.cuda.current_stream().synchronize()
     return du.cpu().numpy().astype(np.float64), dv.cpu().numpy().astype(np.float64)
+
+
+def _level_solver_f64(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag, a_data,
+                     a_smooth, hx, hy, gnc_beta):
+    J = np.stack([np.asarray(a, dtype=np.float64) for a in (J11, J22, J33, J12, J13, J23)])
+    if J.ndim == 3:
+        J = J[..., None]
+    _, m, n, K = J.shape
+    wgt = np.asarray(weight, dtype=np.float64)
+    if wgt.ndim == 2:
+        wgt = wgt[..., None]
+    wgt = np.ascontiguousarray(np.broadcast_to(wgt, (m, n, K)))
+    ad = np.ascontiguousarray(normalize_a_data(a_data, K))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    Jt = torch.from_numpy(np.ascontiguousarray(J)).to(dev)
+    Wt = torch.from_numpy(wgt).to(dev)
+    ut = torch.from_numpy(np.ascontiguousarray(u, dtype=np.float64)).to(dev)
+    vt = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+    du = torch.empty((m, n), dtype=torch.float64, device=dev)
+    dv = torch.empty((m, n), dtype=torch.float64, device=dev)
+    ax, ay = alpha_pair(alpha)
+    beta = -1.0 if gnc_beta is None else float(gnc_beta)
+    if not (beta < 0.0 or 0.0 <= beta <= 1.0):
+        raise ValueError("gnc_beta must lie in [0, 1]")
+    lib = _lib.load()
+    _lib.check(lib.frg_level_solve_f64(m, n, K, _ptr(Jt), _ptr(Wt), _ptr(ut), _ptr(vt), ax, ay, int(iterations),
+                                       int(update_lag), ad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       float(a_smooth), float(hx), float(hy), 1.95, beta, _ptr(du), _ptr(dv),
+                                       _stream_ptr()), "frg_level_solve_f64")
+    torch.cuda.current_stream().synchronize()
+    return du.cpu().numpy(), dv.cpu().numpy()
 
 
 # --------------------------------------------------------------------------

@@ -1230,6 +1230,50 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
     return rc;
 }
 
+int frg_level_solve_f64(int m, int n, int K, const double* J, const double* weight, const double* u, const double* v,
+                        double alpha_x, double alpha_y, int iterations, int update_lag, const double* a_data,
+                        double a_smooth, double hx, double hy, double omega, double gnc_beta, double* du, double* dv,
+                        void* stream)
+{
+    if (!J || !weight || !u || !v || !a_data || !du || !dv) return fail(FRG_EINVAL, "NULL argument");
+    if (m < 3 || n < 3 || K < 1 || K > kMaxK) return fail(FRG_EINVAL, "bad shape");
+    if (iterations < 1 || update_lag < 1) return fail(FRG_EINVAL, "iterations and update_lag must be >= 1");
+    if (!(a_smooth > 0.0)) return fail(FRG_EINVAL, "a_smooth must be > 0");
+    if (gnc_beta > 1.0) return fail(FRG_EINVAL, "gnc_beta must lie in [0, 1] (negative: no GNC)");
+    const int h = m - 2, w = n - 2;
+    const long long mn = (long long)m * n;
+    const bool smooth = a_smooth != 1.0;
+    cudaStream_t st = (cudaStream_t)stream;
+    double* scratch = nullptr;
+    const size_t elems = (size_t)(6 * K + 2 * K + (smooth ? 3 : 0)) * mn;
+    FRG_CUDA(cudaMallocAsync((void**)&scratch, elems * sizeof(double), st));
+    double* Jp = scratch;              // (6, K, mn)
+    double* Wp = Jp + 6LL * K * mn;    // (K, mn)
+    double* wp = Wp + (long long)K * mn;
+    double* psis = wp + (long long)K * mn;
+    double* snap = psis + mn;
+    auto run = [&]() -> int {
+        FRG_LAUNCH(launch_x_hwk_to_planes(J, 6, mn, K, Jp, st));
+        FRG_LAUNCH(launch_x_hwk_to_planes(weight, 1, mn, K, Wp, st));
+        if (!smooth) {
+            FRG_LAUNCH(launch_x_sor(Jp, Wp, u, v, 0, du, dv, wp, 1, K, h, w, alpha_x, alpha_y, hx, hy, iterations,
+                                    update_lag, a_data, omega, gnc_beta, st));
+        } else {
+            long long n_launch = 0;
+            cudaError_t e = launch_x_sor_smooth(Jp, Wp, u, v, 0, du, dv, wp, psis, snap, 1, K, h, w, alpha_x,
+                                                alpha_y, hx, hy, iterations, update_lag, a_data, a_smooth, omega,
+                                                gnc_beta, st, &n_launch);
+            g_launches.fetch_add(n_launch, std::memory_order_relaxed);
+            if (e != cudaSuccess) return fail(FRG_ECUDA, std::string("launch_x_sor_smooth: ") + cudaGetErrorString(e));
+        }
+        return FRG_OK;
+    };
+    const int rc = run();
+    cudaError_t e = cudaFreeAsync(scratch, st);
+    if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
+    return rc;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -737,6 +737,21 @@ cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaSt
     return cudaGetLastError();
 }
 
+// n_arrays arrays of (mn, K) channel-last doubles -> (n_arrays, K, mn) planes
+__global__ void kx_hwk_to_planes(const double* __restrict__ src, long long mn, int K, double* __restrict__ dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long a = blockIdx.y;
+    if (i >= mn) return;
+    for (int k = 0; k < K; ++k) dst[(a * K + k) * mn + i] = src[(a * mn + i) * K + k];
+}
+
+cudaError_t launch_x_hwk_to_planes(const double* src, int n_arrays, long long mn, int K, double* dst, cudaStream_t st)
+{
+    kx_hwk_to_planes<<<dim3((unsigned)((mn + 255) / 256), (unsigned)n_arrays), 256, 0, st>>>(src, mn, K, dst);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Median (scipy "mirror", exact selection) and accumulate in float64
 // (core/optical_flow.py:607-611).  du, dv, u, v: padded (m, n) planes; output

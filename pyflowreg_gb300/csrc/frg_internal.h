@@ -122,6 +122,7 @@ cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* 
                                 int update_lag, const double* a_data, double a_smooth, double omega, double gnc_beta,
                                 cudaStream_t st, long long* launches);
 cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st);
+cudaError_t launch_x_hwk_to_planes(const double* src, int n_arrays, long long mn, int K, double* dst, cudaStream_t st);
 // cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
 // (oh, ow): width pass into tmp, height pass into the strided dst view.
 template <typename T>

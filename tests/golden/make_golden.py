@@ -147,6 +147,11 @@ def main():
         res = ls.compute_flow(*[np.ascontiguousarray(a) for a in Js], wgt, uu, vv, 1.7, 2.3, 23, lag,
                               np.array([0.45, 0.6]), a_s, 1.25, 0.8)
         sol[name] = res
+    # compute_flow_gnc (core/level_solver.py:372-555): the GNC stage weight mixes psi and psi_s
+    for name, a_s, lag, beta in (("gnc0_smooth05", 0.5, 3, 0.0), ("gnc05_smooth1", 1.0, 5, 0.5),
+                                 ("gnc05_smooth05", 0.5, 3, 0.5)):
+        sol[name] = ls.compute_flow_gnc(*[np.ascontiguousarray(a) for a in Js], wgt, uu, vv, 1.7, 2.3, 23, lag,
+                                        np.array([0.45, 0.6]), a_s, 1.25, 0.8, beta)
     out["solver"] = sol
 
     # 5) full get_displacement (core/optical_flow.py:773-929)

@@ -124,3 +124,39 @@ def test_host_tables_pinned_to_golden(golden_dir):
         ix, wx = tables.resize_tables(iw, ow, sig)
         np.testing.assert_array_equal(ix, g[f"ix{q}"])
         np.testing.assert_allclose(wx, g[f"wx{q}"], rtol=0, atol=2e-7)
+
+
+def test_params_struct_layout_matches_header(tmp_path):
+    """The ctypes mirror of frg_params has the C struct's size and offsets."""
+    import subprocess
+
+    fields = [f[0] for f in _lib.FrgParams._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "flowreg_gb300.h"\nint main(void){\n'
+                   + 'printf("%zu\\n", sizeof(frg_params));\n'
+                   + "".join(f'printf("%zu\\n", offsetof(frg_params, {f}));\n' for f in fields) + "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(_lib.FrgParams)
+    assert vals[1:] == [getattr(_lib.FrgParams, f).offset for f in fields]
+
+
+@pytest.mark.parametrize("stages,sched,steps", [
+    (1, [0.0], 2), (3, [0.5, 0.7, 1.0], 2), (3, [0.0, 0.7, 0.5], 2), (2, [0.0, 0.9], 2), (2, [0.0, 1.0], 0),
+    (17, [0.0] * 16, 2), (2, [0.0, 1.5], 2),
+])
+def test_plan_create_rejects_bad_gnc_options(stages, sched, steps):
+    """normalize_gnc_schedule / normalize_warping_steps (core/optical_flow.py:414-443)
+    are checked before anything touches the device."""
+    from pyflowreg_gb300.api import make_params
+
+    lib = _lib.load()
+    p = make_params()
+    p.gnc_stages = stages
+    for i, b in enumerate(sched[:_lib.FRG_MAX_GNC_STAGES]):
+        p.gnc_schedule[i] = b
+    p.warping_steps = steps
+    out = ctypes.c_void_p()
+    assert lib.frg_plan_create(ctypes.byref(p), 32, 32, 1, 1, ctypes.byref(out)) == 1  # FRG_EINVAL
+    assert b"gnc" in lib.frg_last_error() or b"warping" in lib.frg_last_error()

@@ -60,3 +60,31 @@ def test_red_black_order_is_not_the_reference(oracle):
     e_gpu = np.abs(gpu - lex)[1:-1, 1:-1].max()
     e_rb = np.abs(rb - lex)[1:-1, 1:-1].max()
     assert e_gpu < 1e-4 < e_rb
+
+
+@pytest.mark.parametrize("name,a_s,lag,beta", [("smooth1", 1.0, 5, None), ("smooth05", 0.5, 3, None),
+                                               ("gnc0_smooth05", 0.5, 3, 0.0), ("gnc05_smooth1", 1.0, 5, 0.5),
+                                               ("gnc05_smooth05", 0.5, 3, 0.5)])
+def test_level_solve_f64_golden(golden_dir, name, a_s, lag, beta):
+    """The float64 seam (compute_flow / compute_flow_gnc) against the
+    reference's own solver output, rings included."""
+    g = np.load(f"{golden_dir}/solver.npz")
+    du, dv = G.level_solver(*g["J"], g["weight"], g["u"], g["v"], (1.7, 2.3), 23, lag, 0, np.array([0.45, 0.6]),
+                            a_s, 1.25, 0.8, gnc_beta=beta, precision="fp64")
+    got = np.stack([du, dv], axis=2)
+    assert got.dtype == np.float64
+    np.testing.assert_allclose(got, g[name], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("h,w,K,its,lag,a_s,beta", [
+    (21, 17, 2, 23, 3, 1.0, 0.25), (40, 64, 1, 30, 5, 0.6, 0.75), (64, 40, 3, 17, 1, 0.8, 0.0),
+    (33, 35, 1, 12, 4, 1.0, 1.0), (5, 4, 1, 9, 2, 0.7, 0.5),
+])
+def test_level_solve_f64_gnc_matches_oracle(oracle, h, w, K, its, lag, a_s, beta):
+    rng = np.random.default_rng(h * 11 + w)
+    J, wgt, u, v = level_inputs(rng, h, w, K, oracle)
+    a_data = np.linspace(0.45, 0.6, K)
+    ref = oracle.compute_flow(*J, wgt, u, v, 1.7, 2.3, its, lag, a_data, a_s, 1.25, 0.8, gnc_beta=beta)
+    du, dv = G.level_solver(*J, wgt, u, v, (1.7, 2.3), its, lag, 0, a_data, a_s, 1.25, 0.8, gnc_beta=beta)
+    got = np.stack([du, dv], axis=2)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9 * max(1.0, np.abs(ref).max()))

@@ -53,6 +53,20 @@ def test_level_solver(oracle, golden_dir, name, a_s, lag):
     np.testing.assert_array_equal(r, g[name])
 
 
+@pytest.mark.parametrize("name,a_s,lag,beta", [("gnc0_smooth05", 0.5, 3, 0.0), ("gnc05_smooth1", 1.0, 5, 0.5),
+                                               ("gnc05_smooth05", 0.5, 3, 0.5)])
+def test_level_solver_gnc(oracle, golden_dir, name, a_s, lag, beta):
+    g = load(golden_dir, "solver")
+    r = oracle.compute_flow(*g["J"], g["weight"], g["u"], g["v"], 1.7, 2.3, 23, lag, np.array([0.45, 0.6]), a_s,
+                            1.25, 0.8, gnc_beta=beta)
+    np.testing.assert_array_equal(r, g[name])
+    # beta = 1 is the plain solver
+    plain = oracle.compute_flow(*g["J"], g["weight"], g["u"], g["v"], 1.7, 2.3, 23, lag, np.array([0.45, 0.6]),
+                                a_s, 1.25, 0.8)
+    np.testing.assert_array_equal(oracle.compute_flow(*g["J"], g["weight"], g["u"], g["v"], 1.7, 2.3, 23, lag,
+                                                      np.array([0.45, 0.6]), a_s, 1.25, 0.8, gnc_beta=1.0), plain)
+
+
 def test_full_displacement(oracle, golden_dir):
     f = load(golden_dir, "full")
     a = oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="python")
@@ -75,7 +89,7 @@ def test_full_displacement(oracle, golden_dir):
     gnc = oracle.get_displacement(f["b_fixed"], f["b_moving"], alpha=(1.5, 1.5), gnc_schedule=(0.0, 0.5, 1.0),
                                   warping_steps=2, iterations=6, a_smooth=0.7, semantics="python")
     np.testing.assert_array_equal(gnc, f["g_flow"])
-    an =oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
+    an = oracle.get_displacement(f["a_fixed"], f["a_moving"], alpha=(1.5, 1.5), semantics="numba")
     assert np.abs(an - f["a_flow"]).max() < 1e-4
 
 
