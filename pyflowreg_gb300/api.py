@@ -520,7 +520,7 @@ def level_solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, 
     wgt = np.asarray(weight, dtype=np.float32)
     if wgt.ndim == 2:
         wgt = wgt[..., None]
-    wgt = np.ascontiguousarray(np.broadcast_to(wgt, (m, n, K)))
+    wgt = np.array(np.broadcast_to(wgt, (m, n, K)), order="C")
     ad = np.ascontiguousarray(normalize_a_data(a_data, K))
     dev = torch.device("cuda", torch.cuda.current_device())
     Jt = torch.from_numpy(np.ascontiguousarray(J)).to(dev)
@@ -548,7 +548,7 @@ def _level_solver_f64(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterati
     wgt = np.asarray(weight, dtype=np.float64)
     if wgt.ndim == 2:
         wgt = wgt[..., None]
-    wgt = np.ascontiguousarray(np.broadcast_to(wgt, (m, n, K)))
+    wgt = np.array(np.broadcast_to(wgt, (m, n, K)), order="C")
     ad = np.ascontiguousarray(normalize_a_data(a_data, K))
     dev = torch.device("cuda", torch.cuda.current_device())
     Jt = torch.from_numpy(np.ascontiguousarray(J)).to(dev)
