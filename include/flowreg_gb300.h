@@ -12,7 +12,7 @@
  * Reference interfaces (pyflowreg, paths relative to src/pyflowreg/):
  *   frg_plan_create / frg_set_reference / frg_get_displacement
  *       replace get_displacement(fixed, moving, ...)     core/optical_flow.py:773-929
- *       called once per frame by the executors          motion_correction/parallelization/sequential.py:296-298
+ *       called once per frame by the executors          motion_correction/parallelization/sequential.py:141-145
  *   frg_level_solve  replaces compute_flow via the level_solver_backend seam
  *                                                        core/optical_flow.py:348-411, 584-606
  *                                                        core/level_solver.py:158-369
@@ -250,6 +250,12 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream);
 int frg_preprocess(int n_frames, int height, int width, int channels, const float* raw, const double* lo,
                    const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
                    const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, void* stream);
+/* frg_preprocess for float64 frames (the raw reference is held in float64,
+ * motion_correction/compensate_recording.py:491-498): numpy then normalises
+ * in float64, so there is no f32_norm argument; f32_storage must be 0. */
+int frg_preprocess_f64(int n_frames, int height, int width, int channels, const double* raw, const double* lo,
+                       const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                       const double* wx, const int* rx, int f32_storage, void* tmp, float* out, void* stream);
 
 /* Post-registration pass over flows (n_frames, height, width, 2) float32:
  * valid (n_frames, height, width) uint8 0/255 masks of the backward warp
@@ -333,7 +339,7 @@ int frg_diff_forward(frg_diff_plan* plan, int n_frames, double alpha_x, double a
 int frg_diff_backward(frg_diff_plan* plan, const void* g_flow, void* g_fixed, void* g_moving, double* g_alpha,
                       int flags, void* stream);
 /* Continuous compensation warp out = src(x + flow) with out-of-bounds pixels
- * from fill (motion_correction/parallelization/sequential.py:300-307), and its
+ * from fill (motion_correction/parallelization/sequential.py:148-154), and its
  * adjoint (g_src, g_fill, g_flow overwritten; any may be NULL except g_src).
  * precision selects float (FRG_FP32) or double (FRG_FP64_REFERENCE). */
 int frg_diff_warp(int precision, int n_frames, int channels, int height, int width, const void* src,

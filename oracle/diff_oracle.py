@@ -268,7 +268,7 @@ def loss(fixed, moving, truth, w_true, alpha, weight, lam=0.1, **opts):
     """MSE(warp(moving, flow), truth) + lam * mean(|flow - w_true|^2) for one
     pair (K, H, W); the compensation warp uses the continuous warp with the
     reference frame for out-of-bounds pixels (motion_correction/parallelization/
-    sequential.py:300-307)."""
+    sequential.py:148-154)."""
     u, v = flow(fixed, moving, alpha, weight, **opts)
     reg = warp(moving, u, v, fixed, oob_fill=not opts.get("smooth_only", False))
     return ((reg - truth) ** 2).mean() + lam * ((u - w_true[0]) ** 2 + (v - w_true[1]) ** 2).mean()

@@ -107,6 +107,7 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_motion_tensor", I, [I, I, P, P, D, D, I, P, P])
         _sig(lib, "frg_median5", I, [I, I, P, P, P])
         _sig(lib, "frg_preprocess", I, [I, I, I, I, P, pD, pD, P, pI, P, pI, P, pI, I, I, P, P, P])
+        _sig(lib, "frg_preprocess_f64", I, [I, I, I, I, P, pD, pD, P, pI, P, pI, P, pI, I, P, P, P])
         _sig(lib, "frg_flow_post_workspace", S, [I, I, I])
         _sig(lib, "frg_flow_post", I, [I, I, I, P, P, P, P, P])
         _sig(lib, "frg_diff_plan_create", I, [pP, I, I, I, I, I, ctypes.POINTER(P)])

@@ -1,7 +1,7 @@
 """Uneven batches: frames of several sizes and channel counts registered in one call.
 
 pyflowreg registers one frame at a time (the executors call get_displacement
-per frame, motion_correction/parallelization/sequential.py:296-298), so a
+per frame, motion_correction/parallelization/sequential.py:141-145), so a
 recording of mixed sizes costs nothing extra there.  On the GPU a batch of
 mixed sizes is grouped by (height, width, channels): each group runs through
 its own cached plan as one batched launch sequence, the groups are spread

@@ -141,9 +141,10 @@ cudaError_t launch_x_gnc_update(const double* du, const double* dv, double* u, d
 
 // Preprocessing and post-registration statistics (frg_prep.cu).
 // taps w[k][0 .. r] stored with stride (max_k r + 1); radii per channel (host arrays)
-cudaError_t launch_preprocess(const float* raw, int T, int H, int W, int K, const double* lo, const double* den,
-                              const double* wt, const int* rt, const double* wy, const int* ry, const double* wx,
-                              const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, cudaStream_t st);
+cudaError_t launch_preprocess(const float* raw, const double* raw64, int T, int H, int W, int K, const double* lo,
+                              const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                              const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out,
+                              cudaStream_t st);
 cudaError_t launch_flow_post(const float* flow, int T, int H, int W, uint8_t* valid, double* part, double* stats,
                              cudaStream_t st);
 

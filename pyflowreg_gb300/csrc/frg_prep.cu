@@ -42,7 +42,8 @@ __device__ __forceinline__ int reflect_scipy(int i, int n)
 }
 
 struct PrepArgs {
-    const float* raw;   // (T, H, W, K)
+    const float* raw;   // (T, H, W, K) float32 frames, or
+    const double* raw64;  // the same in float64 (then raw is NULL and numpy normalises in float64)
     int T, H, W, K;
     double lo[kMaxK], den[kMaxK];  // normalisation per channel (same value for all channels when joint)
     const double* wt;   // temporal taps [K][rt + 1] (channel k uses its first rtk[k] + 1)
@@ -68,7 +69,8 @@ __device__ __forceinline__ float normed<float>(const PrepArgs& A, int t, int y, 
 template <>
 __device__ __forceinline__ double normed<double>(const PrepArgs& A, int t, int y, int x, int k)
 {
-    const double v = (double)A.raw[(((long long)t * A.H + y) * A.W + x) * A.K + k];
+    const long long i = (((long long)t * A.H + y) * A.W + x) * A.K + k;
+    const double v = A.raw64 ? A.raw64[i] : (double)A.raw[i];
     return __ddiv_rn(__dsub_rn(v, A.lo[k]), A.den[k]);
 }
 
@@ -232,12 +234,14 @@ __global__ void k_flow_stats(const double* __restrict__ part, long long n_slots,
 
 }  // namespace
 
-cudaError_t launch_preprocess(const float* raw, int T, int H, int W, int K, const double* lo, const double* den,
-                              const double* wt, const int* rt, const double* wy, const int* ry, const double* wx,
-                              const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, cudaStream_t st)
+cudaError_t launch_preprocess(const float* raw, const double* raw64, int T, int H, int W, int K, const double* lo,
+                              const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                              const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out,
+                              cudaStream_t st)
 {
     PrepArgs A;
     A.raw = raw;
+    A.raw64 = raw64;
     A.T = T;
     A.H = H;
     A.W = W;
@@ -285,12 +289,15 @@ cudaError_t launch_flow_post(const float* flow, int T, int H, int W, uint8_t* va
 
 extern "C" {
 
-int frg_preprocess(int n_frames, int height, int width, int channels, const float* raw, const double* lo,
-                   const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
-                   const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, void* stream)
+namespace {
+
+int preprocess_checked(int n_frames, int height, int width, int channels, const float* raw, const double* raw64,
+                       const double* lo, const double* den, const double* wt, const int* rt, const double* wy,
+                       const int* ry, const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp,
+                       float* out, void* stream)
 {
     using namespace frg;
-    if (!raw || !lo || !den || !wt || !wy || !wx || !rt || !ry || !rx || !tmp || !out)
+    if ((!raw && !raw64) || !lo || !den || !wt || !wy || !wx || !rt || !ry || !rx || !tmp || !out)
         return host_fail(FRG_EINVAL, "NULL argument");
     if (n_frames < 1 || height < 1 || width < 1 || channels < 1 || channels > kMaxK)
         return host_fail(FRG_EINVAL, "bad shape");
@@ -298,13 +305,34 @@ int frg_preprocess(int n_frames, int height, int width, int channels, const floa
     for (int k = 0; k < channels; ++k)
         if (rt[k] < 0 || ry[k] < 0 || rx[k] < 0) return host_fail(FRG_EINVAL, "negative filter radius");
     if (f32_storage && !f32_norm) return host_fail(FRG_EINVAL, "float32 storage needs float32 normalisation");
+    if (raw64 && f32_norm) return host_fail(FRG_EINVAL, "float64 frames normalise in float64");
     for (int k = 0; k < channels; ++k)
         if (!(den[k] != 0.0)) return host_fail(FRG_EINVAL, "zero normalisation range");
     host_count_launches(2);
-    cudaError_t e = launch_preprocess(raw, n_frames, height, width, channels, lo, den, wt, rt, wy, ry, wx, rx,
+    cudaError_t e = launch_preprocess(raw, raw64, n_frames, height, width, channels, lo, den, wt, rt, wy, ry, wx, rx,
                                       f32_norm, f32_storage, tmp, out, (cudaStream_t)stream);
     if (e != cudaSuccess) return host_fail(FRG_ECUDA, cudaGetErrorString(e));
     return FRG_OK;
+}
+
+}  // namespace
+
+int frg_preprocess(int n_frames, int height, int width, int channels, const float* raw, const double* lo,
+                   const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                   const double* wx, const int* rx, int f32_norm, int f32_storage, void* tmp, float* out, void* stream)
+{
+    if (!raw) return frg::host_fail(FRG_EINVAL, "NULL argument");
+    return preprocess_checked(n_frames, height, width, channels, raw, nullptr, lo, den, wt, rt, wy, ry, wx, rx,
+                              f32_norm, f32_storage, tmp, out, stream);
+}
+
+int frg_preprocess_f64(int n_frames, int height, int width, int channels, const double* raw, const double* lo,
+                       const double* den, const double* wt, const int* rt, const double* wy, const int* ry,
+                       const double* wx, const int* rx, int f32_storage, void* tmp, float* out, void* stream)
+{
+    if (!raw) return frg::host_fail(FRG_EINVAL, "NULL argument");
+    return preprocess_checked(n_frames, height, width, channels, nullptr, raw, lo, den, wt, rt, wy, ry, wx, rx, 0,
+                              f32_storage, tmp, out, stream);
 }
 
 size_t frg_flow_post_workspace(int n_frames, int height, int width)

@@ -287,7 +287,7 @@ class _WarpFn(torch.autograd.Function):
 
 def warp(src, flw, fill):
     """Continuous compensation warp out = src(x + flow), out-of-bounds pixels
-    from fill (motion_correction/parallelization/sequential.py:300-307);
+    from fill (motion_correction/parallelization/sequential.py:148-154);
     src, fill (F, K, H, W), flow (F, 2, H, W); differentiable in all three."""
     if fill.dim() == 3:
         fill = fill.unsqueeze(0).expand_as(src)

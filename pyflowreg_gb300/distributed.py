@@ -2,7 +2,7 @@
 exchange of pyflowreg's batch loop.
 
 Frames of a batch are independent once ``w_init`` is fixed
-(motion_correction/parallelization/sequential.py:250-298), so ranks take
+(motion_correction/parallelization/sequential.py:97-163), so ranks take
 contiguous frame ranges and register them with no communication.  Between
 batches pyflowreg sets the next initial field to the mean of the last (up to
 20) flows of the batch (motion_correction/compensate_recording.py:801-806);

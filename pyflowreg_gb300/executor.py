@@ -3,7 +3,7 @@ one device pass.
 
 Implements ``BaseExecutor.process_batch`` (motion_correction/parallelization/
 base.py:76-110) with the semantics of ``SequentialExecutor.process_batch``
-(sequential.py:180-322, no cross-correlation pre-alignment): flow of every
+(sequential.py:27-169, no cross-correlation pre-alignment): flow of every
 frame against the preprocessed reference starting from ``w_init``, then the
 compensation warp of the raw frame against the raw reference.  The batch is
 uploaded once, all flows are computed by the batched plan, the warp runs on
@@ -49,8 +49,11 @@ class GB300Executor(BaseExecutor):
         ref_t = torch.from_numpy(np.ascontiguousarray(reference_raw, dtype=np.float32)).to(dev)
         reg = api.imregister_device(frames_t, flow_t, ref_t, interpolation_method).cpu().numpy()
         if np.issubdtype(batch.dtype, np.integer):
+            # registered[t] = reg_frame into np.empty_like(batch) (sequential.py:82, 159-163) casts
+            # unsafely: in-range values truncate toward zero; out-of-range ones (cubic overshoot),
+            # which numpy leaves to the platform, saturate here
             info = np.iinfo(batch.dtype)
-            reg = np.clip(np.rint(reg), info.min, info.max)
+            reg = np.clip(np.trunc(reg), info.min, info.max)
         registered = reg.astype(batch.dtype, copy=False)
         if progress_callback is not None:
             progress_callback(T)

@@ -77,14 +77,17 @@ def normalization(ref, K, channel_normalization="together", frames_dtype=np.floa
 def preprocess_device(frames, ref_raw, sigma=((1.0, 1.0, 0.1),), channel_normalization="together",
                       truncate: float = 4.0, frames_dtype=np.float32, out=None, stream=None):
     """frames: (T, H, W, K) or (H, W, K) float32 CUDA tensor holding the raw
-    values (exact for uint16 sources); ref_raw: the raw reference (numpy or
+    values (exact for uint16 sources), or float64 (then numpy's arithmetic is
+    float64 whatever frames_dtype says); ref_raw: the raw reference (numpy or
     tensor) whose min/max normalise.  sigma: (3,) or (K, 3) as (sy, sx, st).
     frames_dtype: the dtype the frames had in the reference pipeline (it
     decides float32 or float64 arithmetic as numpy would).  Returns float32."""
     single = frames.dim() == 3
     x = frames.unsqueeze(0) if single else frames
-    if not (x.is_cuda and x.dtype == torch.float32):
-        raise ValueError("frames must be a float32 CUDA tensor")
+    if not (x.is_cuda and x.dtype in (torch.float32, torch.float64)):
+        raise ValueError("frames must be a float32 or float64 CUDA tensor")
+    if x.dtype == torch.float64:
+        frames_dtype = np.float64
     x = x.contiguous()
     T, H, W, K = x.shape
     ref_np = ref_raw.detach().cpu().numpy() if torch.is_tensor(ref_raw) else np.asarray(ref_raw)
@@ -97,20 +100,23 @@ def preprocess_device(frames, ref_raw, sigma=((1.0, 1.0, 0.1),), channel_normali
     wy, ry = _taps_tensor([gaussian_taps(s[0], truncate) for s in sig], x.device)
     wx, rx = _taps_tensor([gaussian_taps(s[1], truncate) for s in sig], x.device)
     tmp = torch.empty((T * K * H * W,), dtype=torch.float32 if f32_store else torch.float64, device=x.device)
-    out_t = out if out is not None else torch.empty_like(x)
+    out_t = out if out is not None else torch.empty(x.shape, dtype=torch.float32, device=x.device)
     lib = _lib.load()
     pD = ctypes.POINTER(ctypes.c_double)
     lo_c = (ctypes.c_double * K)(*lo)
     den_c = (ctypes.c_double * K)(*den)
     s = stream if stream is not None else torch.cuda.current_stream()
     pI = ctypes.POINTER(ctypes.c_int)
-    _lib.check(lib.frg_preprocess(T, H, W, K, ctypes.c_void_p(x.data_ptr()), ctypes.cast(lo_c, pD),
-                                  ctypes.cast(den_c, pD), ctypes.c_void_p(wt.data_ptr()), ctypes.cast(rt, pI),
-                                  ctypes.c_void_p(wy.data_ptr()), ctypes.cast(ry, pI),
-                                  ctypes.c_void_p(wx.data_ptr()), ctypes.cast(rx, pI),
-                                  1 if f32 else 0, 1 if f32_store else 0, ctypes.c_void_p(tmp.data_ptr()),
-                                  ctypes.c_void_p(out_t.data_ptr()), ctypes.c_void_p(s.cuda_stream)),
-               "frg_preprocess")
+    common = (ctypes.cast(lo_c, pD), ctypes.cast(den_c, pD), ctypes.c_void_p(wt.data_ptr()), ctypes.cast(rt, pI),
+              ctypes.c_void_p(wy.data_ptr()), ctypes.cast(ry, pI), ctypes.c_void_p(wx.data_ptr()),
+              ctypes.cast(rx, pI))
+    tail = (ctypes.c_void_p(tmp.data_ptr()), ctypes.c_void_p(out_t.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+    if x.dtype == torch.float64:
+        _lib.check(lib.frg_preprocess_f64(T, H, W, K, ctypes.c_void_p(x.data_ptr()), *common, 0, *tail),
+                   "frg_preprocess_f64")
+    else:
+        _lib.check(lib.frg_preprocess(T, H, W, K, ctypes.c_void_p(x.data_ptr()), *common, 1 if f32 else 0,
+                                      1 if f32_store else 0, *tail), "frg_preprocess")
     return out_t[0] if single else out_t
 
 
