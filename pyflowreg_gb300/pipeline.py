@@ -86,7 +86,8 @@ def _mean_frames(x):
     acc = x[0].clone()
     for t in range(1, x.shape[0]):
         acc.add_(x[t])
-    return acc.div_(x.shape[0])
+    # a tensor divisor: torch turns division by a Python scalar into a multiplication by its reciprocal
+    return acc.div_(torch.full_like(acc, float(x.shape[0])))
 
 
 class _ArraySource:
