@@ -444,8 +444,10 @@ def run_gb300(args):
     if not args.no_autotune:
         # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
         chosen = plan.autotune(frames, n_levels=4, reps=1)
-        tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)": {"G": g, "threads": t}
-                  for i, (g, t, _) in chosen.items()}
+        tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
+                  {"kernel": ("rows_in_registers" if v == 1 else "diagonal_ring"), "G": g,
+                   "threads": t or plan.level_tuning()[i][3]}
+                  for i, (v, g, t, _) in chosen.items()}
     for _ in range(max(args.warmup, 3)):
         plan.displacement(frames, None, out)
     torch.cuda.synchronize()

@@ -132,6 +132,13 @@ int frg_plan_set_level_tables(frg_plan* plan, int level, int kind, int taps, con
  * not use the fused kernel report gmax 0 and accept only (0, 0). */
 int frg_plan_set_level_tuning(frg_plan* plan, int level, int sor_G, int sor_threads);
 int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_threads, int* gmax, int* rows);
+/* Which fused SOR kernel a level runs: 0 the diagonal ring in shared memory
+ * (any level up to 1024 rows; sor_threads applies), 1 one thread per row with
+ * the state in registers (levels up to 512 rows; sor_G applies, sor_threads
+ * does not).  Both give the same bits.  n_variants: how many serve the level
+ * (0 when it does not use a fused kernel). */
+int frg_plan_set_level_variant(frg_plan* plan, int level, int variant);
+int frg_plan_level_variant(const frg_plan* plan, int level, int* variant, int* n_variants);
 
 /* Reference (fixed) frame (height, width, channels) float32 and the per-pixel
  * channel weight (height, width, channels) float32 (NULL: 1/channels), as

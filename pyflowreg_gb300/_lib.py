@@ -92,6 +92,8 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_plan_set_level_tables", I, [P, I, I, I, pI, pF, pI, pF])
         _sig(lib, "frg_plan_set_level_tuning", I, [P, I, I, I])
         _sig(lib, "frg_plan_level_tuning", I, [P, I, pI, pI, pI, pI])
+        _sig(lib, "frg_plan_set_level_variant", I, [P, I, I])
+        _sig(lib, "frg_plan_level_variant", I, [P, I, pI, pI])
         _sig(lib, "frg_launch_count", ctypes.c_longlong, [])
         _sig(lib, "frg_plan_set_profiling", I, [P, I])
         _sig(lib, "frg_plan_profile", I, [P, ctypes.POINTER(ctypes.c_longlong), pD, pD])

@@ -245,13 +245,25 @@ class Plan:
         _lib.check(self.lib.frg_plan_set_level_tuning(self.handle, level, sor_G, sor_threads),
                    "frg_plan_set_level_tuning")
 
+    def level_variant(self, level: int):
+        """(variant, n_variants) of a level's fused SOR kernel: 0 the diagonal
+        ring, 1 rows with the state in registers; n_variants 0 when the level
+        does not use a fused kernel."""
+        v, n = ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.frg_plan_level_variant(self.handle, level, ctypes.byref(v), ctypes.byref(n)))
+        return v.value, n.value
+
+    def set_level_variant(self, level: int, variant: int) -> None:
+        _lib.check(self.lib.frg_plan_set_level_variant(self.handle, level, variant), "frg_plan_set_level_variant")
+
     def autotune(self, moving_t, n_levels: int = 5, reps: int = 2):
-        """Picks, for the `n_levels` finest levels that use the fused SOR kernel,
-        the iterations per wavefront pass and the threads per CTA that make
-        full calls on `moving_t` (a representative device batch) fastest:
-        coordinate descent from the finest level, each candidate timed with
-        CUDA events (best of `reps`).  The flows do not depend on the choice.
-        Returns {level: (sor_G, sor_threads, ms)}."""
+        """Picks, for the `n_levels` finest levels that use a fused SOR kernel,
+        the kernel variant, the iterations per wavefront pass and (ring variant)
+        the threads per CTA that make full calls on `moving_t` (a
+        representative device batch) fastest: coordinate descent from the
+        finest level, each candidate timed with CUDA events (best of `reps`).
+        The flows do not depend on the choice.
+        Returns {level: (variant, sor_G, sor_threads, ms)}."""
         tun = self.level_tuning()
         out_t = torch.empty((moving_t.shape[0], self.H, self.W, 2), dtype=torch.float32, device=moving_t.device)
 
@@ -275,14 +287,18 @@ class Plan:
             # every pass length: short passes free shared memory for a second CTA per SM
             gs = list(range(gmax, 0, -1))
             ths = sorted({t for t in (rows, ((rows * 3 // 2) + 31) // 32 * 32, 1024) if rows <= t <= 1024})
+            cands = [(0, g, t) for g in gs for t in ths]
+            if self.level_variant(i)[1] > 1:
+                cands += [(1, g, 0) for g in gs]
             best = None
-            for g in gs:
-                for t in ths:
-                    self.set_level_tuning(i, g, t)
-                    ms = timed()
-                    if best is None or ms < best[2]:
-                        best = (g, t, ms)
-            self.set_level_tuning(i, best[0], best[1])
+            for var, g, t in cands:
+                self.set_level_variant(i, var)
+                self.set_level_tuning(i, g, t)
+                ms = timed()
+                if best is None or ms < best[3]:
+                    best = (var, g, t, ms)
+            self.set_level_variant(i, best[0])
+            self.set_level_tuning(i, best[1], best[2])
             chosen[i] = best
         return chosen
 

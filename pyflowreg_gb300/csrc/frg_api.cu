@@ -271,6 +271,7 @@ struct LevelPlan {
     double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
     int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
+    int sor_variant = 0;  // fused SOR kernel: 0 diagonal ring in shared memory, 1 rows with the state in registers
 };
 
 // Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
@@ -444,11 +445,12 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
                 long long st_fs, float* coef, long long coef_fs, int T, int K, const DiagGeom& g,
                 const float* a_data, float wx, float wy, float omega, cudaStream_t st,
                 SorProfile* prof = nullptr, float* rm_du = nullptr, float* rm_dv = nullptr, long long rm_fs = 0,
-                int tune_G = 0, int tune_threads = 0)
+                int tune_G = 0, int tune_threads = 0, int tune_variant = 0)
 {
     const SorKind kind = sor_kind(K, g);
     const bool fused = kind == kSorFused;
-    int gmax = kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag);
+    const bool regs = fused && tune_variant == 1 && sor_regs_supports(K, g);
+    int gmax = kind == kSorFused ? (regs ? kGMax : sor_fused_gmax(g.P)) : (kind == kSorRows ? kGMax : update_lag);
     if (fused && tune_G > 0 && tune_G < gmax) gmax = tune_G;
     const std::vector<Pass> passes = make_passes(iterations, update_lag, gmax);
     for (size_t pi = 0; pi < passes.size(); ++pi) {
@@ -461,7 +463,13 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
             int rc = record_event(prof, st);
             if (rc) return rc;
         }
-        if (fused) {
+        if (regs) {
+            const bool continued = pi + 1 < passes.size() && passes[pi + 1].fold_mode < 0;
+            const bool final_pass = pi + 1 == passes.size();
+            FRG_LAUNCH(launch_sor_regs(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, T, K, g, ps.G,
+                                       ps.fold_mode, (ps.fold_mode >= 0 && continued) ? 1 : 0, a_data, wx, wy, omega,
+                                       st, final_pass ? rm_du : nullptr, final_pass ? rm_dv : nullptr, rm_fs));
+        } else if (fused) {
             const bool continued = pi + 1 < passes.size() && passes[pi + 1].fold_mode < 0;
             const bool final_pass = pi + 1 == passes.size();
             FRG_LAUNCH(launch_sor_fused(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, T, K, g, ps.G,
@@ -831,6 +839,28 @@ int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_
     return FRG_OK;
 }
 
+int frg_plan_set_level_variant(frg_plan* plan, int level, int variant)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    LevelPlan& L = plan->levels[level];
+    const bool fused = sor_kind(plan->K, L.g) == kSorFused;
+    if (variant < 0 || variant > 1) return fail(FRG_EINVAL, "variant must be 0 (diagonal ring) or 1 (rows in registers)");
+    if (variant == 1 && !(fused && sor_regs_supports(plan->K, L.g)))
+        return fail(FRG_EINVAL, "the rows-in-registers SOR does not serve this level");
+    L.sor_variant = variant;
+    return FRG_OK;
+}
+
+int frg_plan_level_variant(const frg_plan* plan, int level, int* variant, int* n_variants)
+{
+    if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
+    const LevelPlan& L = plan->levels[level];
+    const bool fused = sor_kind(plan->K, L.g) == kSorFused;
+    if (variant) *variant = L.sor_variant;
+    if (n_variants) *n_variants = fused ? (sor_regs_supports(plan->K, L.g) ? 2 : 1) : 0;
+    return FRG_OK;
+}
+
 int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, void* stream)
 {
     if (!pl || !fixed) return fail(FRG_EINVAL, "plan or fixed is NULL");
@@ -942,7 +972,8 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         const bool fused = sor_kind(K, L.g) == kSorFused;
         int rc = solve_level(pl->p.iterations, pl->p.update_lag, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du,
                              pl->dv, dp, pl->coef, 5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st,
-                             &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw, L.sor_G, L.sor_threads);
+                             &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw, L.sor_G, L.sor_threads,
+                             L.sor_variant);
         if (rc) return rc;
         // 6. median + accumulate (core/optical_flow.py:607-611)
         const int do_median = std::min(h, w) > 5 ? 1 : 0;

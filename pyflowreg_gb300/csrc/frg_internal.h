@@ -82,6 +82,15 @@ cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, lon
                              float* out_dv = nullptr, long long out_fs = 0, int threads = 0);
 // threads per CTA of launch_sor_fused: 0 = P (the rows of the level, rounded
 // up to 32); otherwise a multiple of 32 in [P, 1024].
+// The same pass with one thread per row and the state in registers (frg_sor.cu,
+// k_sor_regs): levels of at most 512 (padded) rows, K <= 4, G <= kGMax; same
+// arguments and bit-identical results.
+bool sor_regs_supports(int K, const DiagGeom& g);
+cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
+                            long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                            int n_frames, int K, DiagGeom g, int G, int mode, int store_coef, const float* a_data,
+                            float wx, float wy, float omega, cudaStream_t st, float* out_du = nullptr,
+                            float* out_dv = nullptr, long long out_fs = 0);
 // 5x5 median (mirror) of row-major du, dv (T, h, w) plus accumulation into u, v.
 cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
                              int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st);

@@ -85,58 +85,106 @@ __device__ __forceinline__ void load_raw(const SorArgs& A, const float* J, const
     }
 }
 
+// The five coefficients of one pixel: stored ones passed through (mode < 0),
+// or folded from J, W, lap and, at a psi tick, the pixel's du, dv
+// (core/level_solver.py:229-255, 342-364).  Explicit round-to-nearest
+// intrinsics fix every rounding, so every kernel that folds through here
+// gets the same bits.
+struct Coef {
+    float A12, BU, BV, iDu, iDv;
+};
+
+template <int K>
+__device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
+{
+    Coef o;
+    if (A.mode < 0) {
+        o.A12 = r.j[0];
+        o.BU = r.j[1];
+        o.BV = r.j[2];
+        o.iDu = r.j[3];
+        o.iDv = r.j[4];
+        return o;
+    }
+    const bool tick = (A.mode & 2) != 0;
+    float A11 = 0.f, A22 = 0.f, a12 = 0.f, C13 = 0.f, C23 = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float j11 = r.j[0 * K + k], j22 = r.j[1 * K + k], j33 = r.j[2 * K + k];
+        const float j12 = r.j[3 * K + k], j13 = r.j[4 * K + k], j23 = r.j[5 * K + k];
+        float psi = 1.0f;
+        if (tick) {
+            const float a = r.du, b = r.dv;
+            // E in the reference's order: J11 a a + J22 b b + J23 b + 2 J12 a b + 2 J13 a + J23 b + J33
+            float E = __fmul_rn(__fmul_rn(j11, a), a);
+            E = __fadd_rn(E, __fmul_rn(__fmul_rn(j22, b), b));
+            E = __fadd_rn(E, __fmul_rn(j23, b));
+            E = __fadd_rn(E, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, j12), a), b));
+            E = __fadd_rn(E, __fmul_rn(__fmul_rn(2.0f, j13), a));
+            E = __fadd_rn(E, __fmul_rn(j23, b));
+            E = __fadd_rn(E, j33);
+            E = fmaxf(E, 0.0f);
+            // (E + eps)^(a_k - 1) as exp2((a_k - 1) log2(E + eps)) on the special-function
+            // unit: relative error ~1e-6, the fp32 path's rounding level
+            psi = __fmul_rn(A.a_data[k],
+                            exp2f(__fmul_rn(__fsub_rn(A.a_data[k], 1.0f), __log2f(__fadd_rn(E, 1e-5f)))));
+        }
+        const float wp = __fmul_rn(r.w[k], psi);
+        A11 = __fmaf_rn(wp, j11, A11);
+        A22 = __fmaf_rn(wp, j22, A22);
+        a12 = __fmaf_rn(wp, j12, a12);
+        C13 = __fmaf_rn(wp, j13, C13);
+        C23 = __fmaf_rn(wp, j23, C23);
+    }
+    const float den_u = __fadd_rn(A.wsum, A11), den_v = __fadd_rn(A.wsum, A22);
+    o.A12 = a12;
+    o.BU = __fsub_rn(r.lu, C13);
+    o.BV = __fsub_rn(r.lv, C23);
+    o.iDu = den_u != 0.0f ? __frcp_rn(den_u) : 0.0f;
+    o.iDv = den_v != 0.0f ? __frcp_rn(den_v) : 0.0f;
+    return o;
+}
+
+__device__ __forceinline__ void store_coef(const SorArgs& A, const Coef& c, float* coef, long long o, long long plane)
+{
+    if (A.mode >= 0 && A.store_coef) {
+        coef[o] = c.A12;
+        coef[plane + o] = c.BU;
+        coef[2 * plane + o] = c.BV;
+        coef[3 * plane + o] = c.iDu;
+        coef[4 * plane + o] = c.iDv;
+    }
+}
+
 // fold (or pass the stored coefficients through) and store into ring row a
 template <int K>
 __device__ __forceinline__ void put_raw(const SorArgs& A, const Raw<K>& r, float2* DV, float4* C4, float* C1, int a,
                                         float* coef, long long o, long long plane)
 {
-    float A12, BU, BV, iDu, iDv;
-    if (A.mode < 0) {
-        A12 = r.j[0];
-        BU = r.j[1];
-        BV = r.j[2];
-        iDu = r.j[3];
-        iDv = r.j[4];
-    } else {
-        const bool tick = (A.mode & 2) != 0;
-        float A11 = 0.f, A22 = 0.f, a12 = 0.f, C13 = 0.f, C23 = 0.f;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const float j11 = r.j[0 * K + k], j22 = r.j[1 * K + k], j33 = r.j[2 * K + k];
-            const float j12 = r.j[3 * K + k], j13 = r.j[4 * K + k], j23 = r.j[5 * K + k];
-            float psi = 1.0f;
-            if (tick) {
-                const float a = r.du, b = r.dv;
-                float E = j11 * a * a + j22 * b * b + j23 * b + 2.0f * j12 * a * b + 2.0f * j13 * a + j23 * b + j33;
-                E = fmaxf(E, 0.0f);
-                // (E + eps)^(a_k - 1) as exp2((a_k - 1) log2(E + eps)) on the special-function
-                // unit: relative error ~1e-6, the fp32 path's rounding level
-                psi = A.a_data[k] * exp2f((A.a_data[k] - 1.0f) * __log2f(E + 1e-5f));
-            }
-            const float wp = r.w[k] * psi;
-            A11 = fmaf(wp, j11, A11);
-            A22 = fmaf(wp, j22, A22);
-            a12 = fmaf(wp, j12, a12);
-            C13 = fmaf(wp, j13, C13);
-            C23 = fmaf(wp, j23, C23);
-        }
-        const float den_u = A.wsum + A11, den_v = A.wsum + A22;
-        A12 = a12;
-        BU = r.lu - C13;
-        BV = r.lv - C23;
-        iDu = den_u != 0.0f ? __frcp_rn(den_u) : 0.0f;
-        iDv = den_v != 0.0f ? __frcp_rn(den_v) : 0.0f;
-        if (A.store_coef) {
-            coef[o] = A12;
-            coef[plane + o] = BU;
-            coef[2 * plane + o] = BV;
-            coef[3 * plane + o] = iDu;
-            coef[4 * plane + o] = iDv;
-        }
-    }
+    const Coef c = fold<K>(A, r);
+    store_coef(A, c, coef, o, plane);
     DV[a] = make_float2(r.du, r.dv);
-    C4[a] = make_float4(A12, BU, BV, iDu);
-    C1[a] = iDv;
+    C4[a] = make_float4(c.A12, c.BU, c.BV, c.iDu);
+    C1[a] = c.iDv;
+}
+
+// One SOR update of a pixel (core/level_solver.py:309-364 with a_smooth = 1):
+// c its (du, dv) before the update; up/dn the row above (new) and below (old),
+// lf/rt the column left (new) and right (old), Neumann copies already applied;
+// wa weights the row neighbours, wb the column neighbours.  du first, then dv
+// from the new du.
+__device__ __forceinline__ float2 sor_point(float2 c, float2 up, float2 dn, float2 lf, float2 rt, float4 c4, float iDv,
+                                            float wa, float wb, float omega, float one_m_omega)
+{
+    float nu = __fmaf_rn(wa, __fadd_rn(up.x, dn.x), __fmul_rn(wb, __fadd_rn(lf.x, rt.x)));
+    nu = __fadd_rn(nu, c4.y);
+    nu = __fmaf_rn(-c4.x, c.y, nu);
+    const float dun = __fmaf_rn(one_m_omega, c.x, __fmul_rn(omega, __fmul_rn(nu, c4.w)));
+    float nv = __fmaf_rn(wa, __fadd_rn(up.y, dn.y), __fmul_rn(wb, __fadd_rn(lf.y, rt.y)));
+    nv = __fadd_rn(nv, c4.z);
+    nv = __fmaf_rn(-c4.x, dun, nv);
+    const float dvn = __fmaf_rn(one_m_omega, c.y, __fmul_rn(omega, __fmul_rn(nv, iDv)));
+    return make_float2(dun, dvn);
 }
 
 template <int K, int PF, int MAXT>
@@ -259,11 +307,7 @@ __global__ void __launch_bounds__(MAXT) k_sor_fused(SorArgs A)
                     const float2 bm = b > 0 ? DVm[a] : c;
                     const float2 ap = a < Hh - 1 ? DVp[a + 1] : c;
                     const float2 bp = b < Bw - 1 ? DVp[a] : c;
-                    const float nu = wa * (am.x + ap.x) + wb * (bm.x + bp.x) + c4.y - c4.x * c.y;
-                    const float dun = one_m_omega * c.x + omega * (nu * c4.w);
-                    const float nv = wa * (am.y + ap.y) + wb * (bm.y + bp.y) + c4.z - c4.x * dun;
-                    const float dvn = one_m_omega * c.y + omega * (nv * iDv);
-                    DVc[a] = make_float2(dun, dvn);
+                    DVc[a] = sor_point(c, am, ap, bm, bp, c4, iDv, wa, wb, omega, one_m_omega);
                 }
                 if (++slot_s == R) slot_s = 0;
             }
@@ -271,6 +315,160 @@ __global__ void __launch_bounds__(MAXT) k_sor_fused(SorArgs A)
         }
     }
     for (int e = nsteps - 2 * G > 0 ? nsteps - 2 * G : 0; e < D; ++e) writeback(e, e % R);
+}
+
+// ---------------------------------------------------------------------------
+// The same exact-order SOR pass with one thread per row and the state in
+// registers.  Thread r updates, at step s, pixel (r, s - r - 2 gi) of every
+// pipelined iteration gi (the schedule above).  Every neighbour the update
+// reads was produced one step earlier, so it travels without shared memory:
+//   left  (r, c - 1), iteration gi      this thread, step s - 1, iteration gi
+//   right (r, c + 1), iteration gi - 1  this thread, step s - 1, iteration gi - 1
+//   own   (r, c),     iteration gi - 1  this thread, step s - 2, iteration gi - 1
+//   up    (r - 1, c), iteration gi      thread r - 1, step s - 1, iteration gi (shfl_up)
+//   down  (r + 1, c), iteration gi - 1  thread r + 1, step s - 1, iteration gi - 1 (shfl_down)
+// Iteration gi = 0 reads the pass-start state in place of "iteration -1":
+// the thread's own pixels on diagonals s and s + 1 and row r + 1's pixel on
+// diagonal s + 1, all loaded two steps ahead with the raw fold inputs of the
+// entering pixel (r, s - r).  Lanes 0 and 31 take the cross-warp neighbours
+// from a two-parity exchange buffer written in the previous step; one
+// __syncthreads per step.  A pixel's coefficients, folded when it enters, stay
+// in a per-thread ring of 2G - 1 shared-memory slots until its last update.
+// Shared memory: C4 float4[S][NT] | C1 float[S][NT] | X float2[2][NW][2][G].
+// ---------------------------------------------------------------------------
+template <int K>
+struct Pre {
+    Raw<K> raw;   // pixel (r, d - r)
+    float nu, nv; // pass-start du, dv of pixel (r + 1, d - r - 1)
+};
+
+template <int K, int G>
+__global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
+{
+    extern __shared__ __align__(16) float sm[];
+    constexpr int S = 2 * G - 1;
+    const DiagGeom g = A.g;
+    const int P = g.P, D = g.D, h = g.h, w = g.w;
+    const int NT = blockDim.x, r = threadIdx.x, lane = r & 31, warp = r >> 5, NW = NT >> 5;
+    float4* C4 = reinterpret_cast<float4*>(sm);
+    float* C1 = sm + 4 * S * NT;
+    float2* X = reinterpret_cast<float2*>(C1 + S * NT);
+    const long long plane = (long long)D * P;
+    const int f = blockIdx.x;
+    const float* J = A.J + f * A.J_fs;
+    const float* W = A.W + f * A.W_fs;
+    const float* lap = A.lap + f * A.lap_fs;
+    float* coef = A.coef + f * A.coef_fs;
+    float* du = A.du + f * A.st_fs;
+    float* dv = A.dv + f * A.st_fs;
+    float* odu = A.out_du ? A.out_du + f * A.out_fs : nullptr;
+    float* odv = A.out_dv ? A.out_dv + f * A.out_fs : nullptr;
+    const float omega = A.omega, one_m_omega = 1.0f - omega, wa = A.wa, wb = A.wb;
+    const bool zero_start = A.mode >= 0 && (A.mode & 1);
+    const bool row_ok = r < h;
+    const bool has_below = r + 1 < h;
+
+    auto fetch = [&](int d, Pre<K>& p) {
+        const int c = d - r;
+        if (row_ok && c >= 0 && c < w) load_raw<K>(A, J, W, lap, coef, du, dv, (long long)d * P + r, plane, p.raw);
+        if (has_below && c >= 1 && c <= w) {
+            if (zero_start) {
+                p.nu = 0.0f;
+                p.nv = 0.0f;
+            } else {
+                p.nu = du[(long long)d * P + r + 1];
+                p.nv = dv[(long long)d * P + r + 1];
+            }
+        }
+    };
+    // exchange slot: parity, warp, direction (0: this warp's lane 31 for the warp below,
+    // 1: lane 0 for the warp above), iteration
+    auto xs = [&](int par, int wp, int dir, int gi) -> float2& { return X[((par * NW + wp) * 2 + dir) * G + gi]; };
+
+    Pre<K> pre[2];
+    fetch(0, pre[0]);
+    fetch(1, pre[1]);
+    float2 V0[G], V1[G], V2[G];
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) V0[gi] = V1[gi] = V2[gi] = make_float2(0.0f, 0.0f);
+
+    const int nsteps = D + 2 * (G - 1);
+    int slot0 = 0;  // s % S
+    for (int s0 = 0; s0 < nsteps; s0 += 2) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int s = s0 + q;
+            if (s < nsteps) {
+                Pre<K>& cur = pre[q];       // diagonal s
+                Pre<K>& nxt = pre[q ^ 1];   // diagonal s + 1
+                const int c0 = s - r;
+                const float2 ps0 = make_float2(cur.raw.du, cur.raw.dv);
+                const float2 ps1 = make_float2(nxt.raw.du, nxt.raw.dv);
+                const float2 dn1 = make_float2(nxt.nu, nxt.nv);
+                if (row_ok && c0 >= 0 && c0 < w) {
+                    const Coef cf = fold<K>(A, cur.raw);
+                    store_coef(A, cf, coef, (long long)s * P + r, plane);
+                    C4[slot0 * NT + r] = make_float4(cf.A12, cf.BU, cf.BV, cf.iDu);
+                    C1[slot0 * NT + r] = cf.iDv;
+                }
+                fetch(s + 2, cur);
+                const int pin = (s + 1) & 1;  // parity written at step s - 1
+#pragma unroll
+                for (int gi = 0; gi < G; ++gi) {
+                    float2 up, dn;
+                    up.x = __shfl_up_sync(0xffffffffu, V1[gi].x, 1);
+                    up.y = __shfl_up_sync(0xffffffffu, V1[gi].y, 1);
+                    if (lane == 0 && warp > 0) up = xs(pin, warp - 1, 0, gi);
+                    if (gi == 0) {
+                        dn = dn1;
+                    } else {
+                        dn.x = __shfl_down_sync(0xffffffffu, V1[gi - 1].x, 1);
+                        dn.y = __shfl_down_sync(0xffffffffu, V1[gi - 1].y, 1);
+                        if (lane == 31 && warp < NW - 1) dn = xs(pin, warp + 1, 1, gi - 1);
+                    }
+                    const int c = c0 - 2 * gi;
+                    if (row_ok && c >= 0 && c < w) {
+                        const float2 own = gi == 0 ? ps0 : V2[gi - 1];
+                        const float2 lf = c > 0 ? V1[gi] : own;
+                        const float2 rt = c < w - 1 ? (gi == 0 ? ps1 : V1[gi - 1]) : own;
+                        const float2 u_ = r > 0 ? up : own;
+                        const float2 d_ = r < h - 1 ? dn : own;
+                        int sl = slot0 - 2 * gi;
+                        if (sl < 0) sl += S;
+                        V0[gi] = sor_point(own, u_, d_, lf, rt, C4[sl * NT + r], C1[sl * NT + r], wa, wb, omega,
+                                           one_m_omega);
+                        if (gi == G - 1) {
+                            if (odu) {
+                                const long long o = (long long)r * w + c;
+                                odu[o] = V0[gi].x;
+                                odv[o] = V0[gi].y;
+                            } else {
+                                const long long o = (long long)(r + c) * P + r;
+                                du[o] = V0[gi].x;
+                                dv[o] = V0[gi].y;
+                            }
+                        }
+                    }
+                }
+                const int pout = s & 1;
+                if (lane == 31) {
+#pragma unroll
+                    for (int gi = 0; gi < G; ++gi) xs(pout, warp, 0, gi) = V0[gi];
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int gi = 0; gi + 1 < G; ++gi) xs(pout, warp, 1, gi) = V0[gi];
+                }
+#pragma unroll
+                for (int gi = 0; gi < G; ++gi) {
+                    V2[gi] = V1[gi];
+                    V1[gi] = V0[gi];
+                }
+                if (++slot0 == S) slot0 = 0;
+            }
+            __syncthreads();
+        }
+    }
 }
 
 constexpr int kSmemLimit = 232448;  // 227 KB of dynamic shared memory per CTA
@@ -310,6 +508,94 @@ int sor_fused_gmax(int P)
     for (int G = kGMax; G >= 1; --G)
         if ((size_t)(2 * G + 3) * 7 * P * sizeof(float) <= (size_t)kSmemLimit) return G;
     return 0;
+}
+
+size_t sor_regs_smem(int G, int threads)
+{
+    return (size_t)(2 * G - 1) * 5 * threads * sizeof(float) + (size_t)2 * (threads / 32) * 2 * G * sizeof(float2);
+}
+
+bool sor_regs_supports(int K, const DiagGeom& g) { return K >= 1 && K <= 4 && g.P <= kMaxLane && (g.P & 31) == 0; }
+
+namespace {
+
+template <int K, int G>
+cudaError_t run_regs_t(const SorArgs& A, int n_frames, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmemLimit);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int threads = A.g.P;
+    k_sor_regs<K, G><<<n_frames, threads, sor_regs_smem(G, threads), st>>>(A);
+    return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t run_regs(const SorArgs& A, int n_frames, cudaStream_t st)
+{
+    switch (A.G) {
+        case 1: return run_regs_t<K, 1>(A, n_frames, st);
+        case 2: return run_regs_t<K, 2>(A, n_frames, st);
+        case 3: return run_regs_t<K, 3>(A, n_frames, st);
+        case 4: return run_regs_t<K, 4>(A, n_frames, st);
+        default: return run_regs_t<K, 5>(A, n_frames, st);
+    }
+}
+
+SorArgs make_args(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap, long long lap_fs,
+                  float* coef, long long coef_fs, float* du, float* dv, long long st_fs, int K, DiagGeom g, int G,
+                  int mode, int store_coef, const float* a_data, float wx, float wy, float omega, float* out_du,
+                  float* out_dv, long long out_fs)
+{
+    SorArgs A;
+    A.J = J;
+    A.J_fs = J_fs;
+    A.W = W;
+    A.W_fs = W_fs;
+    A.lap = lap;
+    A.lap_fs = lap_fs;
+    A.coef = coef;
+    A.coef_fs = coef_fs;
+    A.du = du;
+    A.dv = dv;
+    A.st_fs = st_fs;
+    A.out_du = out_du;
+    A.out_dv = out_dv;
+    A.out_fs = out_fs;
+    A.g = g;
+    A.G = G;
+    A.mode = mode;
+    A.store_coef = store_coef;
+    A.wa = wy;  // the lane index runs along rows: row neighbours carry the y weight
+    A.wb = wx;
+    A.wsum = ((wx + wx) + wy) + wy;
+    A.omega = omega;
+    for (int k = 0; k < kMaxK; ++k) A.a_data[k] = k < K ? a_data[k] : 0.0f;
+    return A;
+}
+
+}  // namespace
+
+cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
+                            long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                            int n_frames, int K, DiagGeom g, int G, int mode, int store_coef, const float* a_data,
+                            float wx, float wy, float omega, cudaStream_t st, float* out_du, float* out_dv,
+                            long long out_fs)
+{
+    if (G < 1 || G > kGMax || !sor_regs_supports(K, g) || sor_regs_smem(G, g.P) > (size_t)kSmemLimit)
+        return cudaErrorInvalidValue;
+    const SorArgs A = make_args(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, K, g, G, mode,
+                                store_coef, a_data, wx, wy, omega, out_du, out_dv, out_fs);
+    switch (K) {
+        case 1: return run_regs<1>(A, n_frames, st);
+        case 2: return run_regs<2>(A, n_frames, st);
+        case 3: return run_regs<3>(A, n_frames, st);
+        default: return run_regs<4>(A, n_frames, st);
+    }
 }
 
 cudaError_t launch_sor_fused(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,

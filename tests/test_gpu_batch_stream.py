@@ -93,7 +93,30 @@ def test_autotuned_plan_gives_identical_flows():
     assert chosen
     tuned = plan.displacement(fr)
     assert torch.equal(base, tuned)
-    for i, (g, t, ms) in chosen.items():
+    for i, (v, g, t, ms) in chosen.items():
+        plan.set_level_variant(i, 0)
         plan.set_level_tuning(i, max(1, g - 1), 1024)
     assert torch.equal(base, plan.displacement(fr))
+    plan.close()
+
+
+@pytest.mark.parametrize("key,frames", [((200, 168, 2), 3), ((96, 130, 1), 2), ((150, 90, 3), 2),
+                                        ((70, 64, 4), 2), ((600, 96, 2), 2)])
+def test_sor_variants_give_identical_flows(key, frames):
+    """The rows-in-registers SOR and the diagonal-ring SOR give the same bits
+    on every level either serves, for every pass length."""
+    from pyflowreg_gb300 import api
+
+    ref, fr = _frames(key, frames, 7)
+    plan = api.Plan(api.make_params(K=key[2], **OPTS), *key, frames)
+    plan.set_reference(ref)
+    base = plan.displacement(fr).clone()
+    tun = plan.level_tuning()
+    served = [i for i in range(len(tun)) if plan.level_variant(i)[1] > 1]
+    assert served
+    for G in (5, 3, 1):
+        for i in served:
+            plan.set_level_variant(i, 1)
+            plan.set_level_tuning(i, min(G, tun[i][2]), 0)
+        assert torch.equal(base, plan.displacement(fr)), G
     plan.close()
