@@ -529,7 +529,8 @@ def run_gb300(args):
     per_launch_bytes = sor_bytes / max(sor_n, 1)
     ratio = profiled_traffic()
     roofline = {
-        "kernel": "k_sor_fused (exact-order wavefront SOR, fold in the loader)",
+        "kernel": "k_sor_regs (exact-order wavefront SOR, one thread per row, state in registers, fold in "
+                  "the loader; k_sor_fused on levels it does not serve)",
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
@@ -541,7 +542,7 @@ def run_gb300(args):
         "launches": sor_n,
         "share_of_step": (sor_ms / ms) if ms > 0 else None,
         "note": "achieved = 36 B per interior pixel per pipelined SOR iteration (streaming model) / "
-                "CUDA-event time of the SOR launches; the kernel keeps G iterations in shared memory, so "
+                "CUDA-event time of the SOR launches; the kernel keeps G iterations on chip, so "
                 "frac can exceed 1; traffic = measured DRAM/model ratio (profiles/dram_traffic.txt) x model "
                 "bytes per launch",
     }

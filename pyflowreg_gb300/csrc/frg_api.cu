@@ -272,6 +272,7 @@ struct LevelPlan {
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
     int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
     int sor_variant = 0;  // fused SOR kernel: 0 diagonal ring in shared memory, 1 rows with the state in registers
+                          // (the default where it serves)
 };
 
 // Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
@@ -628,6 +629,8 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         L.wx = (float)(L.alpha_x / (L.h_col * L.h_col));
         L.wy = (float)(L.alpha_y / (L.h_row * L.h_row));
         L.g = make_geom(L.h, L.w);
+        // the rows-in-registers SOR is the faster kernel wherever it serves (same bits either way)
+        L.sor_variant = (sor_kind(channels, L.g) == kSorFused && sor_regs_supports(channels, L.g)) ? 1 : 0;
         const double sig = resize_sigma(m, n, L.h, L.w);
         HostTables tx = make_tables(n, L.w, sig), ty = make_tables(m, L.h, sig);
         if ((rc = upload_tables(pl, tx, L.w, ty, L.h, &L.img))) { frg_plan_destroy(pl); return rc; }
@@ -1249,7 +1252,7 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
                                 0, g, st));
         FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
         int r = solve_level(iterations, update_lag, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy,
-                            (float)omega, st);
+                            (float)omega, st, nullptr, nullptr, nullptr, 0, 0, 0, sor_regs_supports(K, g) ? 1 : 0);
         if (r) return r;
         FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
         FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
@@ -1386,6 +1389,7 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
     // the passes of make_passes, generated in place (no host container), run
     // with the same kernels as solve_level uses for frg_level_solve
     const bool fused = sor_fused_supports(K);
+    const bool regs = sor_regs_supports(K, g);
     for (int t = 0; t < iterations;) {
         const bool tick = ((t + 1) % update_lag) == 0;
         int end = t + 1;
@@ -1394,7 +1398,11 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
         for (int s = t; s < end; s += kGMax) {
             const int G = std::min(kGMax, end - s);
             const int pass_mode = s == t ? mode : -1;
-            if (fused) {
+            if (regs) {
+                const int store = (s == t && s + kGMax < end) ? 1 : 0;
+                FRG_LAUNCH(launch_sor_regs(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode, store, ad,
+                                           wx, wy, (float)omega, st));
+            } else if (fused) {
                 const int store = (s == t && s + kGMax < end) ? 1 : 0;
                 FRG_LAUNCH(launch_sor_fused(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode, store,
                                             ad, wx, wy, (float)omega, st));

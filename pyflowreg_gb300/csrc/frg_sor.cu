@@ -115,14 +115,14 @@ __device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
         float psi = 1.0f;
         if (tick) {
             const float a = r.du, b = r.dv;
-            // E in the reference's order: J11 a a + J22 b b + J23 b + 2 J12 a b + 2 J13 a + J23 b + J33
-            float E = __fmul_rn(__fmul_rn(j11, a), a);
-            E = __fadd_rn(E, __fmul_rn(__fmul_rn(j22, b), b));
-            E = __fadd_rn(E, __fmul_rn(j23, b));
-            E = __fadd_rn(E, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, j12), a), b));
-            E = __fadd_rn(E, __fmul_rn(__fmul_rn(2.0f, j13), a));
-            E = __fadd_rn(E, __fmul_rn(j23, b));
-            E = __fadd_rn(E, j33);
+            // E = J11 a a + J22 b b + 2 J23 b + 2 J12 a b + 2 J13 a + J33 (the reference adds J23 b
+            // twice) as a chain of fused multiply-adds: E cancels to near zero where the
+            // linearisation fits, and each fused step rounds once
+            float E = __fmaf_rn(__fmul_rn(2.0f, j13), a, j33);
+            E = __fmaf_rn(__fmul_rn(2.0f, j23), b, E);
+            E = __fmaf_rn(__fmul_rn(__fmul_rn(2.0f, j12), a), b, E);
+            E = __fmaf_rn(__fmul_rn(j22, b), b, E);
+            E = __fmaf_rn(__fmul_rn(j11, a), a, E);
             E = fmaxf(E, 0.0f);
             // (E + eps)^(a_k - 1) as exp2((a_k - 1) log2(E + eps)) on the special-function
             // unit: relative error ~1e-6, the fp32 path's rounding level
