@@ -66,7 +66,9 @@ __global__ void k_resize_v(const float* __restrict__ src, int n_planes, int ih, 
 // Horizontal pass, shared-memory form: one block takes `rows` input rows of
 // one frame (all planes), stages them and the level's tap table in shared
 // memory, and each thread produces one (plane, output column) for all the
-// block's rows, so each table entry is read once per `rows` outputs.
+// block's rows, so each table entry is read once per `rows` outputs.  The
+// table is staged tap-major ([P][ow]) so that neighbouring threads (columns)
+// read neighbouring words.
 __global__ void k_resize_h_smem(View src, int n_planes, int ih, int iw, float* __restrict__ dst, int ow,
                                 const int32_t* __restrict__ ix, const float* __restrict__ wx, int P, int rows)
 {
@@ -79,8 +81,9 @@ __global__ void k_resize_h_smem(View src, int n_planes, int ih, int iw, float* _
     const int nr = min(rows, ih - y0);
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int i = tid; i < ow * P; i += nth) {
-        tix[i] = ix[i];
-        twx[i] = wx[i];
+        const int x = i / P, p = i - x * P;
+        tix[p * ow + x] = ix[i];
+        twx[p * ow + x] = wx[i];
     }
     const float* base = src.p + f * src.fs;
     const int row_elems = n_planes * iw;
@@ -104,8 +107,8 @@ __global__ void k_resize_h_smem(View src, int n_planes, int ih, int iw, float* _
 #pragma unroll
         for (int r = 0; r < 8; ++r) acc[r] = 0.0f;
         for (int p = 0; p < P; ++p) {
-            const int j = tix[x * P + p];
-            const float wgt = twx[x * P + p];
+            const int j = tix[p * ow + x];
+            const float wgt = twx[p * ow + x];
 #pragma unroll
             for (int r = 0; r < 8; ++r)
                 if (r < nr) acc[r] = fmaf(srow[((size_t)r * n_planes + pl) * iw + j], wgt, acc[r]);
@@ -296,17 +299,20 @@ __global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float 
 // Tiled form: a 32 x 32 pixel tile is computed into shared memory, then every
 // diagonal crossing the tile is written as one contiguous run of the
 // diagonal-major layout (up to 128 bytes per warp store instead of 32
-// scattered 4-byte stores).
+// scattered 4-byte stores).  Row pitch 34: the row writes (lane = column) and
+// the anti-diagonal reads (lane = row, column falling, word step 33) both hit
+// 32 different banks.
 constexpr int kTensTile = 32;
+constexpr int kTensLd = kTensTile + 2;
 
 __global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, int h, int w, float hy, float hx,
                                                       int gray, float* __restrict__ J, long long J_fs, DiagGeom g)
 {
-    extern __shared__ float tile[];  // [6K][32][33]
+    extern __shared__ float tile[];  // [6K][32][34]
     const int f = blockIdx.z;
     const int r0 = blockIdx.y * kTensTile, c0 = blockIdx.x * kTensTile;
     const int tx = threadIdx.x & 31, tw = threadIdx.x >> 5;  // 8 warps
-    const int ld = kTensTile + 1;
+    const int ld = kTensLd;
     for (int rr = tw; rr < kTensTile; rr += 8) {
         const int y = r0 + rr, x = c0 + tx;
         if (y < h && x < w) {
@@ -337,7 +343,7 @@ __global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, i
 cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
                           int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st)
 {
-    const size_t smem = (size_t)6 * K * kTensTile * (kTensTile + 1) * sizeof(float);
+    const size_t smem = (size_t)6 * K * kTensTile * kTensLd * sizeof(float);
     if (smem <= 200 * 1024) {
         static bool attr = false;
         if (!attr) {
