@@ -325,8 +325,6 @@ struct frg_plan {
     bool has_ref = false;
     // per-batch workspace
     float* tmp = nullptr;     // horizontal resize pass
-    float* pyr_tmp = nullptr; // horizontal pass of every level at once, level l at pyr.off[l] (fp32 path)
-    PyrTabs pyr;
     float* f2 = nullptr;      // (T, K, h, w)
     float* warped = nullptr;  // (T, K, h, w)
     float* J = nullptr;       // (T, 6, K, D*P)
@@ -716,28 +714,6 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             frg_plan_destroy(pl);
             return rc;
         }
-        // horizontal resize of every level in one pass over the moving frames
-        if (pl->levels.size() <= (size_t)kMaxPyr) {
-            PyrTabs& t = pl->pyr;
-            t.n = (int)pl->levels.size();
-            long long off = 0;
-            for (int l = 0; l < t.n; ++l) {
-                const LevelPlan& L = pl->levels[l];
-                t.ow[l] = L.w;
-                t.P[l] = L.img.P;
-                t.ix[l] = L.img.ix;
-                t.wx[l] = L.img.wx;
-                t.off[l] = off;
-                t.max_entries = std::max(t.max_entries, L.w * L.img.P);
-                off += (long long)T * K * height * L.w;
-            }
-            if (resize_h_levels_smem(1, channels, width, t) <= (size_t)kPyrSmem) {
-                if ((rc = dev_alloc(pl, &pl->pyr_tmp, (size_t)off))) {
-                    frg_plan_destroy(pl);
-                    return rc;
-                }
-            }
-        }
     }
     {
         std::vector<float> ones(K * (size_t)height * width, 1.0f / (float)channels);
@@ -952,19 +928,10 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         const int h = L.h, w = L.w;
         const long long hw = (long long)h * w, pad = (long long)(h + 2) * (w + 2);
         const long long dp = (long long)L.g.D * L.g.P;
-        // 1. moving level images from full resolution (core/optical_flow.py:520); the
-        // horizontal pass of every level ran once before the level loop when the plan has room
-        const float* hsrc = pl->tmp;
-        if (pl->pyr_tmp) {
-            if (li == 0)
-                FRG_LAUNCH(launch_resize_h_levels(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->pyr_tmp,
-                                                  pl->pyr, st));
-            hsrc = pl->pyr_tmp + pl->pyr.off[li];
-        } else {
-            FRG_LAUNCH(launch_resize_h(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->tmp, w, L.img.ix,
-                                       L.img.wx, L.img.P, st));
-        }
-        FRG_LAUNCH(launch_resize_v(hsrc, T, K, H, w, vieww(pl->f2, K * hw, hw, w, 1), h, 0, L.img.iy, L.img.wy,
+        // 1. moving level images from full resolution (core/optical_flow.py:520)
+        FRG_LAUNCH(launch_resize_h(view(moving, fsz, 1, (long long)W * K, K), T, K, H, W, pl->tmp, w, L.img.ix,
+                                 L.img.wx, L.img.P, st));
+        FRG_LAUNCH(launch_resize_v(pl->tmp, T, K, H, w, vieww(pl->f2, K * hw, hw, w, 1), h, 0, L.img.iy, L.img.wy,
                                  L.img.P, st));
         // 2. flow at this level with an edge ring (core/optical_flow.py:530-536)
         long long uv_fs;

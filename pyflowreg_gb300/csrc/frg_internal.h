@@ -43,23 +43,6 @@ __host__ __device__ inline long long diag_index(const DiagGeom& g, int r, int c)
 // launch status; none synchronises.
 cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
                             const int32_t* ix, const float* wx, int P, cudaStream_t st);
-// Horizontal resize pass of every pyramid level in one launch (k_resize_h_levels):
-// level l writes (n_frames, n_planes, ih, ow[l]) at dst + off[l], bit-identical
-// to launch_resize_h's output for that level.
-constexpr int kMaxPyr = 40;
-constexpr int kPyrSmem = 200 * 1024;
-struct PyrTabs {
-    int n = 0;
-    int max_entries = 0;  // largest ow[l] * P[l]
-    int ow[kMaxPyr];
-    int P[kMaxPyr];
-    const int32_t* ix[kMaxPyr];
-    const float* wx[kMaxPyr];
-    long long off[kMaxPyr];
-};
-size_t resize_h_levels_smem(int rows, int n_planes, int iw, const PyrTabs& t);
-cudaError_t launch_resize_h_levels(View src, int n_frames, int n_planes, int ih, int iw, float* dst,
-                                   const PyrTabs& t, cudaStream_t st);
 cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih, int ow, ViewW dst,
                             int oh, int pad, const int32_t* iy, const float* wy, int P, cudaStream_t st);
 cudaError_t launch_warp(View f2, View f1, View u, View v, int n_frames, int K, int h, int w,

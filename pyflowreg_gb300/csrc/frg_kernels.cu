@@ -140,89 +140,6 @@ cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw
     return cudaGetLastError();
 }
 
-// Horizontal pass of every pyramid level in one launch: a block stages `rows`
-// input rows of one frame (all planes) once, then, level by level, stages that
-// level's tap table (tap-major) and writes the level's output columns.  The
-// input is read once per call instead of once per level; each output sample
-// is accumulated exactly as k_resize_h_smem accumulates it.
-__global__ void k_resize_h_levels(View src, int n_planes, int ih, int iw, float* __restrict__ dst,
-                                  const __grid_constant__ PyrTabs T, int rows, int n_frames)
-{
-    extern __shared__ float sh[];
-    float* srow = sh;                                             // [rows][n_planes][iw]
-    int32_t* tix = reinterpret_cast<int32_t*>(sh + (size_t)rows * n_planes * iw);
-    float* twx = reinterpret_cast<float*>(tix + T.max_entries);   // [P][ow] per level
-    const int f = blockIdx.y;
-    const int y0 = blockIdx.x * rows;
-    const int nr = min(rows, ih - y0);
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const float* base = src.p + f * src.fs;
-    const int row_elems = n_planes * iw;
-    for (int i = tid; i < nr * row_elems; i += nth) {
-        const int r = i / row_elems, rem = i - r * row_elems;
-        int pl, x;
-        if (src.cs == 1) {
-            pl = rem / iw;
-            x = rem - pl * iw;
-        } else {
-            x = rem / n_planes;
-            pl = rem - x * n_planes;
-        }
-        srow[((size_t)r * n_planes + pl) * iw + x] =
-            base[pl * src.ps + (long long)(y0 + r) * src.rs + (long long)x * src.cs];
-    }
-    for (int l = 0; l < T.n; ++l) {
-        const int ow = T.ow[l], P = T.P[l];
-        __syncthreads();  // previous level's table no longer read (and, at l = 0, rows staged)
-        for (int i = tid; i < ow * P; i += nth) {
-            const int x = i / P, p = i - x * P;
-            tix[p * ow + x] = T.ix[l][i];
-            twx[p * ow + x] = T.wx[l][i];
-        }
-        __syncthreads();
-        float* out = dst + T.off[l];
-        for (int item = tid; item < n_planes * ow; item += nth) {
-            const int pl = item / ow, x = item - pl * ow;
-            float acc[8];
-#pragma unroll
-            for (int r = 0; r < 8; ++r) acc[r] = 0.0f;
-            for (int p = 0; p < P; ++p) {
-                const int j = tix[p * ow + x];
-                const float wgt = twx[p * ow + x];
-#pragma unroll
-                for (int r = 0; r < 8; ++r)
-                    if (r < nr) acc[r] = fmaf(srow[((size_t)r * n_planes + pl) * iw + j], wgt, acc[r]);
-            }
-            for (int r = 0; r < nr; ++r) out[(((long long)f * n_planes + pl) * ih + y0 + r) * ow + x] = acc[r];
-        }
-    }
-    (void)n_frames;
-}
-
-size_t resize_h_levels_smem(int rows, int n_planes, int iw, const PyrTabs& t)
-{
-    return (size_t)rows * n_planes * iw * sizeof(float) + (size_t)t.max_entries * 8;
-}
-
-cudaError_t launch_resize_h_levels(View src, int n_frames, int n_planes, int ih, int iw, float* dst,
-                                   const PyrTabs& t, cudaStream_t st)
-{
-    int rows = 8;
-    while (rows > 1 && resize_h_levels_smem(rows, n_planes, iw, t) > (size_t)kPyrSmem) rows /= 2;
-    if (resize_h_levels_smem(rows, n_planes, iw, t) > (size_t)kPyrSmem || n_frames > 65535 || t.n < 1)
-        return cudaErrorInvalidValue;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_resize_h_levels, cudaFuncAttributeMaxDynamicSharedMemorySize, kPyrSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
-    dim3 grd((ih + rows - 1) / rows, n_frames);
-    k_resize_h_levels<<<grd, 256, resize_h_levels_smem(rows, n_planes, iw, t), st>>>(src, n_planes, ih, iw, dst, t,
-                                                                                    rows, n_frames);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih, int ow, ViewW dst,
                             int oh, int pad, const int32_t* iy, const float* wy, int P, cudaStream_t st)
 {
