@@ -651,8 +651,9 @@ def cpu_baseline(args, ref, frames, gpu_out):
               "fp64_reference_order": diff(f64.cpu().numpy()),
               "fp32_fast_path": diff(gpu_out[:n].cpu().numpy().astype(np.float64)),
               "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4},
-              "note": "fp32 deviation is bounded by the reference's own rounding amplification "
-                      "(oracle vs itself under 1e-7 input perturbation), see DESIGN.md"}
+              "note": "the fp64 reference-order mode is the parity mode; the fp32 deviation is bounded by "
+                      "the reference's own rounding amplification (the oracle moves by ~0.1 px under a 1e-7 "
+                      "relative input perturbation)"}
     cpu = {"value": n / dt, "unit": "frames/s", "cores": cores, "kind": "port",
            "sample": f"{n} frames of the same batch, one frame per thread (OpenMP), fp64 lexicographic oracle"}
     return cpu, parity

@@ -5,7 +5,7 @@ typing): max |delta flow| <= 1e-3 px and mean endpoint error <= 1e-4 px.
 
 The fp32 fast path cannot meet that bar against any fp64 run, because the
 reference algorithm amplifies rounding: perturbing the input by one float32
-ulp moves the oracle's own output by ~0.1 px (DESIGN.md section 2).  Its test
+ulp moves the oracle's own output by ~0.1 px.  Its test
 therefore measures that envelope on the same case -- the oracle re-run on
 inputs perturbed at the float32 rounding level -- and requires the fp32
 deviation to stay within twice it, and its accuracy against the known
