@@ -449,14 +449,14 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
                 int tune_G = 0, int tune_threads = 0, int tune_variant = 0)
 {
     const SorKind kind = sor_kind(K, g);
-    const bool fused = kind == kSorFused;
-    const bool regs = fused && tune_variant == 1 && sor_regs_supports(K, g);
-    int gmax = kind == kSorFused ? (regs ? kGMax : sor_fused_gmax(g.P)) : (kind == kSorRows ? kGMax : update_lag);
-    if (fused && tune_G > 0 && tune_G < gmax) gmax = tune_G;
+    const bool regs = tune_variant == 1 && sor_regs_supports(K, g);
+    const bool fused = kind == kSorFused && !regs;
+    int gmax = regs ? kGMax : (kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag));
+    if ((fused || regs) && tune_G > 0 && tune_G < gmax) gmax = tune_G;
     const std::vector<Pass> passes = make_passes(iterations, update_lag, gmax);
     for (size_t pi = 0; pi < passes.size(); ++pi) {
         const Pass& ps = passes[pi];
-        if (!fused && ps.fold_mode >= 0)
+        if (!fused && !regs && ps.fold_mode >= 0)
             FRG_LAUNCH(launch_fold(J, J_fs, W, W_fs, lap, lap_fs, du, dv, st_fs, coef, coef_fs, T, K, g,
                                    a_data, ps.fold_mode, wx, wy, st));
         const bool timed = prof && prof->on;
@@ -629,8 +629,9 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         L.wx = (float)(L.alpha_x / (L.h_col * L.h_col));
         L.wy = (float)(L.alpha_y / (L.h_row * L.h_row));
         L.g = make_geom(L.h, L.w);
-        // the rows-in-registers SOR is the faster kernel wherever it serves (same bits either way)
-        L.sor_variant = (sor_kind(channels, L.g) == kSorFused && sor_regs_supports(channels, L.g)) ? 1 : 0;
+        // the rows-in-registers SOR is the faster kernel wherever it serves (same bits as the
+        // diagonal ring; levels taller than 512 rows run it as a cluster of row strips)
+        L.sor_variant = sor_regs_supports(channels, L.g) ? 1 : 0;
         const double sig = resize_sigma(m, n, L.h, L.w);
         HostTables tx = make_tables(n, L.w, sig), ty = make_tables(m, L.h, sig);
         if ((rc = upload_tables(pl, tx, L.w, ty, L.h, &L.img))) { frg_plan_destroy(pl); return rc; }
@@ -846,9 +847,9 @@ int frg_plan_set_level_variant(frg_plan* plan, int level, int variant)
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     LevelPlan& L = plan->levels[level];
-    const bool fused = sor_kind(plan->K, L.g) == kSorFused;
-    if (variant < 0 || variant > 1) return fail(FRG_EINVAL, "variant must be 0 (diagonal ring) or 1 (rows in registers)");
-    if (variant == 1 && !(fused && sor_regs_supports(plan->K, L.g)))
+    if (variant < 0 || variant > 1)
+        return fail(FRG_EINVAL, "variant must be 0 (the level's ring / row / global kernel) or 1 (rows in registers)");
+    if (variant == 1 && !sor_regs_supports(plan->K, L.g))
         return fail(FRG_EINVAL, "the rows-in-registers SOR does not serve this level");
     L.sor_variant = variant;
     return FRG_OK;
@@ -858,9 +859,8 @@ int frg_plan_level_variant(const frg_plan* plan, int level, int* variant, int* n
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     const LevelPlan& L = plan->levels[level];
-    const bool fused = sor_kind(plan->K, L.g) == kSorFused;
     if (variant) *variant = L.sor_variant;
-    if (n_variants) *n_variants = fused ? (sor_regs_supports(plan->K, L.g) ? 2 : 1) : 0;
+    if (n_variants) *n_variants = sor_regs_supports(plan->K, L.g) ? 2 : 1;
     return FRG_OK;
 }
 
@@ -971,8 +971,9 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         FRG_LAUNCH(launch_tensor(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
                                pl->J, J_fs, L.g, st));
         FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
-        // 5. level solve (core/optical_flow.py:584-606)
-        const bool fused = sor_kind(K, L.g) == kSorFused;
+        // 5. level solve (core/optical_flow.py:584-606); the fused kernels write the last pass
+        // row-major for the median
+        const bool fused = sor_kind(K, L.g) == kSorFused || (L.sor_variant == 1 && sor_regs_supports(K, L.g));
         int rc = solve_level(pl->p.iterations, pl->p.update_lag, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du,
                              pl->dv, dp, pl->coef, 5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st,
                              &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw, L.sor_G, L.sor_threads,

@@ -18,6 +18,8 @@
 // handles a given row in the two operations.
 #include "frg_internal.h"
 
+#include <cooperative_groups.h>
+
 namespace frg {
 
 namespace {
@@ -45,6 +47,7 @@ struct SorArgs {
     float wsum;          // 2 wx + 2 wy, summed as the reference does
     float omega;
     float a_data[kMaxK];
+    int nc;              // k_sor_regs cluster form: CTAs (row strips) per frame
 };
 
 __device__ __forceinline__ int rmin_of(const DiagGeom& g, int d) { return d - (g.w - 1) > 0 ? d - (g.w - 1) : 0; }
@@ -334,7 +337,15 @@ __global__ void __launch_bounds__(MAXT) k_sor_fused(SorArgs A)
 // from a two-parity exchange buffer written in the previous step; one
 // __syncthreads per step.  A pixel's coefficients, folded when it enters, stay
 // in a per-thread ring of 2G - 1 shared-memory slots until its last update.
-// Shared memory: C4 float4[S][NT] | C1 float[S][NT] | X float2[2][NW][2][G].
+// Shared memory: C4 float4[S][NT] | C1 float[S][NT] | X float2[2][NW][2][G]
+// | XE float2[2][2][G].
+//
+// Cluster form (CL): levels taller than one CTA split their rows into nc
+// strips of NT rows, one CTA per strip, the nc CTAs of a frame forming a
+// thread-block cluster.  The strips' edge rows exchange their values through
+// distributed shared memory (each writes into the neighbouring CTA's XE) and a
+// cluster barrier replaces __syncthreads, so the strips advance step by step
+// as one wavefront.
 // ---------------------------------------------------------------------------
 template <int K>
 struct Pre {
@@ -342,19 +353,23 @@ struct Pre {
     float nu, nv; // pass-start du, dv of pixel (r + 1, d - r - 1)
 };
 
-template <int K, int G>
+template <int K, int G, bool CL>
 __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
 {
     extern __shared__ __align__(16) float sm[];
     constexpr int S = 2 * G - 1;
     const DiagGeom g = A.g;
     const int P = g.P, D = g.D, h = g.h, w = g.w;
-    const int NT = blockDim.x, r = threadIdx.x, lane = r & 31, warp = r >> 5, NW = NT >> 5;
+    const int NT = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, NW = NT >> 5;
+    const int nc = CL ? A.nc : 1;
+    const int strip = CL ? (int)(blockIdx.x % nc) : 0;
+    const int f = CL ? (int)(blockIdx.x / nc) : (int)blockIdx.x;
+    const int r = strip * NT + t;  // the level row of this thread
     float4* C4 = reinterpret_cast<float4*>(sm);
     float* C1 = sm + 4 * S * NT;
     float2* X = reinterpret_cast<float2*>(C1 + S * NT);
+    float2* XE = X + 2 * NW * 2 * G;  // [par][0: row above the strip, 1: row below][gi]
     const long long plane = (long long)D * P;
-    const int f = blockIdx.x;
     const float* J = A.J + f * A.J_fs;
     const float* W = A.W + f * A.W_fs;
     const float* lap = A.lap + f * A.lap_fs;
@@ -384,6 +399,13 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
     // exchange slot: parity, warp, direction (0: this warp's lane 31 for the warp below,
     // 1: lane 0 for the warp above), iteration
     auto xs = [&](int par, int wp, int dir, int gi) -> float2& { return X[((par * NW + wp) * 2 + dir) * G + gi]; };
+    auto step_barrier = [&]() {
+        if constexpr (CL)
+            cooperative_groups::this_cluster().sync();
+        else
+            __syncthreads();
+    };
+    if constexpr (CL) step_barrier();  // every CTA of the cluster is running before any remote write
 
     Pre<K> pre[2];
     fetch(0, pre[0]);
@@ -408,8 +430,8 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
                 if (row_ok && c0 >= 0 && c0 < w) {
                     const Coef cf = fold<K>(A, cur.raw);
                     store_coef(A, cf, coef, (long long)s * P + r, plane);
-                    C4[slot0 * NT + r] = make_float4(cf.A12, cf.BU, cf.BV, cf.iDu);
-                    C1[slot0 * NT + r] = cf.iDv;
+                    C4[slot0 * NT + t] = make_float4(cf.A12, cf.BU, cf.BV, cf.iDu);
+                    C1[slot0 * NT + t] = cf.iDv;
                 }
                 fetch(s + 2, cur);
                 const int pin = (s + 1) & 1;  // parity written at step s - 1
@@ -419,12 +441,14 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
                     up.x = __shfl_up_sync(0xffffffffu, V1[gi].x, 1);
                     up.y = __shfl_up_sync(0xffffffffu, V1[gi].y, 1);
                     if (lane == 0 && warp > 0) up = xs(pin, warp - 1, 0, gi);
+                    if (CL && t == 0 && strip > 0) up = XE[(pin * 2 + 0) * G + gi];
                     if (gi == 0) {
                         dn = dn1;
                     } else {
                         dn.x = __shfl_down_sync(0xffffffffu, V1[gi - 1].x, 1);
                         dn.y = __shfl_down_sync(0xffffffffu, V1[gi - 1].y, 1);
                         if (lane == 31 && warp < NW - 1) dn = xs(pin, warp + 1, 1, gi - 1);
+                        if (CL && t == NT - 1 && strip < nc - 1) dn = XE[(pin * 2 + 1) * G + gi - 1];
                     }
                     const int c = c0 - 2 * gi;
                     if (row_ok && c >= 0 && c < w) {
@@ -435,7 +459,7 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
                         const float2 d_ = r < h - 1 ? dn : own;
                         int sl = slot0 - 2 * gi;
                         if (sl < 0) sl += S;
-                        V0[gi] = sor_point(own, u_, d_, lf, rt, C4[sl * NT + r], C1[sl * NT + r], wa, wb, omega,
+                        V0[gi] = sor_point(own, u_, d_, lf, rt, C4[sl * NT + t], C1[sl * NT + t], wa, wb, omega,
                                            one_m_omega);
                         if (gi == G - 1) {
                             if (odu) {
@@ -459,6 +483,20 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
 #pragma unroll
                     for (int gi = 0; gi + 1 < G; ++gi) xs(pout, warp, 1, gi) = V0[gi];
                 }
+                if constexpr (CL) {
+                    // strip edges: the last row feeds the next strip's "up", the first row the
+                    // previous strip's "down", in the neighbouring CTA's shared memory
+                    if (t == NT - 1 && strip < nc - 1) {
+                        float2* dst = cooperative_groups::this_cluster().map_shared_rank(XE, strip + 1);
+#pragma unroll
+                        for (int gi = 0; gi < G; ++gi) dst[(pout * 2 + 0) * G + gi] = V0[gi];
+                    }
+                    if (t == 0 && strip > 0) {
+                        float2* dst = cooperative_groups::this_cluster().map_shared_rank(XE, strip - 1);
+#pragma unroll
+                        for (int gi = 0; gi + 1 < G; ++gi) dst[(pout * 2 + 1) * G + gi] = V0[gi];
+                    }
+                }
 #pragma unroll
                 for (int gi = 0; gi < G; ++gi) {
                     V2[gi] = V1[gi];
@@ -466,7 +504,7 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
                 }
                 if (++slot0 == S) slot0 = 0;
             }
-            __syncthreads();
+            step_barrier();
         }
     }
 }
@@ -512,37 +550,82 @@ int sor_fused_gmax(int P)
 
 size_t sor_regs_smem(int G, int threads)
 {
-    return (size_t)(2 * G - 1) * 5 * threads * sizeof(float) + (size_t)2 * (threads / 32) * 2 * G * sizeof(float2);
+    return (size_t)(2 * G - 1) * 5 * threads * sizeof(float) +
+           (size_t)(2 * (threads / 32) * 2 * G + 2 * 2 * G) * sizeof(float2);
 }
 
-bool sor_regs_supports(int K, const DiagGeom& g) { return K >= 1 && K <= 4 && g.P <= kMaxLane && (g.P & 31) == 0; }
+// Row strips of a level: one CTA when it has at most 512 rows, else a cluster of
+// nc <= 8 CTAs of NT rows each (K <= 2: the registers of the larger K leave no room).
+static void regs_split(int K, const DiagGeom& g, int* nc, int* nt)
+{
+    if (g.P <= kMaxLane) {
+        *nc = 1;
+        *nt = g.P;
+        return;
+    }
+    const int n = (g.P + kMaxLane - 1) / kMaxLane;
+    *nc = (K <= 2 && n <= 8) ? n : 0;
+    *nt = ((g.P + n - 1) / n + 31) / 32 * 32;
+}
+
+bool sor_regs_supports(int K, const DiagGeom& g)
+{
+    int nc, nt;
+    regs_split(K, g, &nc, &nt);
+    return K >= 1 && K <= 4 && (g.P & 31) == 0 && nc >= 1;
+}
 
 namespace {
 
 template <int K, int G>
-cudaError_t run_regs_t(const SorArgs& A, int n_frames, cudaStream_t st)
+cudaError_t run_regs_t(const SorArgs& A, int n_frames, int nt, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemLimit);
-        if (e != cudaSuccess) return e;
-        attr = true;
+    if (A.nc == 1) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 kSmemLimit);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        k_sor_regs<K, G, false><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A);
+        return cudaGetLastError();
     }
-    const int threads = A.g.P;
-    k_sor_regs<K, G><<<n_frames, threads, sor_regs_smem(G, threads), st>>>(A);
-    return cudaGetLastError();
+    if constexpr (K <= 2) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 kSmemLimit);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(n_frames * A.nc));
+        cfg.blockDim = dim3((unsigned)nt);
+        cfg.dynamicSmemBytes = sor_regs_smem(G, nt);
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)A.nc;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_sor_regs<K, G, true>, A);
+    } else {
+        return cudaErrorInvalidValue;
+    }
 }
 
 template <int K>
-cudaError_t run_regs(const SorArgs& A, int n_frames, cudaStream_t st)
+cudaError_t run_regs(const SorArgs& A, int n_frames, int nt, cudaStream_t st)
 {
     switch (A.G) {
-        case 1: return run_regs_t<K, 1>(A, n_frames, st);
-        case 2: return run_regs_t<K, 2>(A, n_frames, st);
-        case 3: return run_regs_t<K, 3>(A, n_frames, st);
-        case 4: return run_regs_t<K, 4>(A, n_frames, st);
-        default: return run_regs_t<K, 5>(A, n_frames, st);
+        case 1: return run_regs_t<K, 1>(A, n_frames, nt, st);
+        case 2: return run_regs_t<K, 2>(A, n_frames, nt, st);
+        case 3: return run_regs_t<K, 3>(A, n_frames, nt, st);
+        case 4: return run_regs_t<K, 4>(A, n_frames, nt, st);
+        default: return run_regs_t<K, 5>(A, n_frames, nt, st);
     }
 }
 
@@ -575,6 +658,7 @@ SorArgs make_args(const float* J, long long J_fs, const float* W, long long W_fs
     A.wsum = ((wx + wx) + wy) + wy;
     A.omega = omega;
     for (int k = 0; k < kMaxK; ++k) A.a_data[k] = k < K ? a_data[k] : 0.0f;
+    A.nc = 1;
     return A;
 }
 
@@ -586,15 +670,19 @@ cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long
                             float wx, float wy, float omega, cudaStream_t st, float* out_du, float* out_dv,
                             long long out_fs)
 {
-    if (G < 1 || G > kGMax || !sor_regs_supports(K, g) || sor_regs_smem(G, g.P) > (size_t)kSmemLimit)
+    int nc = 0, nt = 0;
+    regs_split(K, g, &nc, &nt);
+    if (G < 1 || G > kGMax || !sor_regs_supports(K, g) || sor_regs_smem(G, nt) > (size_t)kSmemLimit ||
+        (long long)n_frames * nc > 0x7fffffffLL)
         return cudaErrorInvalidValue;
-    const SorArgs A = make_args(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, K, g, G, mode,
-                                store_coef, a_data, wx, wy, omega, out_du, out_dv, out_fs);
+    SorArgs A = make_args(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, K, g, G, mode, store_coef,
+                          a_data, wx, wy, omega, out_du, out_dv, out_fs);
+    A.nc = nc;
     switch (K) {
-        case 1: return run_regs<1>(A, n_frames, st);
-        case 2: return run_regs<2>(A, n_frames, st);
-        case 3: return run_regs<3>(A, n_frames, st);
-        default: return run_regs<4>(A, n_frames, st);
+        case 1: return run_regs<1>(A, n_frames, nt, st);
+        case 2: return run_regs<2>(A, n_frames, nt, st);
+        case 3: return run_regs<3>(A, n_frames, nt, st);
+        default: return run_regs<4>(A, n_frames, nt, st);
     }
 }
 

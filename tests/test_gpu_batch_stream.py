@@ -101,22 +101,51 @@ def test_autotuned_plan_gives_identical_flows():
 
 
 @pytest.mark.parametrize("key,frames", [((200, 168, 2), 3), ((96, 130, 1), 2), ((150, 90, 3), 2),
-                                        ((70, 64, 4), 2), ((600, 96, 2), 2)])
+                                        ((70, 64, 4), 2), ((600, 96, 2), 2), ((900, 60, 1), 2)])
 def test_sor_variants_give_identical_flows(key, frames):
-    """The rows-in-registers SOR and the diagonal-ring SOR give the same bits
-    on every level either serves, for every pass length."""
+    """The rows-in-registers SOR (one CTA, or a cluster of row strips above 512
+    rows) and the diagonal-ring SOR give the same bits on every level both
+    serve, for every pass length."""
     from pyflowreg_gb300 import api
 
     ref, fr = _frames(key, frames, 7)
     plan = api.Plan(api.make_params(K=key[2], **OPTS), *key, frames)
     plan.set_reference(ref)
-    base = plan.displacement(fr).clone()
     tun = plan.level_tuning()
-    served = [i for i in range(len(tun)) if plan.level_variant(i)[1] > 1]
-    assert served
+    both = [i for i in range(len(tun)) if tun[i][2] > 0 and plan.level_variant(i)[1] > 1]
+    assert both
+    for i in both:
+        plan.set_level_variant(i, 0)
+    base = plan.displacement(fr).clone()
     for G in (5, 3, 1):
-        for i in served:
+        for i in both:
             plan.set_level_variant(i, 1)
             plan.set_level_tuning(i, min(G, tun[i][2]), 0)
         assert torch.equal(base, plan.displacement(fr)), G
     plan.close()
+
+
+@pytest.mark.parametrize("key", [(1100, 72, 1), (1060, 40, 2), (640, 200, 2)])
+def test_cluster_sor_on_tall_levels_matches_the_other_kernels(oracle, key):
+    """Levels over 512 rows run as clusters of row strips.  Over 1024 rows the
+    alternative is the global-memory wavefront with a separate fold, whose
+    rounding differs: the two stay within float32 rounding of each other, and
+    the cluster result within the fp32 bound of the fp64 oracle."""
+    from pyflowreg_gb300 import api
+
+    ref, fr = _frames(key, 1, 9)
+    opts = dict(OPTS, iterations=10)
+    plan = api.Plan(api.make_params(K=key[2], **opts), *key, 1)
+    plan.set_reference(ref)
+    tall = [i for i in range(len(plan.level_tuning())) if plan.level_tuning()[i][3] > 512]
+    assert tall and all(plan.level_variant(i) == (1, 2) for i in tall)
+    got = plan.displacement(fr).cpu().numpy()
+    for i in tall:
+        plan.set_level_variant(i, 0)
+    other = plan.displacement(fr).cpu().numpy()
+    plan.close()
+    # the reference amplifies rounding (a 1e-7 input change moves its flow by ~0.1 px at
+    # single pixels), so the comparisons are on the mean
+    assert np.abs(got - other).mean() < 0.01, np.abs(got - other).mean()
+    want = oracle.get_displacement(ref.cpu().numpy(), fr[0].cpu().numpy(), **opts)
+    assert np.abs(got[0] - want).mean() < 0.05, np.abs(got[0] - want).mean()
