@@ -145,7 +145,9 @@ def test_cluster_sor_on_tall_levels_matches_the_other_kernels(oracle, key):
     other = plan.displacement(fr).cpu().numpy()
     plan.close()
     # the reference amplifies rounding (a 1e-7 input change moves its flow by ~0.1 px at
-    # single pixels), so the comparisons are on the mean
+    # single pixels), so the comparisons are on the mean, and the fp32 result is held to
+    # the accuracy of the kernel it replaces
     assert np.abs(got - other).mean() < 0.01, np.abs(got - other).mean()
     want = oracle.get_displacement(ref.cpu().numpy(), fr[0].cpu().numpy(), **opts)
-    assert np.abs(got[0] - want).mean() < 0.05, np.abs(got[0] - want).mean()
+    e_got, e_other = np.abs(got[0] - want).mean(), np.abs(other[0] - want).mean()
+    assert e_got <= 1.25 * e_other + 1e-3, (e_got, e_other)
