@@ -356,12 +356,114 @@ class Plan:
             pass
 
 
+def lanes_for(n_frames: int) -> int:
+    """Lanes of a batched plan: one frame's level runs as one CTA (or one cluster),
+    so a batch of a few hundred frames leaves the last wave of every level part
+    empty; independent lanes on their own streams fill those gaps."""
+    return 4 if n_frames >= 256 else (2 if n_frames >= 128 else 1)
+
+
+class LanePlan:
+    """Several plans over contiguous frame ranges of one batch, each on its own
+    stream, joined to the caller's stream by events: the same flows as one
+    plan (every frame is independent), with the levels of different lanes
+    overlapping on the GPU.  Tuning, kernel variants and profiling apply to
+    every lane."""
+
+    def __init__(self, params, H: int, W: int, K: int, max_frames: int, lanes: int):
+        _require_cuda()
+        self.H, self.W, self.K, self.params = H, W, K, params
+        self.device = torch.cuda.current_device()
+        self.lane_frames = -(-int(max_frames) // int(lanes))
+        self.plans = [Plan(params, H, W, K, self.lane_frames) for _ in range(int(lanes))]
+        self.max_frames = self.lane_frames * len(self.plans)
+        self.streams = [torch.cuda.Stream() for _ in self.plans]
+
+    @property
+    def fp64(self) -> bool:
+        return self.plans[0].fp64
+
+    def levels(self):
+        return self.plans[0].levels()
+
+    def level_tuning(self):
+        return self.plans[0].level_tuning()
+
+    def level_variant(self, level: int):
+        return self.plans[0].level_variant(level)
+
+    def set_level_tuning(self, level: int, sor_G: int = 0, sor_threads: int = 0) -> None:
+        for p in self.plans:
+            p.set_level_tuning(level, sor_G, sor_threads)
+
+    def set_level_variant(self, level: int, variant: int) -> None:
+        for p in self.plans:
+            p.set_level_variant(level, variant)
+
+    def device_bytes(self) -> int:
+        return sum(p.device_bytes() for p in self.plans)
+
+    def set_profiling(self, enable: bool) -> None:
+        for p in self.plans:
+            p.set_profiling(enable)
+
+    def profile(self):
+        """Summed over the lanes (their launches overlap in time)."""
+        n = ms = b = 0
+        for p in self.plans:
+            pn, pms, pb = p.profile()
+            n, ms, b = n + pn, ms + pms, b + pb
+        return n, ms, b
+
+    def autotune(self, moving_t, n_levels: int = 5, reps: int = 2):
+        """Plan.autotune on the first lane with a lane-sized slice of the batch;
+        the other lanes take its choice."""
+        chosen = self.plans[0].autotune(moving_t[:self.lane_frames], n_levels, reps)
+        for i, (v, g, t, _) in chosen.items():
+            for p in self.plans[1:]:
+                p.set_level_variant(i, v)
+                p.set_level_tuning(i, g, t)
+        return chosen
+
+    def set_reference(self, fixed_t, weight_t=None, stream=None, key=None):
+        for p in self.plans:
+            p.set_reference(fixed_t, weight_t, stream=stream, key=key)
+
+    def displacement(self, moving_t, uv_t=None, out_t=None, stream=None):
+        T = moving_t.shape[0]
+        odt = torch.float64 if self.fp64 else torch.float32
+        if out_t is None:
+            out_t = torch.empty((T, self.H, self.W, 2), dtype=odt, device=moving_t.device)
+        n = self.lane_frames
+        if T <= n:
+            return self.plans[0].displacement(moving_t, uv_t, out_t, stream=stream)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        start = torch.cuda.Event()
+        start.record(s)
+        per = -(-T // len(self.plans))
+        for i, (p, ls) in enumerate(zip(self.plans, self.streams)):
+            t0, t1 = i * per, min(T, (i + 1) * per)
+            if t0 >= t1:
+                break
+            ls.wait_event(start)
+            p.displacement(moving_t[t0:t1], uv_t, out_t[t0:t1], stream=ls)
+            done = torch.cuda.Event()
+            done.record(ls)
+            s.wait_event(done)
+        return out_t
+
+    def close(self):
+        for p in self.plans:
+            p.close()
+
+
 _plans: dict = {}
 _plans_lock = threading.Lock()
 
 
-def get_plan(params, H: int, W: int, K: int, n_frames: int, max_frames: Optional[int] = None) -> Plan:
-    """Cached plan for (shape, options, device); grown when a larger batch arrives."""
+def get_plan(params, H: int, W: int, K: int, n_frames: int, max_frames: Optional[int] = None):
+    """Cached plan for (shape, options, device); grown when a larger batch
+    arrives.  Batches of 128 frames and more get a LanePlan."""
     _require_cuda()
     key = (H, W, K, _params_key(params), torch.cuda.current_device())
     want = max(1, int(max_frames or n_frames))
@@ -370,7 +472,8 @@ def get_plan(params, H: int, W: int, K: int, n_frames: int, max_frames: Optional
         if plan is None or plan.max_frames < want:
             if plan is not None:
                 plan.close()
-            plan = Plan(params, H, W, K, want)
+            lanes = lanes_for(want)
+            plan = LanePlan(params, H, W, K, want, lanes) if lanes > 1 else Plan(params, H, W, K, want)
             _plans[key] = plan
         return plan
 
