@@ -151,3 +151,25 @@ def test_cluster_sor_on_tall_levels_matches_the_other_kernels(oracle, key):
     want = oracle.get_displacement(ref.cpu().numpy(), fr[0].cpu().numpy(), **opts)
     e_got, e_other = np.abs(got[0] - want).mean(), np.abs(other[0] - want).mean()
     assert e_got <= 1.25 * e_other + 1e-3, (e_got, e_other)
+
+
+@pytest.mark.parametrize("T", [130, 261])
+def test_lane_plan_equals_one_plan(T):
+    """Large batches run as lanes (plans over contiguous frame ranges on their
+    own streams): the flows are exactly those of one plan, also for a batch
+    that the lanes do not divide evenly and for a call smaller than a lane."""
+    from pyflowreg_gb300 import api
+
+    key = (48, 56, 2)
+    ref, fr = _frames(key, T, 11)
+    params = api.make_params(K=2, **OPTS)
+    one = api.Plan(params, *key, T)
+    one.set_reference(ref)
+    want = one.displacement(fr).clone()
+    one.close()
+    lanes = api.LanePlan(params, *key, T, api.lanes_for(T))
+    assert len(lanes.plans) == (4 if T >= 256 else 2)
+    lanes.set_reference(ref)
+    assert torch.equal(lanes.displacement(fr), want)
+    assert torch.equal(lanes.displacement(fr[:7]), want[:7])
+    lanes.close()
