@@ -446,7 +446,7 @@ def run_gb300(args):
         # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
         chosen = plan.autotune(frames, n_levels=4, reps=1)
         tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
-                  {"kernel": ("rows_in_registers" if v == 1 else "diagonal_ring"), "G": g,
+                  {"kernel": {0: "diagonal_ring", 1: "rows_in_registers", 2: "rows_in_registers_chained"}[v], "G": g,
                    "threads": t or plan.level_tuning()[i][3]}
                   for i, (v, g, t, _) in chosen.items()}
     for _ in range(max(args.warmup, 3)):

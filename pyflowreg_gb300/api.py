@@ -247,8 +247,9 @@ class Plan:
 
     def level_variant(self, level: int):
         """(variant, n_variants) of a level's fused SOR kernel: 0 the diagonal
-        ring, 1 rows with the state in registers; n_variants 0 when the level
-        does not use a fused kernel."""
+        ring, 1 rows with the state in registers (one launch per pass), 2 the
+        same with all passes of the level chained in one launch; n_variants
+        counts the variants that serve the level."""
         v, n = ctypes.c_int(), ctypes.c_int()
         _lib.check(self.lib.frg_plan_level_variant(self.handle, level, ctypes.byref(v), ctypes.byref(n)))
         return v.value, n.value
@@ -288,8 +289,8 @@ class Plan:
             gs = list(range(gmax, 0, -1))
             ths = sorted({t for t in (rows, ((rows * 3 // 2) + 31) // 32 * 32, 1024) if rows <= t <= 1024})
             cands = [(0, g, t) for g in gs for t in ths]
-            if self.level_variant(i)[1] > 1:
-                cands += [(1, g, 0) for g in gs]
+            nv = self.level_variant(i)[1]
+            cands += [(v, g, 0) for v in range(1, nv) for g in gs]
             best = None
             for var, g, t in cands:
                 self.set_level_variant(i, var)

@@ -272,7 +272,8 @@ struct LevelPlan {
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
     int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
     int sor_variant = 0;  // fused SOR kernel: 0 diagonal ring in shared memory, 1 rows with the state in registers
-                          // (the default where it serves)
+                          // (one launch per pass), 2 the same with every pass of the level in one launch (the
+                          // default where it serves)
 };
 
 // Iteration groups between nonlinearity ticks ((t+1) % update_lag == 0,
@@ -449,11 +450,37 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
                 int tune_G = 0, int tune_threads = 0, int tune_variant = 0)
 {
     const SorKind kind = sor_kind(K, g);
-    const bool regs = tune_variant == 1 && sor_regs_supports(K, g);
+    const bool regs = tune_variant >= 1 && sor_regs_supports(K, g);
     const bool fused = kind == kSorFused && !regs;
     int gmax = regs ? kGMax : (kind == kSorFused ? sor_fused_gmax(g.P) : (kind == kSorRows ? kGMax : update_lag));
     if ((fused || regs) && tune_G > 0 && tune_G < gmax) gmax = tune_G;
     const std::vector<Pass> passes = make_passes(iterations, update_lag, gmax);
+    if (regs && tune_variant == 2 && sor_chain_supports(K, g, (int)passes.size())) {
+        // every pass in one launch; same arguments per pass as the loop below
+        std::vector<ChainPass> cp(passes.size());
+        double its = 0.0;
+        for (size_t pi = 0; pi < passes.size(); ++pi) {
+            const bool continued = pi + 1 < passes.size() && passes[pi + 1].fold_mode < 0;
+            cp[pi].G = passes[pi].G;
+            cp[pi].mode = passes[pi].fold_mode;
+            cp[pi].store_coef = (passes[pi].fold_mode >= 0 && continued) ? 1 : 0;
+            its += passes[pi].G;
+        }
+        const bool timed = prof && prof->on;
+        if (timed) {
+            int rc = record_event(prof, st);
+            if (rc) return rc;
+        }
+        FRG_LAUNCH(launch_sor_chain(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, T, K, g, cp.data(),
+                                    (int)cp.size(), a_data, wx, wy, omega, st, rm_du, rm_dv, rm_fs));
+        if (timed) {
+            int rc = record_event(prof, st);
+            if (rc) return rc;
+            prof->bytes += 36.0 * its * (double)T * g.h * g.w;
+            prof->launches += 1;
+        }
+        return FRG_OK;
+    }
     for (size_t pi = 0; pi < passes.size(); ++pi) {
         const Pass& ps = passes[pi];
         if (!fused && !regs && ps.fold_mode >= 0)
@@ -630,8 +657,9 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         L.wy = (float)(L.alpha_y / (L.h_row * L.h_row));
         L.g = make_geom(L.h, L.w);
         // the rows-in-registers SOR is the faster kernel wherever it serves (same bits as the
-        // diagonal ring; levels taller than 512 rows run it as a cluster of row strips)
-        L.sor_variant = sor_regs_supports(channels, L.g) ? 1 : 0;
+        // diagonal ring; levels taller than 512 rows run it as a cluster of row strips), with
+        // all passes of the level chained in one launch where one CTA holds the level
+        L.sor_variant = sor_chain_supports(channels, L.g, 1) ? 2 : (sor_regs_supports(channels, L.g) ? 1 : 0);
         const double sig = resize_sigma(m, n, L.h, L.w);
         HostTables tx = make_tables(n, L.w, sig), ty = make_tables(m, L.h, sig);
         if ((rc = upload_tables(pl, tx, L.w, ty, L.h, &L.img))) { frg_plan_destroy(pl); return rc; }
@@ -847,10 +875,13 @@ int frg_plan_set_level_variant(frg_plan* plan, int level, int variant)
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     LevelPlan& L = plan->levels[level];
-    if (variant < 0 || variant > 1)
-        return fail(FRG_EINVAL, "variant must be 0 (the level's ring / row / global kernel) or 1 (rows in registers)");
-    if (variant == 1 && !sor_regs_supports(plan->K, L.g))
+    if (variant < 0 || variant > 2)
+        return fail(FRG_EINVAL, "variant must be 0 (the level's ring / row / global kernel), 1 (rows in registers) "
+                                "or 2 (rows in registers, passes chained in one launch)");
+    if (variant >= 1 && !sor_regs_supports(plan->K, L.g))
         return fail(FRG_EINVAL, "the rows-in-registers SOR does not serve this level");
+    if (variant == 2 && !sor_chain_supports(plan->K, L.g, 1))
+        return fail(FRG_EINVAL, "the chained rows-in-registers SOR does not serve this level");
     L.sor_variant = variant;
     return FRG_OK;
 }
@@ -860,7 +891,8 @@ int frg_plan_level_variant(const frg_plan* plan, int level, int* variant, int* n
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     const LevelPlan& L = plan->levels[level];
     if (variant) *variant = L.sor_variant;
-    if (n_variants) *n_variants = sor_regs_supports(plan->K, L.g) ? 2 : 1;
+    if (n_variants)
+        *n_variants = sor_chain_supports(plan->K, L.g, 1) ? 3 : (sor_regs_supports(plan->K, L.g) ? 2 : 1);
     return FRG_OK;
 }
 
@@ -973,7 +1005,7 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
         // 5. level solve (core/optical_flow.py:584-606); the fused kernels write the last pass
         // row-major for the median
-        const bool fused = sor_kind(K, L.g) == kSorFused || (L.sor_variant == 1 && sor_regs_supports(K, L.g));
+        const bool fused = sor_kind(K, L.g) == kSorFused || (L.sor_variant >= 1 && sor_regs_supports(K, L.g));
         int rc = solve_level(pl->p.iterations, pl->p.update_lag, pl->J, J_fs, L.wdiag, 0, pl->lap, 2 * dp, pl->du,
                              pl->dv, dp, pl->coef, 5 * dp, T, K, L.g, pl->a_data, L.wx, L.wy, (float)pl->p.omega, st,
                              &pl->prof, pl->durm, pl->durm + (long long)T * hw, hw, L.sor_G, L.sor_threads,

@@ -91,6 +91,23 @@ cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long
                             int n_frames, int K, DiagGeom g, int G, int mode, int store_coef, const float* a_data,
                             float wx, float wy, float omega, cudaStream_t st, float* out_du = nullptr,
                             float* out_dv = nullptr, long long out_fs = 0);
+// Every pass of a level in one launch of the rows-in-registers SOR (frg_sor.cu,
+// k_sor_chain): a row starts its next pass as soon as it has finished the
+// current one, so the passes follow each other without restarting the
+// wavefront.  Pass p is the launch_sor_regs pass (G, mode, store_coef); the
+// level's last pass writes out_du/out_dv when given.  Single-CTA levels
+// (sor_regs_supports with P <= kMaxLane), w >= 3, at most kMaxChain passes;
+// bit-identical to one launch_sor_regs call per pass.
+constexpr int kMaxChain = 64;
+struct ChainPass {
+    int G, mode, store_coef;
+};
+bool sor_chain_supports(int K, const DiagGeom& g, int n_passes);
+cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
+                             long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                             int n_frames, int K, DiagGeom g, const ChainPass* passes, int n_passes,
+                             const float* a_data, float wx, float wy, float omega, cudaStream_t st,
+                             float* out_du = nullptr, float* out_dv = nullptr, long long out_fs = 0);
 // 5x5 median (mirror) of row-major du, dv (T, h, w) plus accumulation into u, v.
 cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
                              int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st);

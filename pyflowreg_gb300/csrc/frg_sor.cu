@@ -98,10 +98,10 @@ struct Coef {
 };
 
 template <int K>
-__device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
+__device__ __forceinline__ Coef fold_m(const SorArgs& A, int mode, const Raw<K>& r)
 {
     Coef o;
-    if (A.mode < 0) {
+    if (mode < 0) {
         o.A12 = r.j[0];
         o.BU = r.j[1];
         o.BV = r.j[2];
@@ -109,7 +109,7 @@ __device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
         o.iDv = r.j[4];
         return o;
     }
-    const bool tick = (A.mode & 2) != 0;
+    const bool tick = (mode & 2) != 0;
     float A11 = 0.f, A22 = 0.f, a12 = 0.f, C13 = 0.f, C23 = 0.f;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -146,6 +146,12 @@ __device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
     o.iDu = den_u != 0.0f ? __frcp_rn(den_u) : 0.0f;
     o.iDv = den_v != 0.0f ? __frcp_rn(den_v) : 0.0f;
     return o;
+}
+
+template <int K>
+__device__ __forceinline__ Coef fold(const SorArgs& A, const Raw<K>& r)
+{
+    return fold_m<K>(A, A.mode, r);
 }
 
 __device__ __forceinline__ void store_coef(const SorArgs& A, const Coef& c, float* coef, long long o, long long plane)
@@ -509,6 +515,223 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
     }
 }
 
+// ---------------------------------------------------------------------------
+// k_sor_chain: every pass of a level in one launch of the rows-in-registers
+// schedule.  A row's local time is tau = s - r; pass p occupies the local
+// times [start_p, start_p + span_p) with span_p = w + 2(G_p - 1) (w + 1 for
+// G_p = 1: the prefetch at column w of a pass loads the pass-start value below
+// the pass's last column), and pass p + 1 starts where pass p ends, so a row
+// goes from its last update of one pass to its first of the next without
+// waiting for the wavefront to drain and refill.  Within a pass
+// everything is as in k_sor_regs (pixel (r, c), iteration gi at tau =
+// start_p + c + 2 gi).  The passes never overlap in one row (pass p's last
+// column c = w - 1 of its last iteration falls before pass p + 1's column 0),
+// so the per-row register state serves them one after the other.  Between
+// passes the state goes through du, dv in global memory as between launches:
+// a row's final value of pass p at (r, c) is stored at tau = start_p + c +
+// 2(G_p - 1) and read back for pass p + 1 at least w - 2 steps later (the
+// row below's value too, so past at least one barrier for w >= 3).
+// Three cursors follow the pass of the update (tau), of the coefficient fold
+// (tau + 1: the fold of the diagonal entering next step runs after this step's
+// updates, off their critical path) and of the prefetch (tau + 2).  The ring
+// slot of a pixel is its entry step mod (2G - 1), as in k_sor_regs.
+// Offsets within a frame are 32-bit (the host checks the plane sizes).
+// ---------------------------------------------------------------------------
+// Pass table: one packed word per pass, G << 8 | store << 3 | coef << 2 |
+// tick << 1 | zero (zero: du = dv = 0 at the pass start; tick: psi from the
+// pass-start du, dv; coef: the folded coefficients are read back instead of
+// folded; store: the fold also writes them for the passes that read them).
+struct ChainTable {
+    int n;
+    int pk[kMaxChain];
+};
+
+constexpr int kPkZero = 1, kPkTick = 2, kPkCoef = 4, kPkStore = 8;
+
+// fold of k_sor_regs (fold_m) with the pass's mode given as flags
+template <int K, bool CO>
+__device__ __forceinline__ Coef fold_pk(const SorArgs& A, int pk, const Raw<K>& r)
+{
+    if (CO && (pk & kPkCoef)) return fold_m<K>(A, -1, r);
+    return fold_m<K>(A, (pk & kPkTick) ? 2 : 0, r);
+}
+
+template <int K, int G, bool CO>
+__global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
+{
+    extern __shared__ __align__(16) float sm[];
+    constexpr int S = 2 * G - 1;
+    const DiagGeom g = A.g;
+    const int P = g.P, h = g.h, w = g.w;
+    const int NT = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, NW = NT >> 5;
+    const int f = (int)blockIdx.x;
+    const int r = t;
+    float4* C4 = reinterpret_cast<float4*>(sm);
+    float* C1 = sm + 4 * S * NT;
+    float2* X = reinterpret_cast<float2*>(C1 + S * NT);
+    const int pl = g.D * P;
+    const float* Jr = A.J + f * A.J_fs + r;
+    const float* Wr = A.W + f * A.W_fs + r;
+    const float* lapr = A.lap + f * A.lap_fs + r;
+    float* coefr = A.coef + f * A.coef_fs + r;
+    float* dur = A.du + f * A.st_fs + r;
+    float* dvr = A.dv + f * A.st_fs + r;
+    float* odu = A.out_du ? A.out_du + f * A.out_fs : nullptr;
+    float* odv = A.out_dv ? A.out_dv + f * A.out_fs : nullptr;
+    const float omega = A.omega, one_m_omega = 1.0f - omega, wa = A.wa, wb = A.wb;
+    const bool row_ok = r < h;
+    const bool has_below = r + 1 < h;
+    const int last = T.n - 1;
+    auto span = [&](int pk) {
+        const int G_p = pk >> 8;
+        return w + (G_p > 1 ? 2 * (G_p - 1) : 1);
+    };
+
+    // inputs of the pixel entering at column c of a pass with flags pk, and the
+    // pass-start value of the pixel below its left neighbour (fetch of k_sor_regs)
+    auto fetch = [&](int c, int pk, Pre<K>& p) {
+        const bool zero = (pk & kPkZero) != 0;
+        const int o = (r + c) * P;
+        if (row_ok && c >= 0 && c < w) {
+            if (CO && (pk & kPkCoef)) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) p.raw.j[q] = coefr[q * pl + o];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 6 * K; ++q) p.raw.j[q] = Jr[q * pl + o];
+#pragma unroll
+                for (int k = 0; k < K; ++k) p.raw.w[k] = Wr[k * pl + o];
+                p.raw.lu = lapr[o];
+                p.raw.lv = lapr[pl + o];
+            }
+            p.raw.du = zero ? 0.0f : dur[o];
+            p.raw.dv = zero ? 0.0f : dvr[o];
+        }
+        if (has_below && c >= 1 && c <= w) {
+            p.nu = zero ? 0.0f : dur[o + 1];
+            p.nv = zero ? 0.0f : dvr[o + 1];
+        }
+    };
+    auto fold_into = [&](int c, int pk, const Pre<K>& p, int slot) {
+        if (row_ok && c >= 0 && c < w) {
+            const Coef cf = fold_pk<K, CO>(A, pk, p.raw);
+            if (CO && (pk & kPkStore)) {
+                const int o = (r + c) * P;
+                coefr[o] = cf.A12;
+                coefr[pl + o] = cf.BU;
+                coefr[2 * pl + o] = cf.BV;
+                coefr[3 * pl + o] = cf.iDu;
+                coefr[4 * pl + o] = cf.iDv;
+            }
+            C4[slot * NT + t] = make_float4(cf.A12, cf.BU, cf.BV, cf.iDu);
+            C1[slot * NT + t] = cf.iDv;
+        }
+    };
+    auto xs = [&](int par, int wp, int dir, int gi) -> float2& { return X[((par * NW + wp) * 2 + dir) * G + gi]; };
+
+    // the row's current pass (of the update at tau = s - r): index, local start and
+    // end, its flags and those of the next pass; the fold (tau + 1) and the prefetch
+    // (tau + 2) fall in the current or the next pass (every span is at least w + 1 >= 4)
+    int cp = 0, cstart = 0;
+    int pk_cur = T.pk[0];
+    int pk_nxt = last > 0 ? T.pk[1] : 0;
+    int cend = span(pk_cur);
+    Pre<K> pre[2];
+    fetch(-r, pk_cur, pre[0]);
+    fetch(1 - r, pk_cur, pre[1]);
+    fold_into(-r, pk_cur, pre[0], 0);
+    float2 V0[G], V1[G], V2[G];
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) V0[gi] = V1[gi] = V2[gi] = make_float2(0.0f, 0.0f);
+
+    int total = 0;
+    for (int p = 0; p < T.n; ++p) total += span(T.pk[p]);
+    const int nsteps = total + h - 1;
+    int slot0 = 0;  // s % S
+    for (int s0 = 0; s0 < nsteps; s0 += 2) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int s = s0 + q;
+            if (s < nsteps) {
+                Pre<K>& cur = pre[q];       // the pixel entering at step s
+                Pre<K>& nxt = pre[q ^ 1];   // the pixel entering at step s + 1
+                const int slot1 = slot0 + 1 == S ? 0 : slot0 + 1;
+                const int tau = s - r;
+                if (tau >= cend && cp < last) {
+                    ++cp;
+                    cstart = cend;
+                    pk_cur = pk_nxt;
+                    pk_nxt = cp < last ? T.pk[cp + 1] : 0;
+                    cend = cstart + span(pk_cur);
+                }
+                const bool more = cp < last;
+                const bool e_nx = more && tau + 2 >= cend, f_nx = more && tau + 1 >= cend;
+                const int Gp = pk_cur >> 8;
+                const bool final_rm = !more && odu != nullptr;
+                const int c0 = tau - cstart;
+                const float2 ps0 = make_float2(cur.raw.du, cur.raw.dv);
+                const float2 ps1 = make_float2(nxt.raw.du, nxt.raw.dv);
+                const float2 dn1 = make_float2(nxt.nu, nxt.nv);
+                fetch(e_nx ? tau + 2 - cend : c0 + 2, e_nx ? pk_nxt : pk_cur, cur);
+                const int pin = (s + 1) & 1;  // parity written at step s - 1
+#pragma unroll
+                for (int gj = 0; gj < G; ++gj) {
+                    const int gi = G - 1 - gj;  // the independent updates first, the newest column last
+                    float2 up, dn;
+                    up.x = __shfl_up_sync(0xffffffffu, V1[gi].x, 1);
+                    up.y = __shfl_up_sync(0xffffffffu, V1[gi].y, 1);
+                    if (lane == 0 && warp > 0) up = xs(pin, warp - 1, 0, gi);
+                    if (gi == 0) {
+                        dn = dn1;
+                    } else {
+                        dn.x = __shfl_down_sync(0xffffffffu, V1[gi - 1].x, 1);
+                        dn.y = __shfl_down_sync(0xffffffffu, V1[gi - 1].y, 1);
+                        if (lane == 31 && warp < NW - 1) dn = xs(pin, warp + 1, 1, gi - 1);
+                    }
+                    const int c = c0 - 2 * gi;
+                    if (gi < Gp && row_ok && c >= 0 && c < w) {
+                        const float2 own = gi == 0 ? ps0 : V2[gi - 1];
+                        const float2 lf = c > 0 ? V1[gi] : own;
+                        const float2 rt = c < w - 1 ? (gi == 0 ? ps1 : V1[gi - 1]) : own;
+                        const float2 u_ = r > 0 ? up : own;
+                        const float2 d_ = r < h - 1 ? dn : own;
+                        int sl = slot0 - 2 * gi;
+                        if (sl < 0) sl += S;
+                        V0[gi] = sor_point(own, u_, d_, lf, rt, C4[sl * NT + t], C1[sl * NT + t], wa, wb, omega,
+                                           one_m_omega);
+                        if (gi == Gp - 1) {
+                            if (final_rm) {
+                                odu[r * w + c] = V0[gi].x;
+                                odv[r * w + c] = V0[gi].y;
+                            } else {
+                                dur[(r + c) * P] = V0[gi].x;
+                                dvr[(r + c) * P] = V0[gi].y;
+                            }
+                        }
+                    }
+                }
+                fold_into(f_nx ? tau + 1 - cend : c0 + 1, f_nx ? pk_nxt : pk_cur, nxt, slot1);
+                const int pout = s & 1;
+                if (lane == 31) {
+#pragma unroll
+                    for (int gi = 0; gi < G; ++gi) xs(pout, warp, 0, gi) = V0[gi];
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int gi = 0; gi + 1 < G; ++gi) xs(pout, warp, 1, gi) = V0[gi];
+                }
+#pragma unroll
+                for (int gi = 0; gi < G; ++gi) {
+                    V2[gi] = V1[gi];
+                    V1[gi] = V0[gi];
+                }
+                slot0 = slot1;
+            }
+            __syncthreads();
+        }
+    }
+}
+
 constexpr int kSmemLimit = 232448;  // 227 KB of dynamic shared memory per CTA
 
 template <int K, int PF, int MAXT>
@@ -683,6 +906,86 @@ cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long
         case 2: return run_regs<2>(A, n_frames, nt, st);
         case 3: return run_regs<3>(A, n_frames, nt, st);
         default: return run_regs<4>(A, n_frames, nt, st);
+    }
+}
+
+namespace {
+
+template <int K, int G, bool CO>
+cudaError_t run_chain_t(const SorArgs& A, const ChainTable& T, int n_frames, int nt, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmemLimit);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_sor_chain<K, G, CO><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A, T);
+    return cudaGetLastError();
+}
+
+template <int K, bool CO>
+cudaError_t run_chain_c(const SorArgs& A, const ChainTable& T, int gmax, int n_frames, int nt, cudaStream_t st)
+{
+    switch (gmax) {
+        case 1: return run_chain_t<K, 1, CO>(A, T, n_frames, nt, st);
+        case 2: return run_chain_t<K, 2, CO>(A, T, n_frames, nt, st);
+        case 3: return run_chain_t<K, 3, CO>(A, T, n_frames, nt, st);
+        case 4: return run_chain_t<K, 4, CO>(A, T, n_frames, nt, st);
+        default: return run_chain_t<K, 5, CO>(A, T, n_frames, nt, st);
+    }
+}
+
+// CO: some pass reads back or stores folded coefficients (windows between psi
+// ticks longer than the pass length)
+template <int K>
+cudaError_t run_chain(const SorArgs& A, const ChainTable& T, bool co, int gmax, int n_frames, int nt,
+                      cudaStream_t st)
+{
+    return co ? run_chain_c<K, true>(A, T, gmax, n_frames, nt, st) : run_chain_c<K, false>(A, T, gmax, n_frames, nt, st);
+}
+
+}  // namespace
+
+bool sor_chain_supports(int K, const DiagGeom& g, int n_passes)
+{
+    // 32-bit offsets: the largest plane index read is (6K + 2) planes of D * P
+    const long long plane = (long long)g.D * g.P;
+    return sor_regs_supports(K, g) && g.P <= kMaxLane && g.w >= 3 && n_passes >= 1 && n_passes <= kMaxChain &&
+           plane * (6 * K + 2) < 0x7fffffffLL && (long long)g.h * g.w < 0x7fffffffLL;
+}
+
+cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, long long W_fs, const float* lap,
+                             long long lap_fs, float* coef, long long coef_fs, float* du, float* dv, long long st_fs,
+                             int n_frames, int K, DiagGeom g, const ChainPass* passes, int n_passes,
+                             const float* a_data, float wx, float wy, float omega, cudaStream_t st, float* out_du,
+                             float* out_dv, long long out_fs)
+{
+    if (!sor_chain_supports(K, g, n_passes) || n_frames < 1) return cudaErrorInvalidValue;
+    ChainTable T;
+    T.n = n_passes;
+    int gmax = 1;
+    bool co = false;
+    for (int p = 0; p < n_passes; ++p) {
+        const ChainPass& q = passes[p];
+        if (q.G < 1 || q.G > kGMax || q.mode < -1 || q.mode > 3) return cudaErrorInvalidValue;
+        const bool coef = q.mode < 0, store = q.mode >= 0 && q.store_coef;
+        T.pk[p] = (q.G << 8) | (store ? kPkStore : 0) | (coef ? kPkCoef : 0) |
+                  (!coef && (q.mode & 2) ? kPkTick : 0) | (!coef && (q.mode & 1) ? kPkZero : 0);
+        co = co || coef || store;
+        gmax = q.G > gmax ? q.G : gmax;
+    }
+    for (int p = n_passes; p < kMaxChain; ++p) T.pk[p] = 1 << 8;
+    const int nt = g.P;
+    if (sor_regs_smem(gmax, nt) > (size_t)kSmemLimit) return cudaErrorInvalidValue;
+    SorArgs A = make_args(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, K, g, gmax, 0, 0, a_data, wx,
+                          wy, omega, out_du, out_dv, out_fs);
+    switch (K) {
+        case 1: return run_chain<1>(A, T, co, gmax, n_frames, nt, st);
+        case 2: return run_chain<2>(A, T, co, gmax, n_frames, nt, st);
+        case 3: return run_chain<3>(A, T, co, gmax, n_frames, nt, st);
+        default: return run_chain<4>(A, T, co, gmax, n_frames, nt, st);
     }
 }
 

@@ -104,8 +104,10 @@ def test_autotuned_plan_gives_identical_flows():
                                         ((70, 64, 4), 2), ((600, 96, 2), 2), ((900, 60, 1), 2)])
 def test_sor_variants_give_identical_flows(key, frames):
     """The rows-in-registers SOR (one CTA, or a cluster of row strips above 512
-    rows) and the diagonal-ring SOR give the same bits on every level both
-    serve, for every pass length."""
+    rows; one launch per pass, or every pass of a level chained in one launch)
+    and the diagonal-ring SOR give the same bits on every level they serve,
+    for every pass length (G = 3 splits the windows between psi ticks, so
+    passes that store and read back the folded coefficients are chained too)."""
     from pyflowreg_gb300 import api
 
     ref, fr = _frames(key, frames, 7)
@@ -117,11 +119,15 @@ def test_sor_variants_give_identical_flows(key, frames):
     for i in both:
         plan.set_level_variant(i, 0)
     base = plan.displacement(fr).clone()
-    for G in (5, 3, 1):
-        for i in both:
-            plan.set_level_variant(i, 1)
-            plan.set_level_tuning(i, min(G, tun[i][2]), 0)
-        assert torch.equal(base, plan.displacement(fr)), G
+    for var in (1, 2):
+        for G in (5, 3, 1):
+            served = [i for i in both if plan.level_variant(i)[1] > var]
+            for i in served:
+                plan.set_level_variant(i, var)
+                plan.set_level_tuning(i, min(G, tun[i][2]), 0)
+            assert torch.equal(base, plan.displacement(fr)), (var, G)
+    if key[0] <= 512:
+        assert all(plan.level_variant(i)[1] == 3 for i in both)
     plan.close()
 
 
