@@ -583,8 +583,9 @@ def run_gb300(args):
     per_launch_bytes = sor_bytes / max(sor_n, 1)
     ratio = profiled_traffic()
     roofline = {
-        "kernel": "k_sor_regs (exact-order wavefront SOR, one thread per row, state in registers, fold in "
-                  "the loader; k_sor_fused on levels it does not serve)",
+        "kernel": "k_sor_chain (exact-order wavefront SOR, one thread per row, state in registers, fold in "
+                  "the loader, every pass of a level in one launch; k_sor_regs / k_sor_fused on levels it does "
+                  "not serve)",
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
