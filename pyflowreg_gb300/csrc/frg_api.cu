@@ -1000,9 +1000,8 @@ int frg_get_displacement(frg_plan* pl, int T, const float* moving, const float* 
         }
         // 4. motion tensor and smoothness constants (core/optical_flow.py:547-563)
         const long long J_fs = 6LL * K * dp;
-        FRG_LAUNCH(launch_tensor(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
-                               pl->J, J_fs, L.g, st));
-        FRG_LAUNCH(launch_lap(up, vp, T, h, w, L.wx, L.wy, pl->lap, 2 * dp, L.g, st));
+        FRG_LAUNCH(launch_tensor_lap(f1v, img2, T, K, h, w, (float)L.h_row, (float)L.h_col, pl->p.const_assumption,
+                                   pl->J, J_fs, L.g, up, vp, L.wx, L.wy, pl->lap, 2 * dp, st));
         // 5. level solve (core/optical_flow.py:584-606); the fused kernels write the last pass
         // row-major for the median
         const bool fused = sor_kind(K, L.g) == kSorFused || (L.sor_variant >= 1 && sor_regs_supports(K, L.g));

@@ -49,6 +49,11 @@ cudaError_t launch_warp(View f2, View f1, View u, View v, int n_frames, int K, i
                         float h_col, float h_row, int cubic, ViewW out, cudaStream_t st);
 cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
                           int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st);
+// launch_tensor plus the smoothness constant (launch_lap) from the same
+// pixel tiles: one launch, both written diagonal-major in contiguous runs.
+cudaError_t launch_tensor_lap(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx, int gray,
+                              float* J, long long J_fs, DiagGeom g, View u, View v, float wx, float wy, float* lap,
+                              long long lap_fs, cudaStream_t st);
 cudaError_t launch_lap(View u, View v, int n_frames, int h, int w, float wx, float wy, float* lap,
                        long long lap_fs, DiagGeom g, cudaStream_t st);
 cudaError_t launch_to_diag(View src, int n_frames, int n_planes, int h, int w, float* dst,

@@ -8,6 +8,9 @@
 
 #include <math.h>
 
+#include <algorithm>
+#include <cstdint>
+
 namespace frg {
 
 __constant__ float c_cubic[32 * 4];
@@ -63,76 +66,107 @@ __global__ void k_resize_v(const float* __restrict__ src, int n_planes, int ih, 
     dst.p[f * dst.fs + pl * dst.ps + (long long)yo * dst.rs + (long long)xo * dst.cs] = s;
 }
 
-// Horizontal pass, shared-memory form: one block takes `rows` input rows of
-// one frame (all planes), stages them and the level's tap table in shared
-// memory, and each thread produces one (plane, output column) for all the
-// block's rows, so each table entry is read once per `rows` outputs.  The
-// table is staged tap-major ([P][ow]) so that neighbouring threads (columns)
-// read neighbouring words.
-__global__ void k_resize_h_smem(View src, int n_planes, int ih, int iw, float* __restrict__ dst, int ow,
-                                const int32_t* __restrict__ ix, const float* __restrict__ wx, int P, int rows)
+// Horizontal pass, row-block form: one block takes up to R input rows of one
+// frame (all planes) into shared memory with asynchronous 16-byte copies
+// (cp.async; the rows of an interleaved frame, or of each plane of a planar
+// one, are one contiguous run), so every thread has its whole share of the
+// block's bytes in flight at once.  Each thread then produces one (plane,
+// output column) for RT consecutive rows, reading the tap table through L1;
+// RT shrinks at the coarse levels (few output columns, many taps) so that
+// every thread has work.  The sum is the same fmaf chain over the taps in
+// order as k_resize_h, so the results are the same bits.
+// mode 0: element-wise staging (any strides); 1: one contiguous interleaved
+// run (cs == planes, rs == planes * iw); 2: one contiguous run per plane
+// (cs == 1, rs == iw).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
 {
-    extern __shared__ float sh[];
-    int32_t* tix = reinterpret_cast<int32_t*>(sh);
-    float* twx = sh + (size_t)ow * P;
-    float* srow = twx + (size_t)ow * P;  // [rows][n_planes][iw]
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <int RT>
+__global__ void __launch_bounds__(256) k_resize_h_rows(View src, int n_planes, int ih, int iw, float* __restrict__ dst,
+                                                       int ow, const int32_t* __restrict__ ix,
+                                                       const float* __restrict__ wx, int P, int R, int mode)
+{
+    extern __shared__ __align__(16) float srow[];
     const int f = blockIdx.y;
-    const int y0 = blockIdx.x * rows;
-    const int nr = min(rows, ih - y0);
+    const int y0 = blockIdx.x * R;
+    const int nr = min(R, ih - y0);
     const int tid = threadIdx.x, nth = blockDim.x;
-    for (int i = tid; i < ow * P; i += nth) {
-        const int x = i / P, p = i - x * P;
-        tix[p * ow + x] = ix[i];
-        twx[p * ow + x] = wx[i];
-    }
-    const float* base = src.p + f * src.fs;
     const int row_elems = n_planes * iw;
-    for (int i = tid; i < nr * row_elems; i += nth) {
-        const int r = i / row_elems, rem = i - r * row_elems;
-        int pl, x;
-        if (src.cs == 1) {  // planar rows
-            pl = rem / iw;
-            x = rem - pl * iw;
-        } else {  // interleaved channels: consecutive elements walk the channels
-            x = rem / n_planes;
-            pl = rem - x * n_planes;
+    const float* base = src.p + f * src.fs + (long long)y0 * src.rs;
+    // shared layout: element (r, plane, x) at r * sr + plane * sp + x * sx
+    const int sr = mode == 2 ? iw : row_elems, sp = mode == 2 ? nr * iw : 1, sx = mode == 2 ? 1 : n_planes;
+    if (mode == 1) {
+        const int n4 = (nr * row_elems) >> 2;
+        for (int i = tid; i < n4; i += nth) cp_async16(srow + 4 * i, base + 4LL * i);
+        cp_async_wait_all();
+    } else if (mode == 2) {
+        const int n4 = (nr * iw) >> 2;
+        for (int pl = 0; pl < n_planes; ++pl) {
+            const float* pb = base + pl * src.ps;
+            for (int i = tid; i < n4; i += nth) cp_async16(srow + pl * sp + 4 * i, pb + 4LL * i);
         }
-        srow[((size_t)r * n_planes + pl) * iw + x] =
-            base[pl * src.ps + (long long)(y0 + r) * src.rs + (long long)x * src.cs];
+        cp_async_wait_all();
+    } else {
+        for (int i = tid; i < nr * row_elems; i += nth) {
+            const int r = i / row_elems, rem = i - r * row_elems;
+            const int x = rem / n_planes, pl = rem - x * n_planes;
+            srow[r * sr + pl * sp + x * sx] = base[pl * src.ps + (long long)r * src.rs + (long long)x * src.cs];
+        }
     }
     __syncthreads();
-    for (int item = tid; item < n_planes * ow; item += nth) {
-        const int pl = item / ow, x = item - pl * ow;
-        float acc[8];
+    const int groups = (nr + RT - 1) / RT;
+    const int items = groups * n_planes * ow;
+    for (int it = tid; it < items; it += nth) {
+        const int x = it % ow, rest = it / ow;
+        const int pl = rest % n_planes, r0 = (rest / n_planes) * RT;
+        float acc[RT];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) acc[r] = 0.0f;
+        for (int q = 0; q < RT; ++q) acc[q] = 0.0f;
+        const int32_t* ixr = ix + (long long)x * P;
+        const float* wxr = wx + (long long)x * P;
+        const float* sb = srow + r0 * sr + pl * sp;
         for (int p = 0; p < P; ++p) {
-            const int j = tix[p * ow + x];
-            const float wgt = twx[p * ow + x];
+            const float* sj = sb + __ldg(ixr + p) * sx;
+            const float wgt = __ldg(wxr + p);
 #pragma unroll
-            for (int r = 0; r < 8; ++r)
-                if (r < nr) acc[r] = fmaf(srow[((size_t)r * n_planes + pl) * iw + j], wgt, acc[r]);
+            for (int q = 0; q < RT; ++q)
+                if (r0 + q < nr) acc[q] = fmaf(sj[q * sr], wgt, acc[q]);
         }
-        for (int r = 0; r < nr; ++r)
-            dst[(((long long)f * n_planes + pl) * ih + y0 + r) * ow + x] = acc[r];
+#pragma unroll
+        for (int q = 0; q < RT; ++q)
+            if (r0 + q < nr) dst[(((long long)f * n_planes + pl) * ih + y0 + r0 + q) * ow + x] = acc[q];
     }
 }
 
 cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
                             const int32_t* ix, const float* wx, int P, cudaStream_t st)
 {
-    const int rows = 8;
-    const size_t smem = (size_t)ow * P * 8 + (size_t)rows * n_planes * iw * 4;
-    if (smem <= 96 * 1024 && n_frames <= 65535) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_resize_h_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 96 * 1024);
-            if (e != cudaSuccess) return e;
-            attr = true;
+    const long long row_bytes = (long long)n_planes * iw * 4;
+    const int R = (int)std::min<long long>(std::min(16, ih), 49152 / row_bytes);
+    if (R >= 1 && n_frames <= 65535) {
+        const bool a16 = ((uintptr_t)src.p & 15) == 0 && (src.fs & 3) == 0;
+        int mode = 0;
+        if (a16 && src.cs == n_planes && src.ps == 1 && src.rs == (long long)n_planes * iw && (n_planes * iw) % 4 == 0)
+            mode = 1;
+        else if (a16 && src.cs == 1 && src.rs == iw && iw % 4 == 0 && (src.ps & 3) == 0)
+            mode = 2;
+        // rows per thread: the largest that still gives every thread of the block an output
+        const int per_row = n_planes * ow;
+        int RT = 8;
+        while (RT > 1 && (long long)((R + RT - 1) / RT) * per_row < 256) RT >>= 1;
+        const size_t smem = (size_t)R * row_bytes;
+        dim3 grd((ih + R - 1) / R, n_frames);
+        switch (RT) {
+            case 8: k_resize_h_rows<8><<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, R, mode); break;
+            case 4: k_resize_h_rows<4><<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, R, mode); break;
+            case 2: k_resize_h_rows<2><<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, R, mode); break;
+            default: k_resize_h_rows<1><<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, R, mode);
         }
-        dim3 grd((ih + rows - 1) / rows, n_frames);
-        k_resize_h_smem<<<grd, 256, smem, st>>>(src, n_planes, ih, iw, dst, ow, ix, wx, P, rows);
         return cudaGetLastError();
     }
     dim3 blk(128), grd((ow + 127) / 128, ih, n_frames * n_planes);
@@ -296,6 +330,23 @@ __global__ void k_tensor(View f1, View f2, int K, int h, int w, float hy, float 
     }
 }
 
+// Constant part of the smoothness numerator at level pixel (y, x) from the
+// edge-padded (h+2) x (w+2) u, v (core/level_solver.py:317-340):
+//   lap_u = wx*((uL-uc)+(uR-uc)) + wy*((uU-uc)+(uD-uc)), lap_v likewise.
+__device__ __forceinline__ void lap_at(const View& u, const View& v, int f, int y, int x, float wx, float wy,
+                                       float& lu, float& lv)
+{
+    const float* up = u.p + f * u.fs;
+    const float* vp = v.p + f * v.fs;
+#define U_(r, c) up[(long long)(r) * u.rs + (long long)(c) * u.cs]
+#define V_(r, c) vp[(long long)(r) * v.rs + (long long)(c) * v.cs]
+    const float uc = U_(y + 1, x + 1), vc = V_(y + 1, x + 1);
+    lu = wx * ((U_(y + 1, x) - uc) + (U_(y + 1, x + 2) - uc)) + wy * ((U_(y, x + 1) - uc) + (U_(y + 2, x + 1) - uc));
+    lv = wx * ((V_(y + 1, x) - vc) + (V_(y + 1, x + 2) - vc)) + wy * ((V_(y, x + 1) - vc) + (V_(y + 2, x + 1) - vc));
+#undef U_
+#undef V_
+}
+
 // Tiled form: a 32 x 32 pixel tile is computed into shared memory, then every
 // diagonal crossing the tile is written as one contiguous run of the
 // diagonal-major layout (up to 128 bytes per warp store instead of 32
@@ -306,13 +357,16 @@ constexpr int kTensTile = 32;
 constexpr int kTensLd = kTensTile + 2;
 
 __global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, int h, int w, float hy, float hx,
-                                                      int gray, float* __restrict__ J, long long J_fs, DiagGeom g)
+                                                      int gray, float* __restrict__ J, long long J_fs, DiagGeom g,
+                                                      View u, View v, float wx, float wy, float* __restrict__ lap,
+                                                      long long lap_fs)
 {
-    extern __shared__ float tile[];  // [6K][32][34]
+    extern __shared__ float tile[];  // [6K (+2 with lap)][32][34]
     const int f = blockIdx.z;
     const int r0 = blockIdx.y * kTensTile, c0 = blockIdx.x * kTensTile;
     const int tx = threadIdx.x & 31, tw = threadIdx.x >> 5;  // 8 warps
     const int ld = kTensLd;
+    const int nq = 6 * K + (lap ? 2 : 0);
     for (int rr = tw; rr < kTensTile; rr += 8) {
         const int y = r0 + rr, x = c0 + tx;
         if (y < h && x < w) {
@@ -322,11 +376,18 @@ __global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, i
 #pragma unroll
                 for (int q = 0; q < 6; ++q) tile[((q * K + k) * kTensTile + rr) * ld + tx] = j[q];
             }
+            if (lap) {
+                float lu, lv;
+                lap_at(u, v, f, y, x, wx, wy, lu, lv);
+                tile[((6 * K) * kTensTile + rr) * ld + tx] = lu;
+                tile[((6 * K + 1) * kTensTile + rr) * ld + tx] = lv;
+            }
         }
     }
     __syncthreads();
     const long long plane = (long long)g.D * g.P;
     float* Jf = J + f * J_fs;
+    float* Lf = lap ? lap + f * lap_fs : nullptr;
     // local diagonal dd = rr + cc in [0, 62]; rows of the segment are contiguous
     for (int dd = tw; dd < 2 * kTensTile - 1; dd += 8) {
         const int rr_lo = max(0, dd - (kTensTile - 1));
@@ -337,13 +398,18 @@ __global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, i
         if (y >= h || x >= w) continue;
         const long long di = diag_index(g, y, x);
         for (int qk = 0; qk < 6 * K; ++qk) Jf[(long long)qk * plane + di] = tile[(qk * kTensTile + rr) * ld + cc];
+        for (int qk = 6 * K; qk < nq; ++qk)
+            Lf[(long long)(qk - 6 * K) * plane + di] = tile[(qk * kTensTile + rr) * ld + cc];
     }
 }
 
-cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
-                          int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st)
+namespace {
+
+cudaError_t run_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx, int gray, float* J,
+                       long long J_fs, DiagGeom g, View u, View v, float wx, float wy, float* lap, long long lap_fs,
+                       cudaStream_t st)
 {
-    const size_t smem = (size_t)6 * K * kTensTile * kTensLd * sizeof(float);
+    const size_t smem = (size_t)(6 * K + (lap ? 2 : 0)) * kTensTile * kTensLd * sizeof(float);
     if (smem <= 200 * 1024) {
         static bool attr = false;
         if (!attr) {
@@ -353,12 +419,30 @@ cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, f
             attr = true;
         }
         dim3 grd((w + kTensTile - 1) / kTensTile, (h + kTensTile - 1) / kTensTile, n_frames);
-        k_tensor_tiled<<<grd, 256, smem, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g);
+        k_tensor_tiled<<<grd, 256, smem, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g, u, v, wx, wy, lap, lap_fs);
         return cudaGetLastError();
     }
     dim3 blk(128), grd((w + 127) / 128, h, n_frames);
     k_tensor<<<grd, blk, 0, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g);
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !lap) return e;
+    return launch_lap(u, v, n_frames, h, w, wx, wy, lap, lap_fs, g, st);
+}
+
+}  // namespace
+
+cudaError_t launch_tensor(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx,
+                          int gray, float* J, long long J_fs, DiagGeom g, cudaStream_t st)
+{
+    return run_tensor(f1, f2, n_frames, K, h, w, hy, hx, gray, J, J_fs, g, View{}, View{}, 0.0f, 0.0f, nullptr, 0,
+                      st);
+}
+
+cudaError_t launch_tensor_lap(View f1, View f2, int n_frames, int K, int h, int w, float hy, float hx, int gray,
+                              float* J, long long J_fs, DiagGeom g, View u, View v, float wx, float wy, float* lap,
+                              long long lap_fs, cudaStream_t st)
+{
+    return run_tensor(f1, f2, n_frames, K, h, w, hy, hx, gray, J, J_fs, g, u, v, wx, wy, lap, lap_fs, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -374,17 +458,8 @@ __global__ void k_lap(View u, View v, int h, int w, float wx, float wy, float* _
     const int y = blockIdx.y;
     const int f = blockIdx.z;
     if (x >= w) return;
-    const float* up = u.p + f * u.fs;
-    const float* vp = v.p + f * v.fs;
-#define U_(r, c) up[(long long)(r) * u.rs + (long long)(c) * u.cs]
-#define V_(r, c) vp[(long long)(r) * v.rs + (long long)(c) * v.cs]
-    const float uc = U_(y + 1, x + 1), vc = V_(y + 1, x + 1);
-    const float lu = wx * ((U_(y + 1, x) - uc) + (U_(y + 1, x + 2) - uc)) +
-                     wy * ((U_(y, x + 1) - uc) + (U_(y + 2, x + 1) - uc));
-    const float lv = wx * ((V_(y + 1, x) - vc) + (V_(y + 1, x + 2) - vc)) +
-                     wy * ((V_(y, x + 1) - vc) + (V_(y + 2, x + 1) - vc));
-#undef U_
-#undef V_
+    float lu, lv;
+    lap_at(u, v, f, y, x, wx, wy, lu, lv);
     const long long di = diag_index(g, y, x);
     const long long plane = (long long)g.D * g.P;
     lap[f * lap_fs + di] = lu;
@@ -766,6 +841,59 @@ __device__ float median25(float v[25])
     return t[12];
 }
 
+// Medians of two 25-element windows that share their first 20 elements
+// (vertically adjacent 5 x 5 windows: v[0..19] the four common rows, a[0..4]
+// and b[0..4] the rows only one window has).  Forgetful selection as in
+// median25: the rounds that only see common elements (the first 14, then
+// v[14..19]) run once for both windows; the last four rounds and the final
+// median of three run per window.  Each result is the median of its window.
+__device__ __forceinline__ void median25_pair(const float v[20], const float a[5], const float b[5], float& ma,
+                                              float& mb)
+{
+    float t[14];
+#pragma unroll
+    for (int i = 0; i < 14; ++i) t[i] = v[i];
+#pragma unroll
+    for (int round = 0; round < 7; ++round) {
+        const int lo = round;
+#pragma unroll
+        for (int i = lo + 1; i < 14; ++i) cswap(t[lo], t[i]);
+#pragma unroll
+        for (int i = lo + 1; i < 13; ++i) cswap(t[i], t[13]);
+        t[13] = round < 6 ? v[14 + round] : 0.0f;
+    }
+    // round 6 dropped t[6] and t[13]; t[7..12] are the shared survivors
+    float ta[14], tb[14];
+#pragma unroll
+    for (int i = 7; i < 13; ++i) ta[i] = tb[i] = t[i];
+    ta[13] = a[0];
+    tb[13] = b[0];
+#pragma unroll
+    for (int round = 7; round < 11; ++round) {
+        const int lo = round;
+#pragma unroll
+        for (int i = lo + 1; i < 14; ++i) {
+            cswap(ta[lo], ta[i]);
+            cswap(tb[lo], tb[i]);
+        }
+#pragma unroll
+        for (int i = lo + 1; i < 13; ++i) {
+            cswap(ta[i], ta[13]);
+            cswap(tb[i], tb[13]);
+        }
+        ta[13] = a[round - 6];
+        tb[13] = b[round - 6];
+    }
+    cswap(ta[11], ta[12]);
+    cswap(ta[12], ta[13]);
+    cswap(ta[11], ta[12]);
+    cswap(tb[11], tb[12]);
+    cswap(tb[12], tb[13]);
+    cswap(tb[11], tb[12]);
+    ma = ta[12];
+    mb = tb[12];
+}
+
 __global__ void k_median_accum(const float* __restrict__ du, const float* __restrict__ dv, long long st_fs,
                                View u, View v, DiagGeom g, int do_median, ViewW out_u, ViewW out_v)
 {
@@ -813,25 +941,27 @@ cudaError_t launch_median_accum(const float* du, const float* dv, long long st_f
     return cudaGetLastError();
 }
 
-// Median + accumulate on row-major du, dv (T, h, w): a 32 x 8 output tile with
-// its mirrored 2-pixel halo is staged in shared memory by coalesced row loads.
-constexpr int kMedTx = 32, kMedTy = 8;
+// Median + accumulate on row-major du, dv (T, h, w): a 32 x 16 output tile
+// with its mirrored 2-pixel halo is staged in shared memory by coalesced row
+// loads; each thread takes two vertically adjacent pixels, whose windows share
+// four of their five rows (median25_pair).
+constexpr int kMedTx = 32, kMedTy = 8, kMedRows = 2 * kMedTy;
 
 __global__ void __launch_bounds__(kMedTx * kMedTy) k_median_rm(const float* __restrict__ du,
                                                                const float* __restrict__ dv, long long fs, View u,
                                                                View v, int h, int w, int do_median, ViewW out_u,
                                                                ViewW out_v)
 {
-    __shared__ float su[kMedTy + 4][kMedTx + 4];
-    __shared__ float sv[kMedTy + 4][kMedTx + 4];
+    __shared__ float su[kMedRows + 4][kMedTx + 4];
+    __shared__ float sv[kMedRows + 4][kMedTx + 4];
     const int f = blockIdx.z;
-    const int x0 = blockIdx.x * kMedTx, y0 = blockIdx.y * kMedTy;
+    const int x0 = blockIdx.x * kMedTx, y0 = blockIdx.y * kMedRows;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * kMedTx + tx;
     const float* duf = du + f * fs;
     const float* dvf = dv + f * fs;
     if (do_median) {
-        for (int i = tid; i < (kMedTy + 4) * (kMedTx + 4); i += kMedTx * kMedTy) {
+        for (int i = tid; i < (kMedRows + 4) * (kMedTx + 4); i += kMedTx * kMedTy) {
             const int r = i / (kMedTx + 4), c = i - r * (kMedTx + 4);
             const int yy = mirror(min(y0 - 2 + r, h + 1), h);
             const int xx = mirror(min(x0 - 2 + c, w + 1), w);
@@ -840,34 +970,53 @@ __global__ void __launch_bounds__(kMedTx * kMedTy) k_median_rm(const float* __re
         }
         __syncthreads();
     }
-    const int x = x0 + tx, y = y0 + ty;
-    if (x >= w || y >= h) return;
-    float mu, mv;
+    const int x = x0 + tx, ya = y0 + 2 * ty, yb = ya + 1;
+    if (x >= w || ya >= h) return;
+    float mua, mva, mub, mvb;
     if (do_median) {
-        float a[25], b[25];
+        // window of ya: tile rows 2ty .. 2ty + 4; of yb: 2ty + 1 .. 2ty + 5
+        float c20[20], ea[5], eb[5];
 #pragma unroll
-        for (int dy = 0; dy < 5; ++dy)
+        for (int dy = 0; dy < 4; ++dy)
 #pragma unroll
-            for (int dx = 0; dx < 5; ++dx) {
-                a[dy * 5 + dx] = su[ty + dy][tx + dx];
-                b[dy * 5 + dx] = sv[ty + dy][tx + dx];
-            }
-        mu = median25(a);
-        mv = median25(b);
+            for (int dx = 0; dx < 5; ++dx) c20[dy * 5 + dx] = su[2 * ty + 1 + dy][tx + dx];
+#pragma unroll
+        for (int dx = 0; dx < 5; ++dx) {
+            ea[dx] = su[2 * ty][tx + dx];
+            eb[dx] = su[2 * ty + 5][tx + dx];
+        }
+        median25_pair(c20, ea, eb, mua, mub);
+#pragma unroll
+        for (int dy = 0; dy < 4; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 5; ++dx) c20[dy * 5 + dx] = sv[2 * ty + 1 + dy][tx + dx];
+#pragma unroll
+        for (int dx = 0; dx < 5; ++dx) {
+            ea[dx] = sv[2 * ty][tx + dx];
+            eb[dx] = sv[2 * ty + 5][tx + dx];
+        }
+        median25_pair(c20, ea, eb, mva, mvb);
     } else {
-        mu = duf[(long long)y * w + x];
-        mv = dvf[(long long)y * w + x];
+        mua = duf[(long long)ya * w + x];
+        mva = dvf[(long long)ya * w + x];
+        mub = yb < h ? duf[(long long)yb * w + x] : 0.0f;
+        mvb = yb < h ? dvf[(long long)yb * w + x] : 0.0f;
     }
-    const float uc = u.p[f * u.fs + (long long)(y + 1) * u.rs + (long long)(x + 1) * u.cs];
-    const float vc = v.p[f * v.fs + (long long)(y + 1) * v.rs + (long long)(x + 1) * v.cs];
-    out_u.p[f * out_u.fs + (long long)y * out_u.rs + (long long)x * out_u.cs] = uc + mu;
-    out_v.p[f * out_v.fs + (long long)y * out_v.rs + (long long)x * out_v.cs] = vc + mv;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int y = ya + q;
+        if (y >= h) break;
+        const float uc = u.p[f * u.fs + (long long)(y + 1) * u.rs + (long long)(x + 1) * u.cs];
+        const float vc = v.p[f * v.fs + (long long)(y + 1) * v.rs + (long long)(x + 1) * v.cs];
+        out_u.p[f * out_u.fs + (long long)y * out_u.rs + (long long)x * out_u.cs] = uc + (q ? mub : mua);
+        out_v.p[f * out_v.fs + (long long)y * out_v.rs + (long long)x * out_v.cs] = vc + (q ? mvb : mva);
+    }
 }
 
 cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
                              int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st)
 {
-    dim3 blk(kMedTx, kMedTy), grd((w + kMedTx - 1) / kMedTx, (h + kMedTy - 1) / kMedTy, n_frames);
+    dim3 blk(kMedTx, kMedTy), grd((w + kMedTx - 1) / kMedTx, (h + kMedRows - 1) / kMedRows, n_frames);
     k_median_rm<<<grd, blk, 0, st>>>(du, dv, fs, u, v, h, w, do_median, out_u, out_v);
     return cudaGetLastError();
 }
