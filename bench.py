@@ -6,10 +6,11 @@ the first 50 frames), with pyflowreg's default flow options (alpha 1.5,
 eta 0.8, 50 iterations, update_lag 5, a_data 0.45, gradient constancy,
 quality preset -> min_level 0, channel weights 0.5/0.5).
 
-Prints one JSON line.  ``value`` is frames/s with the batch resident in HBM;
-``e2e`` is the same through the public device API with the batch in pinned
-host memory and the flows copied back, copies inside the timed region (on a
-side stream, overlapping the neighbouring steps' compute).
+Prints one JSON line.  ``value`` is frames/s with the batch resident in HBM
+(the batch's frame ranges on the lanes of the cached plan, each lane running
+the steps on its own stream); ``e2e`` is the same with the batch in pinned
+host memory and the flows copied back, copies inside the timed region (one
+chunk per lane, on copy streams overlapping compute).
 ``--impl reference`` times the CPU oracle (a restatement of pyflowreg's
 numba path; pyflowreg itself cannot run here) on the host cores instead.
 
@@ -449,8 +450,29 @@ def run_gb300(args):
                   {"kernel": {0: "diagonal_ring", 1: "rows_in_registers", 2: "rows_in_registers_chained"}[v], "G": g,
                    "threads": t or plan.level_tuning()[i][3]}
                   for i, (v, g, t, _) in chosen.items()}
-    for _ in range(max(args.warmup, 3)):
-        plan.displacement(frames, None, out)
+    # The batch's frame ranges go to the plan's lanes (independent plans, each on
+    # its own stream), and each lane runs the steps one after the other without
+    # waiting for the other lanes at step boundaries: one lane's last wave of a
+    # level overlaps another lane's work, also across steps.  One lane per
+    # plan when the batch is small (or per rank under torchrun).
+    lane_plans = list(getattr(plan, "plans", [plan]))
+    lane_streams = list(getattr(plan, "streams", [stream]))
+    per_lane = -(-T // len(lane_plans))
+    lanes = [(lane_plans[i], lane_streams[i], i * per_lane, min(T, (i + 1) * per_lane))
+             for i in range(len(lane_plans)) if i * per_lane < T]
+
+    def run_steps(n):
+        start = torch.cuda.Event()
+        start.record(stream)
+        for lp, ls, t0, t1 in lanes:
+            ls.wait_event(start)
+        for _ in range(n):
+            for lp, ls, t0, t1 in lanes:
+                lp.displacement(frames[t0:t1], None, out[t0:t1], stream=ls)
+        for lp, ls, t0, t1 in lanes:
+            stream.wait_stream(ls)
+
+    run_steps(max(args.warmup, 3))
     torch.cuda.synchronize()
 
     lib = _lib.load()
@@ -462,8 +484,7 @@ def run_gb300(args):
     sampler.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
-        plan.displacement(frames, None, out)
+    run_steps(args.steps)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -509,42 +530,59 @@ def run_gb300(args):
         rcall_ms = ms / args.steps
 
     # e2e through the public API: every step uploads its batch from pinned host
-    # memory and reads its flows back into pinned host memory.  The copies run
-    # on a side stream and overlap the neighbouring steps' compute (two device
-    # slots, events between the streams), as a streaming caller does; the timed
-    # region runs from before the first upload to after the last read-back.
+    # memory and reads its flows back into pinned host memory.  The batch moves
+    # in one chunk per lane of the plan (the frame ranges the lanes register
+    # independently): a lane starts as soon as its chunk is on the device and
+    # its flows go back as soon as it is done, so only the first chunk's upload
+    # and the last chunk's read-back are not hidden behind compute.  Uploads and
+    # read-backs run on two copy streams (two device slots, events between the
+    # streams); the timed region runs from before the first upload to after the
+    # last read-back.
     host_in = frames.cpu().pin_memory()
     host_out = [torch.empty((T, H, W, 2), dtype=torch.float32).pin_memory() for _ in range(2)]
     dev_in = [torch.empty_like(frames) for _ in range(2)]
     dev_out = [torch.empty((T, H, W, 2), dtype=torch.float32, device=dev) for _ in range(2)]
-    comp_s, copy_s = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    lane_plans = list(getattr(plan, "plans", [plan]))
+    lane_streams = list(getattr(plan, "streams", [torch.cuda.Stream(device=dev)]))
+    n_ch = len(lane_plans)
+    per_ch = -(-T // n_ch)
+    chunks = [(i * per_ch, min(T, (i + 1) * per_ch)) for i in range(n_ch) if i * per_ch < T]
+    up_s, down_s = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
 
     def e2e_run(n_steps):
-        ev_in = [torch.cuda.Event() for _ in range(2)]
-        ev_comp = [torch.cuda.Event() for _ in range(2)]
-        ev_out = [torch.cuda.Event() for _ in range(2)]
+        ev = lambda: [[torch.cuda.Event() for _ in chunks] for _ in range(2)]  # noqa: E731
+        ev_in, ev_comp, ev_out = ev(), ev(), ev()
         e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e_start.record(copy_s)
-        with torch.cuda.stream(copy_s):
-            dev_in[0].copy_(host_in, non_blocking=True)
-            ev_in[0].record(copy_s)
+        e_start.record(up_s)
+        down_s.wait_event(e_start)
+
+        def upload(k):
+            sl = k & 1
+            with torch.cuda.stream(up_s):
+                for i, (t0, t1) in enumerate(chunks):
+                    if k >= 2:
+                        up_s.wait_event(ev_comp[sl][i])  # the lane of step k - 2 has consumed this slot
+                    dev_in[sl][t0:t1].copy_(host_in[t0:t1], non_blocking=True)
+                    ev_in[sl][i].record(up_s)
+
+        upload(0)
         for k in range(n_steps):
             sl = k & 1
-            comp_s.wait_event(ev_in[sl])
-            if k >= 2:
-                comp_s.wait_event(ev_out[sl])  # dev_out[sl] read back
-            G.get_displacement_device(ref, dev_in[sl], None, wt, out_t=dev_out[sl], stream=comp_s, **OPTIONS)
-            ev_comp[sl].record(comp_s)
-            with torch.cuda.stream(copy_s):
-                if k + 1 < n_steps:
-                    if k >= 1:
-                        copy_s.wait_event(ev_comp[sl ^ 1])  # dev_in[sl ^ 1] consumed
-                    dev_in[sl ^ 1].copy_(host_in, non_blocking=True)
-                    ev_in[sl ^ 1].record(copy_s)
-                copy_s.wait_event(ev_comp[sl])
-                host_out[sl].copy_(dev_out[sl], non_blocking=True)
-                ev_out[sl].record(copy_s)
-        e_end.record(copy_s)
+            if k + 1 < n_steps:
+                upload(k + 1)
+            for i, (t0, t1) in enumerate(chunks):
+                ls = lane_streams[i]
+                ls.wait_event(ev_in[sl][i])
+                if k >= 2:
+                    ls.wait_event(ev_out[sl][i])  # dev_out[sl] of this chunk read back
+                lane_plans[i].displacement(dev_in[sl][t0:t1], None, dev_out[sl][t0:t1], stream=ls)
+                ev_comp[sl][i].record(ls)
+                with torch.cuda.stream(down_s):
+                    down_s.wait_event(ev_comp[sl][i])
+                    host_out[sl][t0:t1].copy_(dev_out[sl][t0:t1], non_blocking=True)
+                    ev_out[sl][i].record(down_s)
+        up_s.wait_stream(down_s)
+        e_end.record(up_s)
         torch.cuda.synchronize()
         return e_start.elapsed_time(e_end)
 
@@ -637,12 +675,15 @@ def run_gb300(args):
                        "l2": "inputs larger than L2 (%.0f MB per step)" % (T * H * W * K * 4 / 1e6),
                        "parallelism": f"frames sharded over {world} GPU(s)",
                        "sor_launch_tuning": tuning,
-                       "lanes": f"{n_lanes} plans over contiguous parts of the batch, each on its own stream"
+                       "lanes": f"{n_lanes} plans over contiguous parts of the batch, each on its own stream, "
+                                "running the steps without a join between lanes at step boundaries"
                                 if n_lanes > 1 else "one plan"},
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": T * H * W * K * 4,
                     "d2h_bytes_per_step": T * H * W * 2 * 4,
-                    "copies": "pinned host buffers; uploads and read-backs on a side stream overlapping the "
-                              "neighbouring steps' compute; timed from the first upload to the last read-back"},
+                    "copies": "pinned host buffers; each step moves in one chunk per lane (uploads and read-backs "
+                              "on two copy streams overlapping compute); timed from the first upload to the last "
+                              "read-back",
+                    "api": "Plan.displacement of each lane of the cached plan (the get_displacement_device plan)"},
             "gpu_launches": int(launches),
             "roofline": roofline,
             "plain": plain,
