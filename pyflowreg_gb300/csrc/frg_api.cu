@@ -658,7 +658,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         L.g = make_geom(L.h, L.w);
         // the rows-in-registers SOR is the faster kernel wherever it serves (same bits as the
         // diagonal ring; levels taller than 512 rows run it as a cluster of row strips), with
-        // all passes of the level chained in one launch where one CTA holds the level
+        // all passes of the level chained in one launch
         L.sor_variant = sor_chain_supports(channels, L.g, 1) ? 2 : (sor_regs_supports(channels, L.g) ? 1 : 0);
         const double sig = resize_sigma(m, n, L.h, L.w);
         HostTables tx = make_tables(n, L.w, sig), ty = make_tables(m, L.h, sig);

@@ -100,9 +100,10 @@ cudaError_t launch_sor_regs(const float* J, long long J_fs, const float* W, long
 // k_sor_chain): a row starts its next pass as soon as it has finished the
 // current one, so the passes follow each other without restarting the
 // wavefront.  Pass p is the launch_sor_regs pass (G, mode, store_coef); the
-// level's last pass writes out_du/out_dv when given.  Single-CTA levels
-// (sor_regs_supports with P <= kMaxLane), w >= 3, at most kMaxChain passes;
-// bit-identical to one launch_sor_regs call per pass.
+// level's last pass writes out_du/out_dv when given.  Every level
+// launch_sor_regs serves (levels over 512 rows as clusters of row strips),
+// w >= 3, at most kMaxChain passes; bit-identical to one launch_sor_regs call
+// per pass.
 constexpr int kMaxChain = 64;
 struct ChainPass {
     int G, mode, store_coef;

@@ -556,7 +556,11 @@ __device__ __forceinline__ Coef fold_pk(const SorArgs& A, int pk, const Raw<K>& 
     return fold_m<K>(A, (pk & kPkTick) ? 2 : 0, r);
 }
 
-template <int K, int G, bool CO>
+// CL: the level's rows are cut into A.nc strips of NT rows, one CTA each, the
+// strips of a frame forming a thread-block cluster, exactly as k_sor_regs's
+// cluster form (edge rows through distributed shared memory, a cluster barrier
+// per step; every CTA runs the same step count).
+template <int K, int G, bool CO, bool CL>
 __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
 {
     extern __shared__ __align__(16) float sm[];
@@ -564,11 +568,14 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
     const DiagGeom g = A.g;
     const int P = g.P, h = g.h, w = g.w;
     const int NT = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, NW = NT >> 5;
-    const int f = (int)blockIdx.x;
-    const int r = t;
+    const int nc = CL ? A.nc : 1;
+    const int strip = CL ? (int)(blockIdx.x % nc) : 0;
+    const int f = CL ? (int)(blockIdx.x / nc) : (int)blockIdx.x;
+    const int r = strip * NT + t;  // the level row of this thread
     float4* C4 = reinterpret_cast<float4*>(sm);
     float* C1 = sm + 4 * S * NT;
     float2* X = reinterpret_cast<float2*>(C1 + S * NT);
+    float2* XE = X + 2 * NW * 2 * G;  // [par][0: row above the strip, 1: row below][gi]
     const int pl = g.D * P;
     const float* Jr = A.J + f * A.J_fs + r;
     const float* Wr = A.W + f * A.W_fs + r;
@@ -628,6 +635,13 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
         }
     };
     auto xs = [&](int par, int wp, int dir, int gi) -> float2& { return X[((par * NW + wp) * 2 + dir) * G + gi]; };
+    auto step_barrier = [&]() {
+        if constexpr (CL)
+            cooperative_groups::this_cluster().sync();
+        else
+            __syncthreads();
+    };
+    if constexpr (CL) step_barrier();  // every CTA of the cluster is running before any remote write
 
     // the row's current pass (of the update at tau = s - r): index, local start and
     // end, its flags and those of the next pass; the fold (tau + 1) and the prefetch
@@ -681,12 +695,14 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
                     up.x = __shfl_up_sync(0xffffffffu, V1[gi].x, 1);
                     up.y = __shfl_up_sync(0xffffffffu, V1[gi].y, 1);
                     if (lane == 0 && warp > 0) up = xs(pin, warp - 1, 0, gi);
+                    if (CL && t == 0 && strip > 0) up = XE[(pin * 2 + 0) * G + gi];
                     if (gi == 0) {
                         dn = dn1;
                     } else {
                         dn.x = __shfl_down_sync(0xffffffffu, V1[gi - 1].x, 1);
                         dn.y = __shfl_down_sync(0xffffffffu, V1[gi - 1].y, 1);
                         if (lane == 31 && warp < NW - 1) dn = xs(pin, warp + 1, 1, gi - 1);
+                        if (CL && t == NT - 1 && strip < nc - 1) dn = XE[(pin * 2 + 1) * G + gi - 1];
                     }
                     const int c = c0 - 2 * gi;
                     if (gi < Gp && row_ok && c >= 0 && c < w) {
@@ -720,6 +736,20 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
 #pragma unroll
                     for (int gi = 0; gi + 1 < G; ++gi) xs(pout, warp, 1, gi) = V0[gi];
                 }
+                if constexpr (CL) {
+                    // strip edges: the last row feeds the next strip's "up", the first row the
+                    // previous strip's "down", in the neighbouring CTA's shared memory
+                    if (t == NT - 1 && strip < nc - 1) {
+                        float2* dst = cooperative_groups::this_cluster().map_shared_rank(XE, strip + 1);
+#pragma unroll
+                        for (int gi = 0; gi < G; ++gi) dst[(pout * 2 + 0) * G + gi] = V0[gi];
+                    }
+                    if (t == 0 && strip > 0) {
+                        float2* dst = cooperative_groups::this_cluster().map_shared_rank(XE, strip - 1);
+#pragma unroll
+                        for (int gi = 0; gi + 1 < G; ++gi) dst[(pout * 2 + 1) * G + gi] = V0[gi];
+                    }
+                }
 #pragma unroll
                 for (int gi = 0; gi < G; ++gi) {
                     V2[gi] = V1[gi];
@@ -727,7 +757,7 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_chain(SorArgs A, ChainTable T)
                 }
                 slot0 = slot1;
             }
-            __syncthreads();
+            step_barrier();
         }
     }
 }
@@ -914,15 +944,41 @@ namespace {
 template <int K, int G, bool CO>
 cudaError_t run_chain_t(const SorArgs& A, const ChainTable& T, int n_frames, int nt, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemLimit);
-        if (e != cudaSuccess) return e;
-        attr = true;
+    if (A.nc == 1) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO, false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        k_sor_chain<K, G, CO, false><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A, T);
+        return cudaGetLastError();
     }
-    k_sor_chain<K, G, CO><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A, T);
-    return cudaGetLastError();
+    if constexpr (K <= 2) {
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO, true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(n_frames * A.nc));
+        cfg.blockDim = dim3((unsigned)nt);
+        cfg.dynamicSmemBytes = sor_regs_smem(G, nt);
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)A.nc;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_sor_chain<K, G, CO, true>, A, T);
+    } else {
+        return cudaErrorInvalidValue;
+    }
 }
 
 template <int K, bool CO>
@@ -952,7 +1008,7 @@ bool sor_chain_supports(int K, const DiagGeom& g, int n_passes)
 {
     // 32-bit offsets: the largest plane index read is (6K + 2) planes of D * P
     const long long plane = (long long)g.D * g.P;
-    return sor_regs_supports(K, g) && g.P <= kMaxLane && g.w >= 3 && n_passes >= 1 && n_passes <= kMaxChain &&
+    return sor_regs_supports(K, g) && g.w >= 3 && n_passes >= 1 && n_passes <= kMaxChain &&
            plane * (6 * K + 2) < 0x7fffffffLL && (long long)g.h * g.w < 0x7fffffffLL;
 }
 
@@ -962,7 +1018,10 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
                              const float* a_data, float wx, float wy, float omega, cudaStream_t st, float* out_du,
                              float* out_dv, long long out_fs)
 {
-    if (!sor_chain_supports(K, g, n_passes) || n_frames < 1) return cudaErrorInvalidValue;
+    int nc = 0, nt = 0;
+    regs_split(K, g, &nc, &nt);
+    if (!sor_chain_supports(K, g, n_passes) || n_frames < 1 || (long long)n_frames * nc > 0x7fffffffLL)
+        return cudaErrorInvalidValue;
     ChainTable T;
     T.n = n_passes;
     int gmax = 1;
@@ -977,10 +1036,10 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
         gmax = q.G > gmax ? q.G : gmax;
     }
     for (int p = n_passes; p < kMaxChain; ++p) T.pk[p] = 1 << 8;
-    const int nt = g.P;
     if (sor_regs_smem(gmax, nt) > (size_t)kSmemLimit) return cudaErrorInvalidValue;
     SorArgs A = make_args(J, J_fs, W, W_fs, lap, lap_fs, coef, coef_fs, du, dv, st_fs, K, g, gmax, 0, 0, a_data, wx,
                           wy, omega, out_du, out_dv, out_fs);
+    A.nc = nc;
     switch (K) {
         case 1: return run_chain<1>(A, T, co, gmax, n_frames, nt, st);
         case 2: return run_chain<2>(A, T, co, gmax, n_frames, nt, st);
