@@ -46,25 +46,6 @@ __global__ void k_resize_h(View src, int n_planes, int ih, int iw, float* __rest
     (void)iw;
 }
 
-// Vertical pass; with pad = 1 the output is the level array with a one-pixel
-// edge-replicated ring (add_boundary, core/optical_flow.py:48-70).
-__global__ void k_resize_v(const float* __restrict__ src, int n_planes, int ih, int ow, ViewW dst, int oh,
-                           int pad, const int32_t* __restrict__ iy, const float* __restrict__ wy, int P)
-{
-    const int xo = blockIdx.x * blockDim.x + threadIdx.x;
-    const int yo = blockIdx.y;
-    const int fp = blockIdx.z;
-    if (xo >= ow + 2 * pad) return;
-    const int x = clampi(xo - pad, 0, ow - 1);
-    const int y = clampi(yo - pad, 0, oh - 1);
-    const float* col = src + (long long)fp * ih * ow + x;
-    const int32_t* iyr = iy + (long long)y * P;
-    const float* wyr = wy + (long long)y * P;
-    float s = 0.0f;
-    for (int p = 0; p < P; ++p) s = fmaf(__ldg(col + (long long)iyr[p] * ow), wyr[p], s);
-    const int f = fp / n_planes, pl = fp - f * n_planes;
-    dst.p[f * dst.fs + pl * dst.ps + (long long)yo * dst.rs + (long long)xo * dst.cs] = s;
-}
 
 // Horizontal pass, row-block form: one block takes up to R input rows of one
 // frame (all planes) into shared memory with asynchronous 16-byte copies
@@ -174,11 +155,52 @@ cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw
     return cudaGetLastError();
 }
 
+// Vertical pass; with pad = 1 the output is the level array with a one-pixel
+// edge-replicated ring (add_boundary, core/optical_flow.py:48-70).  Four
+// output rows per thread: the four tap chains are independent, so each
+// thread keeps four sets of column loads in flight (one output per thread is
+// bound by the latency of its short chain).  The sum per output is the same
+// fmaf chain over the taps in order.
+constexpr int kRvRows = 4;
+
+__global__ void k_resize_v4(const float* __restrict__ src, int n_planes, int ih, int ow, ViewW dst, int oh, int pad,
+                            const int32_t* __restrict__ iy, const float* __restrict__ wy, int P)
+{
+    const int xo = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yo0 = blockIdx.y * kRvRows;
+    const int fp = blockIdx.z;
+    const int ohp = oh + 2 * pad;
+    if (xo >= ow + 2 * pad) return;
+    const int x = clampi(xo - pad, 0, ow - 1);
+    const float* col = src + (long long)fp * ih * ow + x;
+    const int32_t* iyr[kRvRows];
+    const float* wyr[kRvRows];
+#pragma unroll
+    for (int q = 0; q < kRvRows; ++q) {
+        const int y = clampi(min(yo0 + q, ohp - 1) - pad, 0, oh - 1);
+        iyr[q] = iy + (long long)y * P;
+        wyr[q] = wy + (long long)y * P;
+    }
+    float s[kRvRows];
+#pragma unroll
+    for (int q = 0; q < kRvRows; ++q) s[q] = 0.0f;
+    for (int p = 0; p < P; ++p) {
+#pragma unroll
+        for (int q = 0; q < kRvRows; ++q) s[q] = fmaf(__ldg(col + (long long)iyr[q][p] * ow), wyr[q][p], s[q]);
+    }
+    const int f = fp / n_planes, pl = fp - f * n_planes;
+#pragma unroll
+    for (int q = 0; q < kRvRows; ++q)
+        if (yo0 + q < ohp) dst.p[f * dst.fs + pl * dst.ps + (long long)(yo0 + q) * dst.rs + (long long)xo * dst.cs] = s[q];
+}
+
 cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih, int ow, ViewW dst,
                             int oh, int pad, const int32_t* iy, const float* wy, int P, cudaStream_t st)
 {
-    dim3 blk(128), grd((ow + 2 * pad + 127) / 128, oh + 2 * pad, n_frames * n_planes);
-    k_resize_v<<<grd, blk, 0, st>>>(src, n_planes, ih, ow, dst, oh, pad, iy, wy, P);
+    const int owp = ow + 2 * pad, ohp = oh + 2 * pad;
+    const int bx = owp >= 96 ? 128 : (owp >= 48 ? 64 : 32);
+    dim3 blk(bx), grd((owp + bx - 1) / bx, (ohp + kRvRows - 1) / kRvRows, n_frames * n_planes);
+    k_resize_v4<<<grd, blk, 0, st>>>(src, n_planes, ih, ow, dst, oh, pad, iy, wy, P);
     return cudaGetLastError();
 }
 
@@ -356,7 +378,7 @@ __device__ __forceinline__ void lap_at(const View& u, const View& v, int f, int 
 constexpr int kTensTile = 32;
 constexpr int kTensLd = kTensTile + 2;
 
-__global__ void __launch_bounds__(256) k_tensor_tiled(View f1, View f2, int K, int h, int w, float hy, float hx,
+__global__ void __launch_bounds__(256, 3) k_tensor_tiled(View f1, View f2, int K, int h, int w, float hy, float hx,
                                                       int gray, float* __restrict__ J, long long J_fs, DiagGeom g,
                                                       View u, View v, float wx, float wy, float* __restrict__ lap,
                                                       long long lap_fs)
