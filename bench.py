@@ -60,6 +60,11 @@ def parse():
                     help="gradient modes timed in the differentiation workload")
     ap.add_argument("--uneven-frames", type=int, default=256,
                     help="frames of the uneven-size batch (sizes 256^2, 512^2, 796x512, 1024^2; 1-2 channels); 0 skips")
+    ap.add_argument("--stream-epe-frames", type=int, default=0,
+                    help="frames of the 2048x2048x2 stream compared with the CPU oracle (about a minute of host "
+                         "time per frame, one core each); 0 skips")
+    ap.add_argument("--stream-only", action="store_true",
+                    help="run only the 2048x2048x2 streaming workloads; prints their JSON object")
     ap.add_argument("--stream-frames", type=int, default=128,
                     help="frames of the 2048x2048x2 streaming workload (batches of 32); 0 skips")
     ap.add_argument("--no-autotune", action="store_true",
@@ -270,22 +275,60 @@ def run_stream(args, dev):
     opts.pop("min_level", None)
     sr = StreamRegistrar(refp, batch=B, **opts)
     sink_count = [0]
+    # frames compared with the oracle: one per batch after the first, at its middle; each
+    # batch after the first starts from the mean of the previous batch's last 20 flows
+    n_epe = max(0, min(args.stream_epe_frames, N // B - 1))
+    epe_t = [B * (i + 1) + B // 2 for i in range(n_epe)]
+    kept, w_next = {}, {}
 
     def sink(t0, flows):
         sink_count[0] += len(flows)
+        if n_epe:
+            w_next[t0 + len(flows)] = flows[max(0, len(flows) - 20):].mean(0)
+            for t in epe_t:
+                if t0 <= t < t0 + len(flows):
+                    kept[t] = (flows[t - t0].copy(), w_next.get(t0))
 
     sr.run(lambda t0, n: host[t0:t0 + n], min(N, 2 * B), sink)  # warm-up
     torch.cuda.synchronize()
+    kept.clear()
+    w_next.clear()
     t0 = time.perf_counter()
     info = sr.run(lambda t0, n: host[t0:t0 + n], N, sink)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     sr.close()
-    del host
     stream = {"workload": f"{N} x 2048x2048x2 frames, batches of {B}, pinned host in/out, copies on a side stream",
               "frames_per_s": N / dt, "seconds": dt, "h2d_bytes": info["h2d_bytes"], "d2h_bytes": info["d2h_bytes"],
               "timing": "wall clock around StreamRegistrar.run after a warm-up run"}
+    if n_epe:
+        stream["vs_oracle"] = stream_epe(refp, host, kept, OPTIONS)
+    del host
     return stream, run_compensate(raw_u16, ref_raw_np, B, opts)
+
+
+def stream_epe(refp, host, kept, options):
+    """fp32 flows of the 2048x2048x2 stream against the fp64 CPU oracle, one
+    frame per host thread, each from its batch's initial field."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    fx = refp.cpu().numpy().astype(np.float64)
+    ts = sorted(kept)
+
+    def one(t):
+        got, uv = kept[t]
+        want = O.get_displacement_batch(fx, host[t:t + 1].numpy().astype(np.float64), n_threads=1,
+                                        uv=None if uv is None else uv.astype(np.float64), **options)[0]
+        d = got.astype(np.float64) - want
+        return {"frame": t, "max_abs_px": float(np.abs(d).max()), "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean())}
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=len(ts)) as ex:
+        per = list(ex.map(one, ts))
+    return {"frames": per, "mean_epe_px": float(np.mean([p["mean_epe_px"] for p in per])),
+            "oracle": "fp64 lexicographic C oracle, one frame per host thread", "seconds": time.perf_counter() - t0}
 
 
 def run_compensate(raw_u16, ref_raw, B, opts):
@@ -799,6 +842,13 @@ def main():
 
         torch.cuda.set_device(0)
         print(json.dumps(run_diff(args, torch.device("cuda", 0))))
+        return
+    if args.stream_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        stream, comp = run_stream(args, torch.device("cuda", 0))
+        print(json.dumps({"stream_2048": stream, "compensate_2048": comp}))
         return
     if args.impl == "reference":
         run_reference(args)
