@@ -1284,7 +1284,8 @@ int frg_level_solve(int m, int n, int K, const float* J, const float* weight, co
                                 0, g, st));
         FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
         int r = solve_level(iterations, update_lag, Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, wx, wy,
-                            (float)omega, st, nullptr, nullptr, nullptr, 0, 0, 0, sor_regs_supports(K, g) ? 1 : 0);
+                            (float)omega, st, nullptr, nullptr, nullptr, 0, 0, 0,
+                            sor_chain_supports(K, g, 1) ? 2 : (sor_regs_supports(K, g) ? 1 : 0));
         if (r) return r;
         FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
         FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
