@@ -531,10 +531,12 @@ __global__ void __launch_bounds__(kMaxLane) k_sor_regs(SorArgs A)
 // a row's final value of pass p at (r, c) is stored at tau = start_p + c +
 // 2(G_p - 1) and read back for pass p + 1 at least w - 2 steps later (the
 // row below's value too, so past at least one barrier for w >= 3).
-// Three cursors follow the pass of the update (tau), of the coefficient fold
-// (tau + 1: the fold of the diagonal entering next step runs after this step's
-// updates, off their critical path) and of the prefetch (tau + 2).  The ring
-// slot of a pixel is its entry step mod (2G - 1), as in k_sor_regs.
+// Each row keeps one cursor, the pass of its updates (tau), with the flags of
+// that pass and the next; the coefficient fold (tau + 1: the fold of the
+// diagonal entering next step runs after this step's updates, off their
+// critical path) and the prefetch (tau + 2) fall in the one or the other,
+// since every span is at least 4.  The ring slot of a pixel is its entry step
+// mod (2G - 1), as in k_sor_regs.
 // Offsets within a frame are 32-bit (the host checks the plane sizes).
 // ---------------------------------------------------------------------------
 // Pass table: one packed word per pass, G << 8 | store << 3 | coef << 2 |
