@@ -239,6 +239,17 @@ int frg_motion_tensor(int h, int w, const float* f1, const float* f2, double hy,
 
 /* 5x5 median with mirror boundary of one plane (h, w), h, w >= 3. */
 int frg_median5(int h, int w, const float* src, float* dst, void* stream);
+/* The same in float64, as the reference filters du and dv (float64 arrays):
+ * the selection the float64 level loop uses, exact (ties included). */
+int frg_median5_f64(int h, int w, const double* src, double* dst, void* stream);
+
+/* out[i] = x[i]^b (n doubles, device memory) by the power function of the
+ * float64 solver's data-term nonlinearity psi = a (E + 1e-5)^(a - 1)
+ * (core/level_solver.py:247, `(val + 0.00001) ** (a_data[k] - 1.0)`): a
+ * table-driven log2 / exp2 within a few ulp of the correctly rounded power
+ * for positive normal x.  Exported so that its accuracy can be tested on its
+ * own. */
+int frg_pow_f64(long long n, const double* x, double b, double* out, void* stream);
 
 /* Preprocessing of frames before the flow, as compensate_recording does it
  * (motion_correction/compensate_recording.py:521-561, normalize and

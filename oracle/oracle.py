@@ -36,12 +36,32 @@ ORDER_LEXICOGRAPHIC = 0
 ORDER_RED_BLACK = 1
 
 
+_VARIANTS = {"portable": _LIB_PATH,
+             "native": os.path.join(_HERE, "_build", "liboracle_native.so"),
+             "fastmath": os.path.join(_HERE, "_build", "liboracle_fastmath.so")}
+_variant_libs = {}
+
+
 def build(force: bool = False) -> str:
     """Compile the C oracle (gcc) and return the path of the shared library."""
     src = os.path.join(_HERE, "flowreg_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["bash", os.path.join(_HERE, "build_oracle.sh")])
+    script = os.path.join(_HERE, "build_oracle.sh")
+    stale = any(not os.path.exists(p) or os.path.getmtime(p) < max(os.path.getmtime(src), os.path.getmtime(script))
+                for p in _VARIANTS.values())
+    if force or stale:
+        subprocess.check_call(["bash", script])
     return _LIB_PATH
+
+
+def build_flags() -> dict:
+    """Compiler and flags of the timed builds ("native", "fastmath")."""
+    build()
+    out = {}
+    with open(os.path.join(_HERE, "_build", "flags.txt")) as f:
+        for line in f:
+            k, _, v = line.partition(":")
+            out[k.strip()] = v.strip()
+    return out
 
 
 class _Level(ctypes.Structure):
@@ -69,28 +89,42 @@ class _Params(ctypes.Structure):
     ]
 
 
-def lib():
+def lib(variant: str = "portable"):
+    """The checker ("portable") or one of the timed builds ("native",
+    "fastmath"), see build_oracle.sh."""
     global _lib
+    if variant != "portable":
+        if variant not in _variant_libs:
+            build()
+            v = ctypes.CDLL(_VARIANTS[variant])
+            _declare(v)
+            _variant_libs[variant] = v
+        return _variant_libs[variant]
     if _lib is None:
         path = build()
         _lib = ctypes.CDLL(path)
-        P = ctypes.c_void_p
-        I, D = ctypes.c_int, ctypes.c_double
-        _lib.orc_displacement.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
-        _lib.orc_displacement_gnc.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
-        _lib.orc_displacement_batch.argtypes = [I, I, I, I, P, P, P, P, I, P, P, P, I, I, P, I]
-        _lib.orc_resize_plane.argtypes = [P, I, I, P, I, I, P, P, I, P, P, I, P, I]
-        _lib.orc_resize_plane.restype = None
-        _lib.orc_warp_plane.argtypes = [P, P, P, P, I, I, I, P]
-        _lib.orc_warp_plane.restype = None
-        _lib.orc_motion_tensor.argtypes = [P, P, I, I, D, D, I, I, P, P, P, P, P, P]
-        _lib.orc_compute_flow.argtypes = [P, P, P, P, P, P, P, P, P, I, I, I, D, D, I, I, P, D,
-                                          D, D, I, D, D, P, P]
-        _lib.orc_median5_plane.argtypes = [P, I, I, P]
-        _lib.orc_median5_plane.restype = None
-        _lib.orc_cubic_table.argtypes = [P]
-        _lib.orc_cubic_table.restype = None
+        _declare(_lib)
     return _lib
+
+
+def _declare(lib_):
+    """ctypes signatures of the oracle's C entry points."""
+    P = ctypes.c_void_p
+    I, D = ctypes.c_int, ctypes.c_double
+    lib_.orc_displacement.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
+    lib_.orc_displacement_gnc.argtypes = [I, I, I, P, P, P, P, I, P, P, P, P]
+    lib_.orc_displacement_batch.argtypes = [I, I, I, I, P, P, P, P, I, P, P, P, I, I, P, I]
+    lib_.orc_resize_plane.argtypes = [P, I, I, P, I, I, P, P, I, P, P, I, P, I]
+    lib_.orc_resize_plane.restype = None
+    lib_.orc_warp_plane.argtypes = [P, P, P, P, I, I, I, P]
+    lib_.orc_warp_plane.restype = None
+    lib_.orc_motion_tensor.argtypes = [P, P, I, I, D, D, I, I, P, P, P, P, P, P]
+    lib_.orc_compute_flow.argtypes = [P, P, P, P, P, P, P, P, P, I, I, I, D, D, I, I, P, D,
+                                      D, D, I, D, D, P, P]
+    lib_.orc_median5_plane.argtypes = [P, I, I, P]
+    lib_.orc_median5_plane.restype = None
+    lib_.orc_cubic_table.argtypes = [P]
+    lib_.orc_cubic_table.restype = None
 
 
 def _p(a: np.ndarray):
@@ -470,8 +504,10 @@ def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, m
 def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), update_lag=5,
                            iterations=50, min_level=0, levels=50, eta=0.8, a_smooth=1.0,
                            a_data=0.45, const_assumption="gc", uv=None, weight=None,
-                           order=ORDER_LEXICOGRAPHIC, omega=1.95):
-    """Many moving frames (T, H, W[, K]) against one fixed frame, OpenMP over frames."""
+                           order=ORDER_LEXICOGRAPHIC, omega=1.95, variant="portable"):
+    """Many moving frames (T, H, W[, K]) against one fixed frame, OpenMP over
+    frames.  variant: "portable" (the checker), or a timed build ("native",
+    "fastmath"; see build_oracle.sh)."""
     moving_frames = np.asarray(moving_frames)
     fixed3, m0, weight, a_data_arr = normalize_inputs(fixed, moving_frames[0], weight, a_data)
     m, n, K = fixed3.shape
@@ -484,7 +520,7 @@ def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), u
     oh, ow = plan.out_hw
     out = np.empty((T, oh, ow, 2), np.float64)
     nt = int(n_threads or os.cpu_count() or 1)
-    rc = lib().orc_displacement_batch(T, m, n, K, _p(np.ascontiguousarray(fixed3)), _p(mov), _p(weight),
+    rc = lib(variant).orc_displacement_batch(T, m, n, K, _p(np.ascontiguousarray(fixed3)), _p(mov), _p(weight),
                                       None if uvd is None else _p(uvd), len(plan.sched),
                                       ctypes.byref(plan.levels), _p(a_data_arr), ctypes.byref(prm),
                                       oh, ow, _p(out), nt)

@@ -19,7 +19,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libflowreg_gb300.so")
-SOURCES = ["frg_kernels.cu", "frg_sor.cu", "frg_exact.cu", "frg_diff.cu", "frg_prep.cu", "frg_api.cu",
+SOURCES = ["frg_kernels.cu", "frg_sor.cu", "frg_sor64.cu", "frg_exact.cu", "frg_diff.cu", "frg_prep.cu", "frg_api.cu",
            "frg_diff_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -11,10 +11,11 @@
 
 #include <algorithm>
 #include <atomic>
-#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -223,19 +224,23 @@ void upsample_tables(int in_len, int out_len, std::vector<int32_t>& s0, std::vec
     }
 }
 
+// The tables live in __constant__ memory, which every device holds separately:
+// uploaded once per device, under a lock (plans may be created from several
+// threads).
 int ensure_remap_tables()
 {
-    static bool done = false;
+    static std::mutex mu;
+    static std::set<int> done;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return fail(FRG_ECUDA, "no CUDA device");
-    static int done_dev = -1;
-    if (done && done_dev == dev) return FRG_OK;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(dev)) return FRG_OK;
     float cub[128], lin[64];
     remap_tables(cub, lin);
     FRG_CUDA(upload_cubic_table(cub, lin));
     FRG_CUDA(upload_cubic_table_x(cub));
-    done = true;
-    done_dev = dev;
+    FRG_CUDA(upload_dpow_tables());
+    done.insert(dev);
     return FRG_OK;
 }
 
@@ -269,6 +274,9 @@ struct LevelPlan {
     float* ref = nullptr;    // (K, h, w) reference level
     float* wdiag = nullptr;  // (K, D*P) weight level, diagonal-major
     double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
+    double* wdiag64 = nullptr;  // (K, D*P) the same, diagonal-major, for the float64 chained SOR
+    double* ref64 = nullptr;    // (K, h, w) reference level in float64, for its tensor
+    bool chain64 = false;       // fp64 plan: this level runs the float64 chained SOR
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
     int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
     int sor_variant = 0;  // fused SOR kernel: 0 diagonal ring in shared memory, 1 rows with the state in registers
@@ -283,9 +291,11 @@ struct Pass {
     int fold_mode;  // -1: no fold; else bit0 zero-init, bit1 psi from (du, dv)
 };
 
-std::vector<Pass> make_passes(int iterations, int update_lag, int gmax = kGMax)
+// Writes the passes into out[0, cap) (out may be NULL) and returns how many
+// there are; allocates nothing.
+int fill_passes(int iterations, int update_lag, int gmax, Pass* out, int cap)
 {
-    std::vector<Pass> out;
+    int n = 0;
     int t = 0;
     while (t < iterations) {
         const bool tick = ((t + 1) % update_lag) == 0;
@@ -293,14 +303,38 @@ std::vector<Pass> make_passes(int iterations, int update_lag, int gmax = kGMax)
         while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
         int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
         for (int s = t; s < end; s += gmax) {
-            Pass p;
-            p.G = std::min(gmax, end - s);
-            p.fold_mode = (s == t) ? mode : -1;
-            out.push_back(p);
+            if (out && n < cap) {
+                out[n].G = std::min(gmax, end - s);
+                out[n].fold_mode = (s == t) ? mode : -1;
+            }
+            ++n;
         }
         t = end;
     }
+    return n;
+}
+
+std::vector<Pass> make_passes(int iterations, int update_lag, int gmax = kGMax)
+{
+    std::vector<Pass> out((size_t)fill_passes(iterations, update_lag, gmax, nullptr, 0));
+    fill_passes(iterations, update_lag, gmax, out.data(), (int)out.size());
     return out;
+}
+
+// Chain table of a level's passes (every pass in one k_sor_chain launch): a
+// group's first pass stores its folded coefficients when the group continues
+// in further passes, which read them back.  Returns the iterations summed.
+int chain_passes(const Pass* ps, int n, ChainPass* cp)
+{
+    int its = 0;
+    for (int pi = 0; pi < n; ++pi) {
+        const bool continued = pi + 1 < n && ps[pi + 1].fold_mode < 0;
+        cp[pi].G = ps[pi].G;
+        cp[pi].mode = ps[pi].fold_mode;
+        cp[pi].store_coef = (ps[pi].fold_mode >= 0 && continued) ? 1 : 0;
+        its += ps[pi].G;
+    }
+    return its;
 }
 
 // CUDA-event timing of every SOR launch, enabled by frg_plan_set_profiling.
@@ -355,6 +389,14 @@ struct frg_plan {
     double* xtmp = nullptr;   // fp64 width-pass buffer (T, 2, h_min, W)
     // a_smooth != 1, the census data term and GNC stages run on the reference-order kernels in both precisions
     bool xpath = false;       // precision == FRG_FP64_REFERENCE, a_smooth != 1, census or GNC
+    // FP64 plans with a_smooth = 1, gradient or gray-value constancy and no GNC: the
+    // levels the float64 chained SOR serves run it on diagonal-major float64 buffers
+    bool dpath = false;
+    double* dJ = nullptr;     // (T, 6, K, D*P)
+    double* dlap = nullptr;   // (T, 2, D*P)
+    double* dcoef = nullptr;  // (T, 5, D*P)
+    double* ddu = nullptr;    // (T, D*P)
+    double* ddv = nullptr;    // (T, D*P)
     double* xpsis = nullptr;  // (T, m*n) smoothness weights
     double* xsnap = nullptr;  // (T, 2, m*n) state snapshot for the psi_s border
     double* xflow = nullptr;  // (T, H, W, 2) fp64 flow of an fp32 plan on this path
@@ -458,14 +500,7 @@ int solve_level(int iterations, int update_lag, const float* J, long long J_fs, 
     if (regs && tune_variant == 2 && sor_chain_supports(K, g, (int)passes.size())) {
         // every pass in one launch; same arguments per pass as the loop below
         std::vector<ChainPass> cp(passes.size());
-        double its = 0.0;
-        for (size_t pi = 0; pi < passes.size(); ++pi) {
-            const bool continued = pi + 1 < passes.size() && passes[pi + 1].fold_mode < 0;
-            cp[pi].G = passes[pi].G;
-            cp[pi].mode = passes[pi].fold_mode;
-            cp[pi].store_coef = (passes[pi].fold_mode >= 0 && continued) ? 1 : 0;
-            its += passes[pi].G;
-        }
+        const double its = chain_passes(passes.data(), (int)passes.size(), cp.data());
         const bool timed = prof && prof->on;
         if (timed) {
             int rc = record_event(prof, st);
@@ -622,6 +657,10 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
     pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0 ||
                 params->const_assumption == 2 || params->gnc_stages != 0;
+    pl->dpath = params->precision == FRG_FP64_REFERENCE && params->a_smooth == 1.0 &&
+                params->const_assumption != 2 && params->gnc_stages == 0;
+    const int n_passes = fill_passes(params->iterations, params->update_lag, kGMax, nullptr, 0);
+    size_t max_dp64 = 0;
 
     // schedule: core/optical_flow.py:494-518
     const int m = height, n = width;
@@ -674,6 +713,15 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         else
             rc = dev_alloc(pl, &L.wdiag, (size_t)channels * L.g.D * L.g.P);
         if (rc) { frg_plan_destroy(pl); return rc; }
+        L.chain64 = pl->dpath && sor_chain64_supports(channels, L.g, n_passes);
+        if (L.chain64) {
+            if ((rc = dev_alloc(pl, &L.wdiag64, (size_t)channels * L.g.D * L.g.P)) ||
+                (rc = dev_alloc(pl, &L.ref64, (size_t)channels * L.h * L.w))) {
+                frg_plan_destroy(pl);
+                return rc;
+            }
+            max_dp64 = std::max(max_dp64, (size_t)L.g.D * L.g.P);
+        }
         max_dp = std::max(max_dp, (size_t)L.g.D * L.g.P);
         max_hw = std::max(max_hw, (size_t)L.h * L.w);
         max_pad = std::max(max_pad, (size_t)(L.h + 2) * (L.w + 2));
@@ -734,6 +782,13 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             return rc;
         }
         for (int k = 0; k < channels; ++k) pl->a_data64[k] = params->a_data[k];
+        if (max_dp64 > 0 &&
+            ((rc = dev_alloc(pl, &pl->dJ, T * 6 * K * max_dp64)) || (rc = dev_alloc(pl, &pl->dlap, T * 2 * max_dp64)) ||
+             (rc = dev_alloc(pl, &pl->dcoef, T * 5 * max_dp64)) || (rc = dev_alloc(pl, &pl->ddu, T * max_dp64)) ||
+             (rc = dev_alloc(pl, &pl->ddv, T * max_dp64)))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
     } else {
         if ((rc = dev_alloc(pl, &pl->J, T * 6 * K * max_dp)) || (rc = dev_alloc(pl, &pl->lap, T * 2 * max_dp)) ||
             (rc = dev_alloc(pl, &pl->coef, T * 5 * max_dp)) || (rc = dev_alloc(pl, &pl->du, T * max_dp)) ||
@@ -913,6 +968,10 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
                                            L.img.wx, L.img.P, st));
             FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, 1, K, H, L.w, L.wpad64, 0, mn, L.w + 2, L.h, 2, L.img.iy,
                                            L.img.wy, L.img.P, st));
+            if (L.chain64) {
+                FRG_LAUNCH(launch_x_pad_to_diag(L.wpad64, K, L.h, L.w, L.g, L.wdiag64, st));
+                FRG_LAUNCH(launch_x_to_double(L.ref, (long long)K * hw, L.ref64, st));
+            }
         }
         pl->has_ref = true;
         return FRG_OK;
@@ -1179,13 +1238,41 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
                                      pl->warped, st));
             img2 = pl->warped;
         }
-        FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1, pl->p.const_assumption,
-                                   pl->xJ, st));
-        if (pl->p.a_smooth == 1.0) {
+        if (L.chain64) {
+            // float64 chained SOR on diagonal-major buffers; the level's last pass writes
+            // du, dv into the interiors of the padded xdu, xdv for the median
+            const long long dp = (long long)L.g.D * L.g.P;
+            const double wx = L.alpha_x / (L.h_col * L.h_col), wy = L.alpha_y / (L.h_row * L.h_row);
+            FRG_LAUNCH(launch_x_tensor_diag(L.ref64, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
+                                            pl->p.const_assumption, pl->dJ, 6LL * K * dp, L.g, pl->xuv, pl->xuv + mn,
+                                            uv_fs, wx, wy, pl->dlap, 2 * dp, st));
+            Pass ps[kMaxChain];
+            ChainPass cp[kMaxChain];
+            const int np = fill_passes(pl->p.iterations, pl->p.update_lag, kGMax, ps, kMaxChain);
+            const int its = chain_passes(ps, np, cp);
+            const bool timed = pl->prof.on;
+            if (timed) {
+                int rc = record_event(&pl->prof, st);
+                if (rc) return rc;
+            }
+            FRG_LAUNCH(launch_sor_chain64(pl->dJ, 6LL * K * dp, L.wdiag64, 0, pl->dlap, 2 * dp, pl->dcoef, 5 * dp,
+                                          pl->ddu, pl->ddv, dp, T, K, L.g, cp, np, pl->a_data64, wx, wy, pl->p.omega,
+                                          st, pl->xdu + (w + 2) + 1, pl->xdv + (w + 2) + 1, mn, w + 2));
+            if (timed) {
+                int rc = record_event(&pl->prof, st);
+                if (rc) return rc;
+                pl->prof.bytes += 72.0 * its * (double)T * h * w;
+                pl->prof.launches += 1;
+            }
+        } else if (pl->p.a_smooth == 1.0) {
+            FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
+                                       pl->p.const_assumption, pl->xJ, st));
             FRG_LAUNCH(launch_x_sor(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv, pl->xwp, T, K,
                                     h, w, L.alpha_x, L.alpha_y, L.h_col, L.h_row, pl->p.iterations,
                                     pl->p.update_lag, pl->a_data64, pl->p.omega, -1.0, st));
         } else {
+            FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
+                                       pl->p.const_assumption, pl->xJ, st));
             long long n_launch = 0;
             cudaError_t e = launch_x_sor_smooth(pl->xJ, L.wpad64, pl->xuv, pl->xuv + mn, uv_fs, pl->xdu, pl->xdv,
                                                 pl->xwp, pl->xpsis, pl->xsnap, T, K, h, w, L.alpha_x, L.alpha_y,
@@ -1228,6 +1315,15 @@ int frg_get_displacement_f64(frg_plan* pl, int T, const float* moving, const flo
     if (pl->p.precision != FRG_FP64_REFERENCE)
         return fail(FRG_EINVAL, "this plan computes in fp32: use frg_get_displacement");
     return run_xpath(pl, T, moving, uv_init, flow_out, (cudaStream_t)stream);
+}
+
+int frg_pow_f64(long long n, const double* x, double b, double* out, void* stream)
+{
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(FRG_EINVAL, "bad argument");
+    int rc = ensure_remap_tables();
+    if (rc) return rc;
+    FRG_LAUNCH(launch_pow64(n, x, b, out, (cudaStream_t)stream));
+    return FRG_OK;
 }
 
 int frg_imregister(int n_frames, int height, int width, int channels, const float* frames, const float* flow,
@@ -1391,7 +1487,6 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
     if (a_smooth != 1.0) return fail(FRG_EUNSUPPORTED, "a_smooth != 1 is not supported by the GB300 backend");
     const int h = m - 2, w = n - 2;
     DiagGeom g = make_geom(h, w);
-    if (g.P > kMaxLane) return fail(FRG_EUNSUPPORTED, "levels taller than 512 rows are not supported yet");
     const long long dp = (long long)g.D * g.P;
     const size_t elems = (size_t)(6 * K + K + 2 + 5 + 2) * (size_t)dp;
     if (elems > kNoAllocFloats)
@@ -1419,34 +1514,47 @@ int frg_level_solve_noalloc(int m, int n, int K, const float* J, const float* we
     FRG_LAUNCH(launch_to_diag(view(weight + (n + 1) * (long long)K, 0, 1, (long long)n * K, K), 1, K, h, w, Wd, 0, g,
                               st));
     FRG_LAUNCH(launch_lap(view(u, 0, 0, n, 1), view(v, 0, 0, n, 1), 1, h, w, wx, wy, lap, 2 * dp, g, st));
-    // the passes of make_passes, generated in place (no host container), run
-    // with the same kernels as solve_level uses for frg_level_solve
-    const bool fused = sor_fused_supports(K);
+    // The kernels frg_level_solve runs for the same level (solve_level with the
+    // variant it picks), so both give the same bits, with the passes generated
+    // into stack arrays instead of host containers: the chained SOR (K <= 4,
+    // at most kMaxChain passes), else the rows-in-registers SOR pass by pass
+    // (K <= 4), else (K > 4) the fold kernel at each group start and the
+    // row-per-thread SOR.  Every level within the scratch limit has at most
+    // 512 rows (one of 513 rows needs over 8 MiB at any K); the global-memory
+    // wavefront below only keeps the branch complete.
     const bool regs = sor_regs_supports(K, g);
-    for (int t = 0; t < iterations;) {
-        const bool tick = ((t + 1) % update_lag) == 0;
-        int end = t + 1;
-        while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
-        const int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
-        for (int s = t; s < end; s += kGMax) {
-            const int G = std::min(kGMax, end - s);
-            const int pass_mode = s == t ? mode : -1;
-            if (regs) {
-                const int store = (s == t && s + kGMax < end) ? 1 : 0;
-                FRG_LAUNCH(launch_sor_regs(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode, store, ad,
-                                           wx, wy, (float)omega, st));
-            } else if (fused) {
-                const int store = (s == t && s + kGMax < end) ? 1 : 0;
-                FRG_LAUNCH(launch_sor_fused(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode, store,
-                                            ad, wx, wy, (float)omega, st));
-            } else {
-                if (pass_mode >= 0)
-                    FRG_LAUNCH(launch_fold(Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, pass_mode, wx, wy,
-                                           st));
-                FRG_LAUNCH(launch_sor(coef, 0, dud, dvd, 0, 1, g, G, wy, wx, (float)omega, st));
+    Pass ps[kMaxChain];
+    const int n_passes = fill_passes(iterations, update_lag, kGMax, ps, kMaxChain);
+    if (n_passes <= kMaxChain && sor_chain_supports(K, g, n_passes)) {
+        ChainPass cp[kMaxChain];
+        chain_passes(ps, n_passes, cp);
+        FRG_LAUNCH(launch_sor_chain(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, cp, n_passes, ad, wx, wy,
+                                    (float)omega, st, nullptr, nullptr, 0));
+    } else {
+        for (int t = 0; t < iterations;) {
+            const bool tick = ((t + 1) % update_lag) == 0;
+            int end = t + 1;
+            while (end < iterations && ((end + 1) % update_lag) != 0) ++end;
+            const int mode = (t == 0 ? 1 : 0) | (tick ? 2 : 0);
+            for (int s = t; s < end; s += kGMax) {
+                const int G = std::min(kGMax, end - s);
+                const int pass_mode = s == t ? mode : -1;
+                if (regs) {
+                    const int store = (s == t && s + kGMax < end) ? 1 : 0;
+                    FRG_LAUNCH(launch_sor_regs(Jd, 0, Wd, 0, lap, 0, coef, 0, dud, dvd, 0, 1, K, g, G, pass_mode,
+                                               store, ad, wx, wy, (float)omega, st));
+                } else {
+                    if (pass_mode >= 0)
+                        FRG_LAUNCH(launch_fold(Jd, 0, Wd, 0, lap, 0, dud, dvd, 0, coef, 0, 1, K, g, ad, pass_mode, wx,
+                                               wy, st));
+                    if (g.P <= kMaxLane)
+                        FRG_LAUNCH(launch_sor(coef, 0, dud, dvd, 0, 1, g, G, wy, wx, (float)omega, st));
+                    else
+                        FRG_LAUNCH(launch_sor_global(coef, 0, dud, dvd, 0, 1, g, G, wy, wx, (float)omega, st));
+                }
             }
+            t = end;
         }
-        t = end;
     }
     FRG_LAUNCH(launch_from_diag(dud, 0, 1, 1, g, vieww(du, 0, 0, n, 1), 1, 2, st));
     FRG_LAUNCH(launch_from_diag(dvd, 0, 1, 1, g, vieww(dv, 0, 0, n, 1), 1, 2, st));
@@ -1533,6 +1641,13 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream)
     cudaError_t e = cudaFreeAsync(buf, st);
     if (rc == FRG_OK && e != cudaSuccess) return fail(FRG_ECUDA, cudaGetErrorString(e));
     return rc;
+}
+
+int frg_median5_f64(int h, int w, const double* src, double* dst, void* stream)
+{
+    if (!src || !dst || h < 3 || w < 3) return fail(FRG_EINVAL, "bad argument");
+    FRG_LAUNCH(launch_x_median5_plane(src, h, w, dst, (cudaStream_t)stream));
+    return FRG_OK;
 }
 
 }  // extern "C"

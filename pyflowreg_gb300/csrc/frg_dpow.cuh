@@ -1,0 +1,95 @@
+// Float64 power x^b for the data-term nonlinearity of the float64 solver,
+// psi = a (E + 1e-5)^(a - 1) (core/level_solver.py:247), in about 23 float64
+// operations instead of the ~100 the general pow costs on a float64 pipe that
+// runs at 1/64 of the float32 rate.
+//
+// Method: the table-driven logarithm and exponential of P. T. P. Tang
+// ("Table-driven implementation of the logarithm function in IEEE
+// floating-point arithmetic", ACM TOMS 16(4), 1990; "Table-driven
+// implementation of the exponential function ...", ACM TOMS 15(2), 1989),
+// in base 2, with the product b * log2(x) carried as a double-double:
+//   x = 2^e m, m in [1, 2); j = the top 8 bits of m's fraction;
+//   c_j = 1 + (j + 1/2) / 256, inv_j = double(1 / c_j), r = m inv_j - 1
+//     (one fused multiply-add, |r| <= 2^-9);
+//   log2 x = e - log2(inv_j) + log2(1 + r), log2(1 + r) by its Taylor series
+//     to r^6 (truncation below 2^-65); -log2(inv_j) is tabulated as
+//     Lhi + Llo with Lhi a multiple of 2^-42, so e + Lhi is exact;
+//   y = b log2 x = yh + yl (the product's rounding error kept by an fma);
+//   k = round(128 yh), f = yh - k / 128 + yl, |f| <= 2^-8;
+//   2^y = 2^(k >> 7) * 2^((k & 127) / 128) * (1 + q(f)), q the Taylor series
+//     of 2^f - 1 to f^5 (truncation below 2^-60).
+// Every step is one rounding of a value below the result's ulp except the
+// final two, so the result is within a few ulp of x^b.  Positive normal x
+// with |b log2 x| < 1000 take this path; anything else (0, denormals,
+// infinities, NaN, huge results) goes to pow().
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace frg {
+
+constexpr int kDpowLogN = 256;   // log table entries: (inv_j, Lhi - 1023, Llo)
+constexpr int kDpowExpN = 128;   // exp table entries: 2^(i / 128)
+
+// The tables (device memory of this translation unit; the library is built
+// without relocatable device code, so only frg_sor64.cu includes this header),
+// filled by upload_dpow_tables().
+__device__ double g_dpow_log[3 * kDpowLogN];
+__device__ double g_dpow_exp[kDpowExpN];
+
+// 1 / (i ln 2) with alternating signs: log2(1 + r) = sum_i (-1)^(i+1) r^i / (i ln 2)
+constexpr double kL1 = 1.4426950408889634074;
+constexpr double kL2 = -0.72134752044448170368;
+constexpr double kL3 = 0.48089834696298780245;
+constexpr double kL4 = -0.36067376022224085184;
+constexpr double kL5 = 0.28853900817779268147;
+constexpr double kL6 = -0.24044917348149390123;
+// (ln 2)^i / i!: 2^f - 1 = sum_i (f ln 2)^i / i!
+constexpr double kE1 = 0.69314718055994530942;
+constexpr double kE2 = 0.24022650695910071233;
+constexpr double kE3 = 0.055504108664821579953;
+constexpr double kE4 = 0.0096181291076284771620;
+constexpr double kE5 = 0.0013333558146428443423;
+
+__device__ __forceinline__ double dpow_tab(double x, double b)
+{
+    const int hi = __double2hiint(x);
+    const int lo = __double2loint(x);
+    if (hi < 0x00100000 || hi >= 0x7ff00000) return pow(x, b);  // not a positive normal finite number
+    const int eb = hi >> 20;                                     // biased exponent
+    const int j = (hi >> 12) & 0xff;
+    const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
+    const double* lt = g_dpow_log + 3 * j;
+    const double r = __fma_rn(m, __ldg(lt), -1.0);
+    double p = __fma_rn(r, kL6, kL5);
+    p = __fma_rn(r, p, kL4);
+    p = __fma_rn(r, p, kL3);
+    p = __fma_rn(r, p, kL2);
+    p = __fma_rn(r, p, kL1);
+    p = __dmul_rn(r, p);
+    const double ed = __dsub_rn(__hiloint2double(0x43300000, eb), 4503599627370496.0);  // eb as a double
+    const double lh = __dadd_rn(ed, __ldg(lt + 1));                                     // e + Lhi, exact
+    const double ll = __dadd_rn(__ldg(lt + 2), p);
+    const double yh = __dmul_rn(b, lh);
+    double yl = __fma_rn(b, lh, -yh);
+    yl = __fma_rn(b, ll, yl);
+    if (!(fabs(yh) < 1000.0)) return pow(x, b);
+    const double t = __fma_rn(yh, 128.0, 6755399441055744.0);  // 1.5 * 2^52: round(128 yh) in the low word
+    const int k = __double2loint(t);
+    const double kd = __dsub_rn(t, 6755399441055744.0);
+    double f = __fma_rn(kd, -0.0078125, yh);
+    f = __dadd_rn(f, yl);
+    double q = __fma_rn(f, kE5, kE4);
+    q = __fma_rn(f, q, kE3);
+    q = __fma_rn(f, q, kE2);
+    q = __fma_rn(f, q, kE1);
+    q = __dmul_rn(f, q);
+    const double E = __ldg(g_dpow_exp + (k & 127));
+    const double res = __fma_rn(E, q, E);
+    return __hiloint2double(__double2hiint(res) + (k >> 7) * 0x100000, __double2loint(res));
+}
+
+// Host: fills the tables on the current device (once per device).
+cudaError_t upload_dpow_tables();
+
+}  // namespace frg

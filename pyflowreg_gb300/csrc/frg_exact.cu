@@ -177,6 +177,138 @@ cudaError_t launch_x_warp(const float* f2, const float* f1, const double* u, con
 // f1: (K, h, w) float shared; f2: (T, K, h, w) float; J: (T, 6, K, m*n) double
 // with a zero ring.
 // ---------------------------------------------------------------------------
+// J11..J23 of channel k at padded position (yo, xo) (interior: 1..h, 1..w):
+// the oracle's arithmetic, operation by operation.
+__device__ __forceinline__ void tensor_px64(const float* __restrict__ f1, const float* __restrict__ f2, int f, int K,
+                                            int k, int h, int w, int yo, int xo, double hy, double hx, int f2_f32,
+                                            int gray, double* jo)
+{
+    const long long hw = (long long)h * w;
+    const double h2x = dmul(2.0, hx), h2y = dmul(2.0, hy), hxx = dmul(hx, hx), hyy = dmul(hy, hy);
+    const float h2x_f = (float)h2x, h2y_f = (float)h2y;
+    const float hxx_f = (float)hxx, hyy_f = (float)hyy;
+    const float* a = f1 + (long long)k * hw;
+    const float* b = f2 + ((long long)f * K + k) * hw;
+    // padded (yy, xx) -> unpadded clamp
+    auto A = [&](int yy, int xx) { return (double)a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+    auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+    // numpy.gradient of the padded arrays at an interior padded position
+    auto gx1 = [&](int yy, int xx) { return ddiv(dsub(A(yy, xx + 1), A(yy, xx - 1)), h2x); };
+    auto gy1 = [&](int yy, int xx) { return ddiv(dsub(A(yy + 1, xx), A(yy - 1, xx)), h2y); };
+    auto gx2 = [&](int yy, int xx) {
+        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), h2x_f);
+        return ddiv(dsub((double)Bf(yy, xx + 1), (double)Bf(yy, xx - 1)), h2x);
+    };
+    auto gy2 = [&](int yy, int xx) {
+        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), h2y_f);
+        return ddiv(dsub((double)Bf(yy + 1, xx), (double)Bf(yy - 1, xx)), h2y);
+    };
+    // fx, fy, ft re-padded from the interior: clamp the padded index to [1, h] x [1, w]
+    auto FX = [&](int yy, int xx) {
+        yy = xclamp(yy, 1, h);
+        xx = xclamp(xx, 1, w);
+        return dmul(0.5, dadd(gx1(yy, xx), gx2(yy, xx)));
+    };
+    auto FT = [&](int yy, int xx) {
+        yy = xclamp(yy, 1, h);
+        xx = xclamp(xx, 1, w);
+        return dsub((double)Bf(yy, xx), A(yy, xx));
+    };
+    double j11, j22, j33, j12, j13, j23;
+    if (gray == 2) {
+        // census (core/optical_flow.py:231-345): per neighbour offset the smoothed
+        // Heaviside of the directional difference, s = 0.5 (1 + r / sqrt(r^2 + eps^2)),
+        // edge-padded, differentiated centrally; float32 arithmetic on f2 when
+        // f2_f32 (Python-float constants cast to float32), float64 otherwise
+        const double eps = 0.1 / 255.0, eps2 = dmul(eps, eps);
+        const float eps2f = (float)eps2;
+        j11 = j22 = j33 = j12 = j13 = j23 = 0.0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                if (dy == 0 && dx == 0) continue;
+                const double ty = dmul(hy, (double)dy), tx = dmul(hx, (double)dx);
+                const double dist = __dsqrt_rn(dadd(dmul(ty, ty), dmul(tx, tx)));
+                const float dist_f = (float)dist;
+                // s at padded (yy, xx), the edge pad of the core (clamped into [1, h] x [1, w])
+                auto s1 = [&](int yy, int xx) {
+                    yy = xclamp(yy, 1, h);
+                    xx = xclamp(xx, 1, w);
+                    const double r = ddiv(dsub(A(yy + dy, xx + dx), A(yy, xx)), dist);
+                    return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
+                };
+                auto s2 = [&](int yy, int xx) {
+                    yy = xclamp(yy, 1, h);
+                    xx = xclamp(xx, 1, w);
+                    if (f2_f32) {
+                        const float r = __fdiv_rn(__fsub_rn(Bf(yy + dy, xx + dx), Bf(yy, xx)), dist_f);
+                        const float q = __fsqrt_rn(__fadd_rn(__fmul_rn(r, r), eps2f));
+                        return (double)__fmul_rn(0.5f, __fadd_rn(1.0f, __fdiv_rn(r, q)));
+                    }
+                    const double r = ddiv(dsub((double)Bf(yy + dy, xx + dx), (double)Bf(yy, xx)), dist);
+                    return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
+                };
+                const double sx1 = ddiv(dsub(s1(yo, xo + 1), s1(yo, xo - 1)), h2x);
+                const double sy1 = ddiv(dsub(s1(yo + 1, xo), s1(yo - 1, xo)), h2y);
+                double sx2, sy2;
+                if (f2_f32) {
+                    sx2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo, xo + 1), (float)s2(yo, xo - 1)), h2x_f);
+                    sy2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo + 1, xo), (float)s2(yo - 1, xo)), h2y_f);
+                } else {
+                    sx2 = ddiv(dsub(s2(yo, xo + 1), s2(yo, xo - 1)), h2x);
+                    sy2 = ddiv(dsub(s2(yo + 1, xo), s2(yo - 1, xo)), h2y);
+                }
+                const double sx = dmul(0.5, dadd(sx1, sx2)), sy = dmul(0.5, dadd(sy1, sy2));
+                const double st = dsub(s2(yo, xo), s1(yo, xo));
+                j11 = dadd(j11, dmul(sx, sx));
+                j22 = dadd(j22, dmul(sy, sy));
+                j33 = dadd(j33, dmul(st, st));
+                j12 = dadd(j12, dmul(sx, sy));
+                j13 = dadd(j13, dmul(sx, st));
+                j23 = dadd(j23, dmul(sy, st));
+            }
+        j11 = dmul(j11, 0.25); j22 = dmul(j22, 0.25); j33 = dmul(j33, 0.25);
+        j12 = dmul(j12, 0.25); j13 = dmul(j13, 0.25); j23 = dmul(j23, 0.25);
+    } else if (gray) {
+        const double fxv = FX(yo, xo);
+        const double fyv = dmul(0.5, dadd(gy1(yo, xo), gy2(yo, xo)));
+        const double ftv = FT(yo, xo);
+        j11 = dmul(fxv, fxv); j22 = dmul(fyv, fyv); j33 = dmul(ftv, ftv);
+        j12 = dmul(fxv, fyv); j13 = dmul(fxv, ftv); j23 = dmul(fyv, ftv);
+    } else {
+        const double fxy = ddiv(dsub(FX(yo + 1, xo), FX(yo - 1, xo)), h2y);
+        const double fxt = ddiv(dsub(FT(yo, xo + 1), FT(yo, xo - 1)), h2x);
+        const double fyt = ddiv(dsub(FT(yo + 1, xo), FT(yo - 1, xo)), h2y);
+        const double fxx1 = ddiv(dadd(dsub(A(yo, xo - 1), dmul(2.0, A(yo, xo))), A(yo, xo + 1)), hxx);
+        const double fyy1 = ddiv(dadd(dsub(A(yo - 1, xo), dmul(2.0, A(yo, xo))), A(yo + 1, xo)), hyy);
+        double fxx2, fyy2;
+        if (f2_f32) {
+            fxx2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)), hxx_f);
+            fyy2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)), hyy_f);
+        } else {
+            fxx2 = ddiv(dadd(dsub((double)Bf(yo, xo - 1), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo, xo + 1)), hxx);
+            fyy2 = ddiv(dadd(dsub((double)Bf(yo - 1, xo), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo + 1, xo)), hyy);
+        }
+        const double fxx = dmul(0.5, dadd(fxx1, fxx2));
+        const double fyy = dmul(0.5, dadd(fyy1, fyy2));
+        const double sx = __dsqrt_rn(dadd(dmul(fxx, fxx), dmul(fxy, fxy)));
+        const double sy = __dsqrt_rn(dadd(dmul(fxy, fxy), dmul(fyy, fyy)));
+        const double reg_x = ddiv(1.0, dadd(dmul(sx, sx), 1e-6));
+        const double reg_y = ddiv(1.0, dadd(dmul(sy, sy), 1e-6));
+        j11 = dadd(dmul(reg_x, dmul(fxx, fxx)), dmul(reg_y, dmul(fxy, fxy)));
+        j22 = dadd(dmul(reg_x, dmul(fxy, fxy)), dmul(reg_y, dmul(fyy, fyy)));
+        j33 = dadd(dmul(reg_x, dmul(fxt, fxt)), dmul(reg_y, dmul(fyt, fyt)));
+        j12 = dadd(dmul(dmul(reg_x, fxx), fxy), dmul(dmul(reg_y, fxy), fyy));
+        j13 = dadd(dmul(dmul(reg_x, fxx), fxt), dmul(dmul(reg_y, fxy), fyt));
+        j23 = dadd(dmul(dmul(reg_x, fxy), fxt), dmul(dmul(reg_y, fyy), fyt));
+    }
+    jo[0] = j11;
+    jo[1] = j22;
+    jo[2] = j33;
+    jo[3] = j12;
+    jo[4] = j13;
+    jo[5] = j23;
+}
+
 __global__ void kx_tensor(const float* __restrict__ f1, const float* __restrict__ f2, int K, int h, int w,
                           double hy, double hx, int f2_f32, int gray, double* __restrict__ J)
 {
@@ -186,142 +318,156 @@ __global__ void kx_tensor(const float* __restrict__ f1, const float* __restrict_
     const int n = w + 2, m = h + 2;
     if (xo >= n) return;
     const long long mn = (long long)m * n;
-    const long long hw = (long long)h * w;
     const long long o = (long long)yo * n + xo;
     const bool ring = xo == 0 || xo == n - 1 || yo == 0 || yo == m - 1;
-    const double h2x = dmul(2.0, hx), h2y = dmul(2.0, hy), hxx = dmul(hx, hx), hyy = dmul(hy, hy);
-    const float hx_f = (float)hx, hy_f = (float)hy, h2x_f = (float)h2x, h2y_f = (float)h2y;
-    const float hxx_f = (float)hxx, hyy_f = (float)hyy;
+    const long long qs = (long long)K * mn;
     for (int k = 0; k < K; ++k) {
         double* Jk = J + (long long)f * 6 * K * mn + (long long)k * mn;
-        if (ring) {
-            for (int q = 0; q < 6; ++q) Jk[(long long)q * K * mn + o] = 0.0;
-            continue;
-        }
-        const float* a = f1 + (long long)k * hw;
-        const float* b = f2 + ((long long)f * K + k) * hw;
-        // padded (yy, xx) -> unpadded clamp
-        auto A = [&](int yy, int xx) { return (double)a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
-        auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
-        // numpy.gradient of the padded arrays at an interior padded position
-        auto gx1 = [&](int yy, int xx) { return ddiv(dsub(A(yy, xx + 1), A(yy, xx - 1)), h2x); };
-        auto gy1 = [&](int yy, int xx) { return ddiv(dsub(A(yy + 1, xx), A(yy - 1, xx)), h2y); };
-        auto gx2 = [&](int yy, int xx) {
-            if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), h2x_f);
-            return ddiv(dsub((double)Bf(yy, xx + 1), (double)Bf(yy, xx - 1)), h2x);
-        };
-        auto gy2 = [&](int yy, int xx) {
-            if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), h2y_f);
-            return ddiv(dsub((double)Bf(yy + 1, xx), (double)Bf(yy - 1, xx)), h2y);
-        };
-        // fx, fy, ft re-padded from the interior: clamp the padded index to [1, h] x [1, w]
-        auto FX = [&](int yy, int xx) {
-            yy = xclamp(yy, 1, h);
-            xx = xclamp(xx, 1, w);
-            return dmul(0.5, dadd(gx1(yy, xx), gx2(yy, xx)));
-        };
-        auto FT = [&](int yy, int xx) {
-            yy = xclamp(yy, 1, h);
-            xx = xclamp(xx, 1, w);
-            return dsub((double)Bf(yy, xx), A(yy, xx));
-        };
-        double j11, j22, j33, j12, j13, j23;
-        if (gray == 2) {
-            // census (core/optical_flow.py:231-345): per neighbour offset the smoothed
-            // Heaviside of the directional difference, s = 0.5 (1 + r / sqrt(r^2 + eps^2)),
-            // edge-padded, differentiated centrally; float32 arithmetic on f2 when
-            // f2_f32 (Python-float constants cast to float32), float64 otherwise
-            const double eps = 0.1 / 255.0, eps2 = dmul(eps, eps);
-            const float eps2f = (float)eps2;
-            j11 = j22 = j33 = j12 = j13 = j23 = 0.0;
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    if (dy == 0 && dx == 0) continue;
-                    const double ty = dmul(hy, (double)dy), tx = dmul(hx, (double)dx);
-                    const double dist = __dsqrt_rn(dadd(dmul(ty, ty), dmul(tx, tx)));
-                    const float dist_f = (float)dist;
-                    // s at padded (yy, xx), the edge pad of the core (clamped into [1, h] x [1, w])
-                    auto s1 = [&](int yy, int xx) {
-                        yy = xclamp(yy, 1, h);
-                        xx = xclamp(xx, 1, w);
-                        const double r = ddiv(dsub(A(yy + dy, xx + dx), A(yy, xx)), dist);
-                        return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
-                    };
-                    auto s2 = [&](int yy, int xx) {
-                        yy = xclamp(yy, 1, h);
-                        xx = xclamp(xx, 1, w);
-                        if (f2_f32) {
-                            const float r = __fdiv_rn(__fsub_rn(Bf(yy + dy, xx + dx), Bf(yy, xx)), dist_f);
-                            const float q = __fsqrt_rn(__fadd_rn(__fmul_rn(r, r), eps2f));
-                            return (double)__fmul_rn(0.5f, __fadd_rn(1.0f, __fdiv_rn(r, q)));
-                        }
-                        const double r = ddiv(dsub((double)Bf(yy + dy, xx + dx), (double)Bf(yy, xx)), dist);
-                        return dmul(0.5, dadd(1.0, ddiv(r, __dsqrt_rn(dadd(dmul(r, r), eps2)))));
-                    };
-                    const double sx1 = ddiv(dsub(s1(yo, xo + 1), s1(yo, xo - 1)), h2x);
-                    const double sy1 = ddiv(dsub(s1(yo + 1, xo), s1(yo - 1, xo)), h2y);
-                    double sx2, sy2;
-                    if (f2_f32) {
-                        sx2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo, xo + 1), (float)s2(yo, xo - 1)), h2x_f);
-                        sy2 = (double)__fdiv_rn(__fsub_rn((float)s2(yo + 1, xo), (float)s2(yo - 1, xo)), h2y_f);
-                    } else {
-                        sx2 = ddiv(dsub(s2(yo, xo + 1), s2(yo, xo - 1)), h2x);
-                        sy2 = ddiv(dsub(s2(yo + 1, xo), s2(yo - 1, xo)), h2y);
-                    }
-                    const double sx = dmul(0.5, dadd(sx1, sx2)), sy = dmul(0.5, dadd(sy1, sy2));
-                    const double st = dsub(s2(yo, xo), s1(yo, xo));
-                    j11 = dadd(j11, dmul(sx, sx));
-                    j22 = dadd(j22, dmul(sy, sy));
-                    j33 = dadd(j33, dmul(st, st));
-                    j12 = dadd(j12, dmul(sx, sy));
-                    j13 = dadd(j13, dmul(sx, st));
-                    j23 = dadd(j23, dmul(sy, st));
-                }
-            j11 = dmul(j11, 0.25); j22 = dmul(j22, 0.25); j33 = dmul(j33, 0.25);
-            j12 = dmul(j12, 0.25); j13 = dmul(j13, 0.25); j23 = dmul(j23, 0.25);
-        } else if (gray) {
-            const double fxv = FX(yo, xo);
-            const double fyv = dmul(0.5, dadd(gy1(yo, xo), gy2(yo, xo)));
-            const double ftv = FT(yo, xo);
-            j11 = dmul(fxv, fxv); j22 = dmul(fyv, fyv); j33 = dmul(ftv, ftv);
-            j12 = dmul(fxv, fyv); j13 = dmul(fxv, ftv); j23 = dmul(fyv, ftv);
-        } else {
-            const double fxy = ddiv(dsub(FX(yo + 1, xo), FX(yo - 1, xo)), h2y);
-            const double fxt = ddiv(dsub(FT(yo, xo + 1), FT(yo, xo - 1)), h2x);
-            const double fyt = ddiv(dsub(FT(yo + 1, xo), FT(yo - 1, xo)), h2y);
-            const double fxx1 = ddiv(dadd(dsub(A(yo, xo - 1), dmul(2.0, A(yo, xo))), A(yo, xo + 1)), hxx);
-            const double fyy1 = ddiv(dadd(dsub(A(yo - 1, xo), dmul(2.0, A(yo, xo))), A(yo + 1, xo)), hyy);
-            double fxx2, fyy2;
-            if (f2_f32) {
-                fxx2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)), hxx_f);
-                fyy2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)), hyy_f);
-            } else {
-                fxx2 = ddiv(dadd(dsub((double)Bf(yo, xo - 1), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo, xo + 1)), hxx);
-                fyy2 = ddiv(dadd(dsub((double)Bf(yo - 1, xo), dmul(2.0, (double)Bf(yo, xo))), (double)Bf(yo + 1, xo)), hyy);
-            }
-            const double fxx = dmul(0.5, dadd(fxx1, fxx2));
-            const double fyy = dmul(0.5, dadd(fyy1, fyy2));
-            const double sx = __dsqrt_rn(dadd(dmul(fxx, fxx), dmul(fxy, fxy)));
-            const double sy = __dsqrt_rn(dadd(dmul(fxy, fxy), dmul(fyy, fyy)));
-            const double reg_x = ddiv(1.0, dadd(dmul(sx, sx), 1e-6));
-            const double reg_y = ddiv(1.0, dadd(dmul(sy, sy), 1e-6));
-            j11 = dadd(dmul(reg_x, dmul(fxx, fxx)), dmul(reg_y, dmul(fxy, fxy)));
-            j22 = dadd(dmul(reg_x, dmul(fxy, fxy)), dmul(reg_y, dmul(fyy, fyy)));
-            j33 = dadd(dmul(reg_x, dmul(fxt, fxt)), dmul(reg_y, dmul(fyt, fyt)));
-            j12 = dadd(dmul(dmul(reg_x, fxx), fxy), dmul(dmul(reg_y, fxy), fyy));
-            j13 = dadd(dmul(dmul(reg_x, fxx), fxt), dmul(dmul(reg_y, fxy), fyt));
-            j23 = dadd(dmul(dmul(reg_x, fxy), fxt), dmul(dmul(reg_y, fyy), fyt));
-        }
-        const long long qs = (long long)K * mn;
-        Jk[0 * qs + o] = j11;
-        Jk[1 * qs + o] = j22;
-        Jk[2 * qs + o] = j33;
-        Jk[3 * qs + o] = j12;
-        Jk[4 * qs + o] = j13;
-        Jk[5 * qs + o] = j23;
+        double j[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (!ring) tensor_px64(f1, f2, f, K, k, h, w, yo, xo, hy, hx, f2_f32, gray, j);
+        for (int q = 0; q < 6; ++q) Jk[q * qs + o] = j[q];
     }
-    (void)hx_f;
-    (void)hy_f;
+}
+
+// The tensor for the float64 chained SOR, written diagonal-major: J (T, 6, K,
+// D*P), pixel (r, c) at (r + c) * P + r, plus the smoothness numerator's
+// constant part from the edge-padded float64 u, v (core/level_solver.py:
+// 317-340): lap_u = wx ((uL - uc) + (uR - uc)) + wy ((uU - uc) + (uD - uc)),
+// lap_v likewise, (T, 2, D*P).
+//
+// The float64 arithmetic of core/optical_flow.py:73-228 with its divisions by
+// the spacings as products with their reciprocals, 1 / (sqrt(q)^2 + 1e-6) as
+// 1 / (q + 1e-6), and reciprocals by Newton's iteration from the hardware
+// approximation: each of these moves a value by about one rounding, far
+// below what the flow is sensitive to (the tensor rounded to 48 bits moves the
+// flow by 1e-8 px), at about 70 instead of 185 float64 operations per pixel
+// and channel.  The warped image's own derivatives keep numpy's float32
+// arithmetic exactly (f2_f32, every level below the top).  f1 is the
+// reference level in float64 (K, h, w), f2 the warped level (T, K, h, w).
+// One warp computes 32 consecutive rows of one diagonal, so every store is
+// one contiguous run; the stencil reads go through L1.
+struct TensConsts {
+    double ihx2, ihy2, ihxx, ihyy;  // 1 / (2 hx), 1 / (2 hy), 1 / hx^2, 1 / hy^2
+    float h2x_f, h2y_f, hxx_f, hyy_f;
+};
+
+__device__ __forceinline__ double drcp(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = __fma_rn(-x, y, 1.0);
+    y = __fma_rn(y, e, y);
+    e = __fma_rn(-x, y, 1.0);
+    return __fma_rn(y, e, y);
+}
+
+__device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, const float* __restrict__ b, int h, int w,
+                                              int yo, int xo, const TensConsts& C, int f2_f32, int gray, double* jo)
+{
+    // unpadded reads at padded (yy, xx), clamped into the level
+    auto A = [&](int yy, int xx) { return a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+    auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+    auto gx2 = [&](int yy, int xx) {
+        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), C.h2x_f);
+        return dmul(dsub((double)Bf(yy, xx + 1), (double)Bf(yy, xx - 1)), C.ihx2);
+    };
+    auto gy2 = [&](int yy, int xx) {
+        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), C.h2y_f);
+        return dmul(dsub((double)Bf(yy + 1, xx), (double)Bf(yy - 1, xx)), C.ihy2);
+    };
+    auto FX = [&](int yy, int xx) {
+        yy = xclamp(yy, 1, h);
+        xx = xclamp(xx, 1, w);
+        return dmul(0.5, dadd(dmul(dsub(A(yy, xx + 1), A(yy, xx - 1)), C.ihx2), gx2(yy, xx)));
+    };
+    auto FY = [&](int yy, int xx) {
+        yy = xclamp(yy, 1, h);
+        xx = xclamp(xx, 1, w);
+        return dmul(0.5, dadd(dmul(dsub(A(yy + 1, xx), A(yy - 1, xx)), C.ihy2), gy2(yy, xx)));
+    };
+    auto FT = [&](int yy, int xx) {
+        yy = xclamp(yy, 1, h);
+        xx = xclamp(xx, 1, w);
+        return dsub((double)Bf(yy, xx), A(yy, xx));
+    };
+    if (gray) {
+        const double fxv = FX(yo, xo), fyv = FY(yo, xo), ftv = FT(yo, xo);
+        jo[0] = dmul(fxv, fxv);
+        jo[1] = dmul(fyv, fyv);
+        jo[2] = dmul(ftv, ftv);
+        jo[3] = dmul(fxv, fyv);
+        jo[4] = dmul(fxv, ftv);
+        jo[5] = dmul(fyv, ftv);
+        return;
+    }
+    const double fxy = dmul(dsub(FX(yo + 1, xo), FX(yo - 1, xo)), C.ihy2);
+    const double fxt = dmul(dsub(FT(yo, xo + 1), FT(yo, xo - 1)), C.ihx2);
+    const double fyt = dmul(dsub(FT(yo + 1, xo), FT(yo - 1, xo)), C.ihy2);
+    const double a0 = A(yo, xo);
+    const double fxx1 = dmul(dadd(dsub(A(yo, xo - 1), dadd(a0, a0)), A(yo, xo + 1)), C.ihxx);
+    const double fyy1 = dmul(dadd(dsub(A(yo - 1, xo), dadd(a0, a0)), A(yo + 1, xo)), C.ihyy);
+    double fxx2, fyy2;
+    if (f2_f32) {
+        fxx2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)),
+                                 C.hxx_f);
+        fyy2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)),
+                                 C.hyy_f);
+    } else {
+        const double b0 = (double)Bf(yo, xo);
+        fxx2 = dmul(dadd(dsub((double)Bf(yo, xo - 1), dadd(b0, b0)), (double)Bf(yo, xo + 1)), C.ihxx);
+        fyy2 = dmul(dadd(dsub((double)Bf(yo - 1, xo), dadd(b0, b0)), (double)Bf(yo + 1, xo)), C.ihyy);
+    }
+    const double fxx = dmul(0.5, dadd(fxx1, fxx2));
+    const double fyy = dmul(0.5, dadd(fyy1, fyy2));
+    const double xx2 = dmul(fxx, fxx), xy2 = dmul(fxy, fxy), yy2 = dmul(fyy, fyy);
+    const double reg_x = drcp(dadd(dadd(xx2, xy2), 1e-6));
+    const double reg_y = drcp(dadd(dadd(xy2, yy2), 1e-6));
+    const double rxx = dmul(reg_x, fxx), rxy = dmul(reg_x, fxy);  // reg_x fxx, reg_x fxy
+    const double ryx = dmul(reg_y, fxy), ryy = dmul(reg_y, fyy);  // reg_y fxy, reg_y fyy
+    jo[0] = __fma_rn(rxx, fxx, dmul(ryx, fxy));
+    jo[1] = __fma_rn(rxy, fxy, dmul(ryy, fyy));
+    jo[2] = __fma_rn(dmul(reg_x, fxt), fxt, dmul(dmul(reg_y, fyt), fyt));
+    jo[3] = __fma_rn(rxx, fxy, dmul(ryx, fyy));
+    jo[4] = __fma_rn(rxx, fxt, dmul(ryx, fyt));
+    jo[5] = __fma_rn(rxy, fxt, dmul(ryy, fyt));
+}
+
+__global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__ f1, const float* __restrict__ f2,
+                                                      int K, int h, int w, TensConsts C, int f2_f32, int gray,
+                                                      double* __restrict__ J, long long J_fs, DiagGeom g,
+                                                      const double* __restrict__ u, const double* __restrict__ v,
+                                                      long long uv_fs, double wx, double wy, double* __restrict__ lap,
+                                                      long long lap_fs)
+{
+    const int nstrip = g.P >> 5;
+    const long long wid = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (wid >= (long long)g.D * nstrip) return;
+    const int d = (int)(wid / nstrip);
+    const int r = (int)(wid - (long long)d * nstrip) * 32 + (threadIdx.x & 31);
+    const int c = d - r;
+    if (r >= h || c < 0 || c >= w) return;
+    const int f = blockIdx.y;
+    const long long plane = (long long)g.D * g.P;
+    const long long di = (long long)d * g.P + r;
+    const long long hw = (long long)h * w;
+    double* Jf = J + f * J_fs;
+    for (int k = 0; k < K; ++k) {
+        double j[6];
+        tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) Jf[((long long)q * K + k) * plane + di] = j[q];
+    }
+    const long long n = w + 2;
+    const double* uf = u + f * uv_fs;
+    const double* vf = v + f * uv_fs;
+    const long long o = (long long)(r + 1) * n + c + 1;
+    const double uc = uf[o], vc = vf[o];
+    const double lu = __fma_rn(wx, dadd(dsub(uf[o - 1], uc), dsub(uf[o + 1], uc)),
+                               dmul(wy, dadd(dsub(uf[o - n], uc), dsub(uf[o + n], uc))));
+    const double lv = __fma_rn(wx, dadd(dsub(vf[o - 1], vc), dsub(vf[o + 1], vc)),
+                               dmul(wy, dadd(dsub(vf[o - n], vc), dsub(vf[o + n], vc))));
+    lap[f * lap_fs + di] = lu;
+    lap[f * lap_fs + plane + di] = lv;
 }
 
 cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int K, int h, int w, double hy, double hx,
@@ -329,6 +475,29 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
 {
     dim3 blk(128), grd((w + 2 + 127) / 128, h + 2, n_frames);
     kx_tensor<<<grd, blk, 0, st>>>(f1, f2, K, h, w, hy, hx, f2_f32, gray, J);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_x_tensor_diag(const double* f1, const float* f2, int n_frames, int K, int h, int w, double hy,
+                                 double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
+                                 const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
+                                 long long lap_fs, cudaStream_t st)
+{
+    TensConsts C;
+    const double h2x = 2.0 * hx, h2y = 2.0 * hy, hxx = hx * hx, hyy = hy * hy;
+    C.ihx2 = 1.0 / h2x;
+    C.ihy2 = 1.0 / h2y;
+    C.ihxx = 1.0 / hxx;
+    C.ihyy = 1.0 / hyy;
+    C.h2x_f = (float)h2x;
+    C.h2y_f = (float)h2y;
+    C.hxx_f = (float)hxx;
+    C.hyy_f = (float)hyy;
+    const long long warps = (long long)g.D * (g.P >> 5);
+    if ((warps + 7) / 8 > 0x7fffffffLL || n_frames > 65535) return cudaErrorInvalidValue;
+    dim3 grd((unsigned)((warps + 7) / 8), n_frames);
+    kx_tensor_diag<<<grd, 256, 0, st>>>(f1, f2, K, h, w, C, f2_f32, gray, J, J_fs, g, u, v, uv_fs, wx, wy, lap,
+                                        lap_fs);
     return cudaGetLastError();
 }
 
@@ -725,6 +894,37 @@ cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* 
     return cudaSuccess;
 }
 
+__global__ void kx_to_double(const float* __restrict__ src, long long n, double* __restrict__ dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (double)src[i];
+}
+
+cudaError_t launch_x_to_double(const float* src, long long n, double* dst, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    kx_to_double<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, n, dst);
+    return cudaGetLastError();
+}
+
+// Padded (K, m*n) planes (the interior at (1, 1)) to diagonal-major (K, D*P).
+__global__ void kx_pad_to_diag(const double* __restrict__ src, int K, int h, int w, DiagGeom g, double* __restrict__ dst)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    const int k = blockIdx.z;
+    if (c >= w || k >= K) return;
+    const long long n = w + 2, mn = (long long)(h + 2) * n;
+    dst[(long long)k * g.D * g.P + diag_index(g, r, c)] = src[k * mn + (long long)(r + 1) * n + c + 1];
+}
+
+cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, K);
+    kx_pad_to_diag<<<grd, blk, 0, st>>>(src, K, h, w, g, dst);
+    return cudaGetLastError();
+}
+
 __global__ void kx_to_float(const double* __restrict__ src, long long n, float* __restrict__ dst)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -784,6 +984,59 @@ __device__ double median25d(double v[25])
     return t[12];
 }
 
+// The same median with the comparisons on the float32 pipe.  The high word of
+// a double (sign, exponent, top 20 bits of the fraction), read as a float,
+// orders like the double itself as long as it is a finite float (|x| < 2^1017):
+// both are sign-magnitude encodings with the magnitude bits in significance
+// order.  The 13th smallest key is found by the selection network of
+// median25d on floats; if exactly one value carries it, that value is the
+// median.  When several values share the key (values equal in their top 20
+// fraction bits), or a key is not finite, median25d decides in float64.
+__device__ __forceinline__ float hikey(double x) { return __int_as_float(__double2hiint(x)); }
+
+__device__ __forceinline__ void fswap(float& x, float& y)
+{
+    const float lo = fminf(x, y), hi = fmaxf(x, y);
+    x = lo;
+    y = hi;
+}
+
+__device__ double median25_keys(double v[25])
+{
+    float t[14];
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 14; ++i) {
+        t[i] = hikey(v[i]);
+        finite = finite && fabsf(t[i]) <= 3.402823466e38f;
+    }
+#pragma unroll
+    for (int round = 0; round < 11; ++round) {
+        const int lo = round;
+#pragma unroll
+        for (int i = lo + 1; i < 14; ++i) fswap(t[lo], t[i]);
+#pragma unroll
+        for (int i = lo + 1; i < 13; ++i) fswap(t[i], t[13]);
+        t[13] = hikey(v[14 + round]);
+        finite = finite && fabsf(t[13]) <= 3.402823466e38f;
+    }
+    fswap(t[11], t[12]);
+    fswap(t[12], t[13]);
+    fswap(t[11], t[12]);
+    const float m = t[12];
+    int eq = 0;
+    double pick = 0.0;
+#pragma unroll
+    for (int i = 0; i < 25; ++i) {
+        if (hikey(v[i]) == m) {
+            ++eq;
+            pick = v[i];
+        }
+    }
+    if (finite && eq == 1) return pick;
+    return median25d(v);
+}
+
 __global__ void kx_median_accum(const double* __restrict__ du, const double* __restrict__ dv,
                                 const double* __restrict__ u, const double* __restrict__ v, long long uv_fs, int h,
                                 int w, int do_median, double* ou, double* ov, long long o_fs, long long o_rs,
@@ -814,8 +1067,8 @@ __global__ void kx_median_accum(const double* __restrict__ du, const double* __r
                 ++q;
             }
         }
-        mu = median25d(a);
-        mv = median25d(b);
+        mu = median25_keys(a);
+        mv = median25_keys(b);
     } else {
         const long long o = (long long)(y + 1) * n + x + 1;
         mu = duf[o];
@@ -824,6 +1077,35 @@ __global__ void kx_median_accum(const double* __restrict__ du, const double* __r
     const long long oc = (long long)(y + 1) * n + x + 1;
     ou[f * o_fs + y * o_rs + x * o_cs] = dadd(u[f * uv_fs + oc], mu);
     ov[f * o_fs + y * o_rs + x * o_cs] = dadd(v[f * uv_fs + oc], mv);
+}
+
+// 5x5 median (scipy "mirror") of one float64 plane (h, w), h, w >= 3.
+__global__ void kx_median5_plane(const double* __restrict__ src, int h, int w, double* __restrict__ dst)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) return;
+    double a[25];
+    int q = 0;
+    for (int dy = -2; dy <= 2; ++dy) {
+        int yy = y + dy;
+        if (yy < 0) yy = -yy;
+        if (yy >= h) yy = 2 * (h - 1) - yy;
+        for (int dx = -2; dx <= 2; ++dx) {
+            int xx = x + dx;
+            if (xx < 0) xx = -xx;
+            if (xx >= w) xx = 2 * (w - 1) - xx;
+            a[q++] = src[(long long)yy * w + xx];
+        }
+    }
+    dst[(long long)y * w + x] = median25_keys(a);
+}
+
+cudaError_t launch_x_median5_plane(const double* src, int h, int w, double* dst, cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h);
+    kx_median5_plane<<<grd, blk, 0, st>>>(src, h, w, dst);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
@@ -873,8 +1155,8 @@ __global__ void kx_gnc_median(const double* __restrict__ du, const double* __res
                 ++q;
             }
         }
-        mu = median25d(a);
-        mv = median25d(b);
+        mu = median25_keys(a);
+        mv = median25_keys(b);
     } else {
         const long long o = (long long)(y + 1) * n + x + 1;
         mu = dadd(uf[o], duf[o]);

@@ -39,6 +39,11 @@ __host__ __device__ inline long long diag_index(const DiagGeom& g, int r, int c)
     return (long long)(r + c) * g.P + r;
 }
 
+// cudaFuncSetAttribute(cudaFuncAttributeMaxDynamicSharedMemorySize) holds per
+// device: this sets it once per (kernel, current device) pair, so a process that
+// launches on several GPUs gets it on each of them.  Thread-safe.
+cudaError_t ensure_max_dyn_smem(const void* kernel, int bytes);
+
 // Kernel launchers (frg_kernels.cu).  All enqueue on `st` and return the
 // launch status; none synchronises.
 cudaError_t launch_resize_h(View src, int n_frames, int n_planes, int ih, int iw, float* dst, int ow,
@@ -114,6 +119,22 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
                              int n_frames, int K, DiagGeom g, const ChainPass* passes, int n_passes,
                              const float* a_data, float wx, float wy, float omega, cudaStream_t st,
                              float* out_du = nullptr, float* out_dv = nullptr, long long out_fs = 0);
+// The chained SOR in float64 (frg_sor64.cu, k_sor_chain64): the schedule of
+// launch_sor_chain with float64 state, coefficients and arithmetic (the parity
+// precision).  J [6][K][D*P], W [K][D*P], lap [2][D*P], coef [5][D*P] and the
+// state du, dv [D*P] are diagonal-major doubles; the final pass writes du, dv
+// at out + r * out_rs + c.  Levels of at most 2048 (padded) rows (over 256 as
+// clusters of row strips), K <= 4, w >= 3, at most kMaxChain passes of G <= kGMax.
+bool sor_chain64_supports(int K, const DiagGeom& g, int n_passes);
+cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W, long long W_fs, const double* lap,
+                               long long lap_fs, double* coef, long long coef_fs, double* du, double* dv,
+                               long long st_fs, int n_frames, int K, DiagGeom g, const ChainPass* passes,
+                               int n_passes, const double* a_data, double wx, double wy, double omega,
+                               cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs);
+// x^b elementwise by the float64 solver's table-driven power (frg_dpow.cuh);
+// upload_dpow_tables must have run on the current device.
+cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cudaStream_t st);
+cudaError_t upload_dpow_tables();
 // 5x5 median (mirror) of row-major du, dv (T, h, w) plus accumulation into u, v.
 cudaError_t launch_median_rm(const float* du, const float* dv, long long fs, View u, View v, int n_frames, int h,
                              int w, int do_median, ViewW out_u, ViewW out_v, cudaStream_t st);
@@ -140,6 +161,14 @@ cudaError_t launch_x_warp(const float* f2, const float* f1, const double* u, con
                           int n_frames, int K, int h, int w, double h_col, double h_row, float* out, cudaStream_t st);
 cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int K, int h, int w, double hy, double hx,
                             int f2_f32, int gray, double* J, cudaStream_t st);
+// The tensor diagonal-major (T, 6, K, D*P) with the smoothness constant
+// (T, 2, D*P) from the padded float64 u, v (frame stride uv_fs), for the
+// float64 chained SOR; f1 is the reference level in float64 (K, h, w).
+cudaError_t launch_x_tensor_diag(const double* f1, const float* f2, int n_frames, int K, int h, int w, double hy,
+                                 double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
+                                 const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
+                                 long long lap_fs, cudaStream_t st);
+cudaError_t launch_x_to_double(const float* src, long long n, double* dst, cudaStream_t st);
 cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
                          double alpha_y, double hx, double hy, int iterations, int update_lag,
@@ -154,6 +183,8 @@ cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* 
                                 int update_lag, const double* a_data, double a_smooth, double omega, double gnc_beta,
                                 cudaStream_t st, long long* launches);
 cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st);
+// Padded (K, (h+2)*(w+2)) float64 planes to diagonal-major (K, D*P).
+cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st);
 cudaError_t launch_x_hwk_to_planes(const double* src, int n_arrays, long long mn, int K, double* dst, cudaStream_t st);
 // cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
 // (oh, ow): width pass into tmp, height pass into the strided dst view.
@@ -164,6 +195,9 @@ cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, in
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
+// 5x5 median (mirror) of one float64 plane (h, w), h, w >= 3 (the selection of
+// launch_x_median_accum).
+cudaError_t launch_x_median5_plane(const double* src, int h, int w, double* dst, cudaStream_t st);
 // One GNC warping step's state update (two kernels, the second only when
 // write_ring): (ou, ov) = [median5](u + du) interiors, then the padded u, v
 // rebuilt from them.  Counts 1 + write_ring launches.

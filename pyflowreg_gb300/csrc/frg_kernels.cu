@@ -10,8 +10,27 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 namespace frg {
+
+cudaError_t ensure_max_dyn_smem(const void* kernel, int bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> done;  // (kernel, device) -> bytes set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(kernel, dev);
+    const auto it = done.find(key);
+    if (it != done.end() && it->second >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done[key] = bytes;
+    return e;
+}
 
 __constant__ float c_cubic[32 * 4];
 __constant__ float c_linear[32 * 2];
@@ -433,12 +452,9 @@ cudaError_t run_tensor(View f1, View f2, int n_frames, int K, int h, int w, floa
 {
     const size_t smem = (size_t)(6 * K + (lap ? 2 : 0)) * kTensTile * kTensLd * sizeof(float);
     if (smem <= 200 * 1024) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_tensor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 200 * 1024);
+        {
+            const cudaError_t e = ensure_max_dyn_smem((const void*)k_tensor_tiled, 200 * 1024);
             if (e != cudaSuccess) return e;
-            attr = true;
         }
         dim3 grd((w + kTensTile - 1) / kTensTile, (h + kTensTile - 1) / kTensTile, n_frames);
         k_tensor_tiled<<<grd, 256, smem, st>>>(f1, f2, K, h, w, hy, hx, gray, J, J_fs, g, u, v, wx, wy, lap, lap_fs);
@@ -754,12 +770,10 @@ cudaError_t launch_sor(const float* coef, long long coef_fs, float* du, float* d
     if (g.P > kMaxLane || G < 1 || G > kGMax || (g.P & 31)) return cudaErrorInvalidValue;
     const int R = 2 * G + 2;
     const size_t smem = (size_t)R * 7 * g.P * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_sor, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)((size_t)kRing * 7 * kMaxLane * sizeof(float)));
+    {
+        const cudaError_t e =
+            ensure_max_dyn_smem((const void*)k_sor, (int)((size_t)kRing * 7 * kMaxLane * sizeof(float)));
         if (e != cudaSuccess) return e;
-        attr_set = true;
     }
     k_sor<<<n_frames, g.P, smem, st>>>(coef, coef_fs, du, dv, st_fs, g, G, wa, wb, omega);
     return cudaGetLastError();

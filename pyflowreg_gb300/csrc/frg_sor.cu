@@ -769,12 +769,9 @@ constexpr int kSmemLimit = 232448;  // 227 KB of dynamic shared memory per CTA
 template <int K, int PF, int MAXT>
 cudaError_t run_fused_t(const SorArgs& A, int n_frames, int threads, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_sor_fused<K, PF, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemLimit);
+    {
+        const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_fused<K, PF, MAXT>, kSmemLimit);
         if (e != cudaSuccess) return e;
-        attr = true;
     }
     const size_t smem = (size_t)(2 * A.G + 3) * 7 * A.g.P * sizeof(float);
     k_sor_fused<K, PF, MAXT><<<n_frames, threads, smem, st>>>(A);
@@ -836,23 +833,17 @@ template <int K, int G>
 cudaError_t run_regs_t(const SorArgs& A, int n_frames, int nt, cudaStream_t st)
 {
     if (A.nc == 1) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 kSmemLimit);
+        {
+            const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_regs<K, G, false>, kSmemLimit);
             if (e != cudaSuccess) return e;
-            attr = true;
         }
         k_sor_regs<K, G, false><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A);
         return cudaGetLastError();
     }
     if constexpr (K <= 2) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_sor_regs<K, G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 kSmemLimit);
+        {
+            const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_regs<K, G, true>, kSmemLimit);
             if (e != cudaSuccess) return e;
-            attr = true;
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(n_frames * A.nc));
@@ -947,23 +938,17 @@ template <int K, int G, bool CO>
 cudaError_t run_chain_t(const SorArgs& A, const ChainTable& T, int n_frames, int nt, cudaStream_t st)
 {
     if (A.nc == 1) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO, false>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+        {
+            const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_chain<K, G, CO, false>, kSmemLimit);
             if (e != cudaSuccess) return e;
-            attr = true;
         }
         k_sor_chain<K, G, CO, false><<<n_frames, nt, sor_regs_smem(G, nt), st>>>(A, T);
         return cudaGetLastError();
     }
     if constexpr (K <= 2) {
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_sor_chain<K, G, CO, true>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+        {
+            const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_chain<K, G, CO, true>, kSmemLimit);
             if (e != cudaSuccess) return e;
-            attr = true;
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(n_frames * A.nc));

@@ -6,7 +6,8 @@ Frames of a batch are independent once ``w_init`` is fixed
 contiguous frame ranges and register them with no communication.  Between
 batches pyflowreg sets the next initial field to the mean of the last (up to
 20) flows of the batch (motion_correction/compensate_recording.py:801-806);
-with frames sharded, that mean is an all-reduce of per-rank partial sums.
+with frames sharded, the ranks exchange the flows of that tail and each sums
+them in frame order, so every rank gets numpy's float32 mean bit for bit.
 Everything here runs over any torch.distributed backend (NCCL on GPUs, gloo
 on CPU for tests).
 """
@@ -34,32 +35,62 @@ def _dist():
     return dist
 
 
+def numpy_mean0_f32(frames: np.ndarray) -> np.ndarray:
+    """np.mean(frames, axis=0) of a float32 stack, as numpy computes it: the
+    leading axis is reduced element-wise, one frame after another, in float32,
+    then divided by the count in float32."""
+    acc = np.array(frames[0], dtype=np.float32, copy=True)
+    for i in range(1, frames.shape[0]):
+        acc += frames[i]
+    return acc / np.float32(frames.shape[0])
+
+
 def next_w_init(local_flows, start: int, n_total: int, last: int = 20, group=None) -> np.ndarray:
     """Mean of the last `last` flows of the whole batch (all of them when the
-    batch has no more than `last` frames), from each rank's contiguous share.
+    batch has no more than `last` frames), from each rank's contiguous share,
+    equal bit for bit to pyflowreg's ``np.mean(w[-20:], axis=0)``
+    (motion_correction/compensate_recording.py:801-806).
 
-    local_flows: (t, H, W, 2) flows of global frames [start, start + t).
-    Returns (H, W, 2) float32 on every rank, as the reference stores w_init.
-    The partial sums are float64, so the result may differ from numpy's
-    float32 mean by one float32 rounding.
+    local_flows: (t, H, W, 2) flows of global frames [start, start + t).  The
+    ranks exchange their frames of the tail (at most `last` flows in all), so
+    that every rank sums the same frames in frame order.  Returns (H, W, 2)
+    float32 on every rank.
     """
     import torch
 
-    flows = np.asarray(local_flows, dtype=np.float64)
+    flows = np.asarray(local_flows, dtype=np.float32)
     first = n_total - last if n_total > last else 0
-    t = flows.shape[0]
-    lo = max(first - start, 0)
-    part = flows[lo:t].sum(axis=0) if lo < t else np.zeros(flows.shape[1:], np.float64)
-    count = max(t - lo, 0)
-    dist = _dist()
-    if dist.is_available() and dist.is_initialized():
-        buf = torch.from_numpy(np.concatenate([part.ravel(), [float(count)]]))
-        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
-        part = buf[:-1].numpy().reshape(part.shape)
-        count = int(round(float(buf[-1])))
-    if count == 0:
+    count = n_total - first
+    if count <= 0:
         raise ValueError("empty batch")
-    return (part / count).astype(np.float32)
+    t = flows.shape[0]
+    dist = _dist()
+    world = dist.get_world_size(group) if (dist.is_available() and dist.is_initialized()) else 1
+    if world == 1:
+        if start != 0 or t != n_total:
+            raise ValueError("a single process must hold the whole batch")
+        return numpy_mean0_f32(flows[first:])
+    # this rank's frames of the tail in their slots, the others zero
+    slots = np.zeros((count,) + flows.shape[1:], np.float32)
+    a, b = max(first, start), min(n_total, start + t)
+    if a < b:
+        slots[a - first:b - first] = flows[a - start:b - start]
+    span = torch.tensor([a, b], dtype=torch.int64)
+    spans = [torch.empty_like(span) for _ in range(world)]
+    dist.all_gather(spans, span, group=group)
+    buf = torch.from_numpy(slots)
+    bufs = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(bufs, buf, group=group)
+    tail = np.empty_like(slots)
+    covered = 0
+    for sp, bf in zip(spans, bufs):
+        ra, rb = int(sp[0]), int(sp[1])
+        if ra < rb:
+            tail[ra - first:rb - first] = bf.numpy()[ra - first:rb - first]
+            covered += rb - ra
+    if covered != count:
+        raise ValueError("the ranks' shares do not cover the batch tail exactly once")
+    return numpy_mean0_f32(tail)
 
 
 def max_over_ranks(value: float, group=None) -> float:

@@ -56,7 +56,7 @@ def test_motion_tensor(oracle, golden_dir, gray):
     got = np.stack(fn(f1, f2, hy, hx))
     ref = np.stack(oracle.motion_tensor(f1, f2, hy, hx, 0, gray))
     scale = np.abs(ref).max(axis=(1, 2), keepdims=True) + 1e-30
-    assert np.abs(got - ref).max() / 1 < 1e9
+    assert np.isfinite(got).all()
     np.testing.assert_allclose(got / scale, ref / scale, rtol=0, atol=2e-5)
 
 
@@ -77,3 +77,33 @@ def test_median(oracle, h, w):
     got = G.median_filter5(a)
     ref = oracle.median5(a.astype(np.float64)).astype(np.float32)
     np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("h,w", [(5, 5), (9, 17), (64, 48), (131, 77)])
+def test_median_f64_exact(h, w):
+    """The float64 median (float32-key selection with a float64 tie-break) equals
+    scipy's median_filter(size=(5, 5), mode="mirror") bit for bit, including
+    values that agree in their top 20 fraction bits, exact ties, signed zeros
+    and large magnitudes."""
+    import ctypes
+
+    import scipy.ndimage as ndi
+    import torch
+
+    from pyflowreg_gb300 import _lib
+
+    rng = np.random.default_rng(h * 1000 + w)
+    a = rng.standard_normal((h, w))
+    a[::3, ::2] = a[0, 0]                                   # exact ties
+    a[1::4, 1::3] = a[1, 1] * (1 + 2.0 ** -40 * rng.integers(-3, 4, a[1::4, 1::3].shape))  # same top bits
+    a[2::5, ::4] = 0.0
+    a[3::6, 2::5] = -0.0
+    a[0, :] *= 1e200
+    src = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dst = torch.empty_like(src)
+    rc = _lib.load().frg_median5_f64(h, w, ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(dst.data_ptr()),
+                                     ctypes.c_void_p(0))
+    _lib.check(rc, "frg_median5_f64")
+    torch.cuda.synchronize()
+    ref = ndi.median_filter(a, size=(5, 5), mode="mirror")
+    np.testing.assert_array_equal(dst.cpu().numpy(), ref)

@@ -112,3 +112,19 @@ def test_schedule_matches_reference_level_counts(oracle):
     assert len(oracle.level_schedule(256, 256, 100, 0.8, 0)[0]) == 16
     assert len(oracle.level_schedule(512, 512, 100, 0.8, 0)[0]) == 19
     assert len(oracle.level_schedule(1024, 1024, 100, 0.8, 0)[0]) == 22
+
+
+def test_native_timed_build_returns_the_checkers_bits(oracle):
+    """The CPU baseline is timed on the -O3 -march=native build; it has the
+    checker's float semantics (no contraction, no fast-math), so its flows are
+    bit-identical to the portable build's."""
+    from pyflowreg_gb300.synthetic import pair_256
+
+    fixed, moving, _ = pair_256(5, h=48, w=40)
+    kw = dict(alpha=(1.5, 1.5), iterations=12, update_lag=5, weight=None)
+    mv = np.stack([moving, moving[::-1]]).astype(np.float64)
+    a = oracle.get_displacement_batch(fixed, mv, n_threads=2, **kw)
+    b = oracle.get_displacement_batch(fixed, mv, n_threads=2, variant="native", **kw)
+    np.testing.assert_array_equal(a, b)
+    flags = oracle.build_flags()
+    assert "-O3" in flags["native"] and "-ffp-contract=off" in flags["native"]
