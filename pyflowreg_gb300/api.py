@@ -490,7 +490,7 @@ def clear_plans():
 # get_displacement (core/optical_flow.py:773-929)
 # --------------------------------------------------------------------------
 def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_level, levels, eta, a_smooth,
-             const_assumption, gnc_schedule, warping_steps, level_solver_backend, precision="fp32"):
+             const_assumption, gnc_schedule, warping_steps, level_solver_backend, precision="fp64"):
     const = resolve_const_assumption(const_assumption)
     if level_solver_backend is not None:
         raise NotImplementedError("the GB300 backend runs its own level solver; level_solver_backend must be None")
@@ -507,13 +507,15 @@ def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_l
 
 def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, min_level=0, levels=50, eta=0.8,
                      a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None, weight=None,
-                     level_solver_backend=None, gnc_schedule=None, warping_steps=None, precision="fp32"):
+                     level_solver_backend=None, gnc_schedule=None, warping_steps=None, precision="fp64"):
     """Drop-in for pyflowreg.core.optical_flow.get_displacement on the GPU.
 
     Returns the (H, W, 2) float64 displacement, [..., 0] = u (columns),
-    [..., 1] = v (rows), like the reference.  ``precision`` ("fp32" fast path,
-    "fp64" reference precision and operation order) is the only argument the
-    reference does not have.
+    [..., 1] = v (rows), like the reference.  ``precision`` is the only
+    argument the reference does not have: "fp64" (default) computes in the
+    reference's float64 precision and operation order and matches it within
+    1e-3 px; "fp32" is faster, but the algorithm amplifies float32 rounding to
+    deviations of up to ~0.7 px from the reference's flow.
     """
     assert fixed.ndim == moving.ndim, (
         f"Fixed and moving must have same dimensions: fixed.shape={fixed.shape}, moving.shape={moving.shape}"
@@ -527,10 +529,10 @@ def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, m
 
 def get_displacement_batch(fixed, moving_frames, alpha=(2, 2), update_lag=5, iterations=50, min_level=0,
                            levels=50, eta=0.8, a_smooth=1.0, a_data=0.45, const_assumption="gc", uv=None,
-                           weight=None, gnc_schedule=None, warping_steps=None, max_frames=None, precision="fp32"):
+                           weight=None, gnc_schedule=None, warping_steps=None, max_frames=None, precision="fp64"):
     """Many moving frames (T, H, W[, K]) against one fixed frame in one device
-    pass; returns (T, H, W, 2) float32 (the dtype the executors store), float64
-    for precision="fp64"."""
+    pass; returns (T, H, W, 2) float64 for precision="fp64" (default), float32
+    for "fp32"."""
     moving_frames = np.asarray(moving_frames)
     fixed, _, w, params, m, n, K = _prepare(fixed, moving_frames[0], weight, a_data, alpha, update_lag,
                                             iterations, min_level, levels, eta, a_smooth, const_assumption,
@@ -539,7 +541,36 @@ def get_displacement_batch(fixed, moving_frames, alpha=(2, 2), update_lag=5, ite
     return _run_host(params, fixed.reshape(m, n, K), moving_frames.reshape(T, m, n, K), w, uv, max_frames)
 
 
+class _HostIO:
+    """Per-lane staging of the host-buffer calls, kept with the plan (pinning
+    memory is slow, so it is done once): device input and output slots of a
+    lane's frames, their pinned host copies, and the copy streams."""
+
+    def __init__(self, H, W, K, frames, fp64, dev):
+        odt = torch.float64 if fp64 else torch.float32
+        self.frames = frames
+        self.dev_in = torch.empty((frames, H, W, K), dtype=torch.float32, device=dev)
+        self.dev_out = torch.empty((frames, H, W, 2), dtype=odt, device=dev)
+        self.pin_in = torch.empty((frames, H, W, K), dtype=torch.float32).pin_memory()
+        self.pin_out = torch.empty((frames, H, W, 2), dtype=odt).pin_memory()
+        self.up_done = None    # event: pin_in consumed by the upload
+        self.down_done = None  # event: pin_out filled by the read-back
+
+
+def _host_io(plan, key, H, W, K, frames, fp64, dev):
+    cache = plan.__dict__.setdefault("_host_io", {})
+    io = cache.get(key)
+    if io is None or io.frames < frames:
+        io = cache[key] = _HostIO(H, W, K, frames, fp64, dev)
+    return io
+
+
 def _run_host(params, fixed, moving, weight, uv, max_frames=None):
+    """Host arrays in, host array out.  The batch goes to the plan's lanes in
+    contiguous parts; each part is copied into pinned memory, uploaded on a
+    copy stream, registered on its lane's stream and read back on a second
+    copy stream, so the host copies and transfers of one part overlap the
+    device work of the others."""
     _require_cuda()
     T, m, n, K = moving.shape
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -550,22 +581,73 @@ def _run_host(params, fixed, moving, weight, uv, max_frames=None):
     fixed_t = torch.from_numpy(fixed32).to(dev)
     w_t = torch.from_numpy(w32).to(dev)
     plan.set_reference(fixed_t, w_t, key=key)
-    mov_t = torch.from_numpy(np.ascontiguousarray(moving, dtype=np.float32)).to(dev)
     uv_t = None
     if uv is not None:
         uv_t = torch.from_numpy(np.ascontiguousarray(np.asarray(uv)[:, :, :2], dtype=np.float32)).to(dev)
-    out = plan.displacement(mov_t, uv_t)
-    torch.cuda.current_stream().synchronize()
-    return out.cpu().numpy()
+    lanes = list(getattr(plan, "plans", [plan]))
+    streams = list(getattr(plan, "streams", [torch.cuda.current_stream()]))
+    per = -(-T // len(lanes))
+    if len(lanes) > 1:
+        per = min(per, plan.lane_frames)
+    else:
+        per = min(T, plan.max_frames)
+    parts = [(t0, min(T, t0 + per)) for t0 in range(0, T, per)]
+    cache_owner = plan
+    st_up = cache_owner.__dict__.get("_st_up")
+    if st_up is None:
+        st_up = cache_owner.__dict__["_st_up"] = torch.cuda.Stream(device=dev)
+        cache_owner.__dict__["_st_down"] = torch.cuda.Stream(device=dev)
+    st_down = cache_owner.__dict__["_st_down"]
+    main = torch.cuda.current_stream()
+    st_up.wait_stream(main)  # the reference and uv uploads above precede the lanes' work
+    out = np.empty((T, m, n, 2), np.float64 if plan.fp64 else np.float32)
+    pending = {}  # lane -> (io, t0, t1) awaiting its copy into `out`
+    mov = np.asarray(moving)
+
+    def drain(li):
+        io, a, b = pending.pop(li)
+        io.down_done.synchronize()
+        out[a:b] = io.pin_out[:b - a].numpy()
+
+    for pi, (t0, t1) in enumerate(parts):
+        li = pi % len(lanes)
+        if li in pending:
+            drain(li)
+        io = _host_io(plan, li, m, n, K, t1 - t0, plan.fp64, dev)
+        if io.up_done is not None:
+            io.up_done.synchronize()
+        k = t1 - t0
+        io.pin_in[:k].numpy()[...] = mov[t0:t1]
+        ls = streams[li]
+        with torch.cuda.stream(st_up):
+            io.dev_in[:k].copy_(io.pin_in[:k], non_blocking=True)
+            io.up_done = torch.cuda.Event()
+            io.up_done.record(st_up)
+        ls.wait_event(io.up_done)
+        ls.wait_stream(main)
+        lanes[li].displacement(io.dev_in[:k], uv_t, io.dev_out[:k], stream=ls)
+        done = torch.cuda.Event()
+        done.record(ls)
+        with torch.cuda.stream(st_down):
+            st_down.wait_event(done)
+            io.pin_out[:k].copy_(io.dev_out[:k], non_blocking=True)
+            io.down_done = torch.cuda.Event()
+            io.down_done.record(st_down)
+        pending[li] = (io, t0, t1)
+    for li in list(pending):
+        drain(li)
+    return out
 
 
 def get_displacement_device(fixed_t, moving_t, uv_t=None, weight_t=None, out_t=None, stream=None,
                             max_frames=None, **options):
     """Device-resident form: fixed_t (H, W, K), moving_t (T, H, W, K) and
     optional uv_t (H, W, 2) / weight_t (H, W, K) are float32 CUDA tensors;
-    returns flow (T, H, W, 2) float32 on the device, enqueued on `stream`."""
+    returns flow (T, H, W, 2) on the device, float64 for precision="fp64"
+    (default) and float32 for "fp32", enqueued on `stream`."""
     _require_cuda()
     T, H, W, K = moving_t.shape
+    options.setdefault("precision", "fp64")
     params = make_params(K=K, **options)
     plan = get_plan(params, H, W, K, T, max_frames)
     key = ("device", fixed_t.data_ptr(), fixed_t._version,
@@ -617,15 +699,15 @@ def imregister_wrapper(f2_level, u, v, f1_level, interpolation_method="cubic"):
 # level_solver seam (core/optical_flow.py:348-411)
 # --------------------------------------------------------------------------
 def level_solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag, verbose, a_data,
-                 a_smooth, hx, hy, gnc_beta=None, precision="fp32"):
+                 a_smooth, hx, hy, gnc_beta=None, precision="fp64"):
     """GPU level solver with the signature of ``level_solver_backend``
     (core/optical_flow.py:348-411).
 
     Runs compute_flow's exact update order on the device and returns (du, dv)
-    as float64 (m, n) arrays.  precision "fp32" is the fast solver
-    (a_smooth = 1, no GNC); "fp64" -- taken as well whenever a_smooth != 1 or
-    gnc_beta is given -- computes in the reference's float64 arithmetic,
-    compute_flow_gnc when gnc_beta is not None.
+    as float64 (m, n) arrays.  precision "fp64" (default; taken as well
+    whenever a_smooth != 1 or gnc_beta is given) computes in the reference's
+    float64 arithmetic, compute_flow_gnc when gnc_beta is not None; "fp32" is
+    the float32 solver (a_smooth = 1, no GNC).
     """
     _require_cuda()
     if precision not in PRECISIONS:

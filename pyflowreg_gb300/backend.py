@@ -28,9 +28,9 @@ SUPPORTED_EXECUTORS = {"sequential", EXECUTOR_NAME}
 
 def _factory(**backend_params):
     """Backend factory, called with ``OFOptions.backend_params``: ``device``
-    selects the CUDA device, ``precision`` is "fp32" (default) or "fp64"
-    (reference precision, the parity mode), ``max_frames`` bounds the device
-    batch of one call."""
+    selects the CUDA device, ``precision`` is "fp64" (default: the reference's
+    precision, flows within 1e-3 px of pyflowreg's) or "fp32" (faster, up to
+    ~0.7 px away), ``max_frames`` bounds the device batch of one call."""
     from functools import partial
 
     from . import api
@@ -43,7 +43,10 @@ def _factory(**backend_params):
         import torch
 
         torch.cuda.set_device(torch.device(dev))
-    return partial(api.get_displacement, precision=backend_params.get("precision", "fp32"))
+    precision = backend_params.get("precision", "fp64")
+    if precision not in api.PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(api.PRECISIONS)}")
+    return partial(api.get_displacement, precision=precision)
 
 
 def register(executor: bool = True) -> None:

@@ -127,6 +127,7 @@ class StreamCompensator:
         self.update_w = update_initialization_w
         self.method = interpolation_method
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        flow_options.setdefault("precision", "fp64")
         self.plan = api.Plan(api.make_params(K=self.K, **flow_options), self.H, self.W, self.K, self.B)
         self.fp64 = self.plan.fp64
         self.ref_raw_t = torch.from_numpy(np.ascontiguousarray(ref, dtype=np.float32)).to(self.dev)

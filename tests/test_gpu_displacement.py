@@ -96,7 +96,7 @@ def test_nonlinear_smoothness_golden_and_fp32_rounding(oracle, golden_dir):
     assert_parity(got, oracle.get_displacement(f["b_fixed"], f["b_moving"], **kw))
     # the committed vector comes from the reference source run without numba
     assert flow_diff(got, f["c_flow"])[0] < 1e-3
-    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], **kw)
+    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], precision="fp32", **kw)
     np.testing.assert_array_equal(got32, got.astype(np.float32).astype(np.float64))
 
 
@@ -109,7 +109,7 @@ def test_fp64_census(oracle, golden_dir, kw):
     kw = dict(const_assumption="cs", **kw)
     got = G.get_displacement(f["b_fixed"], f["b_moving"], precision="fp64", **kw)
     assert_parity(got, oracle.get_displacement(f["b_fixed"], f["b_moving"], **kw))
-    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], **kw)
+    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], precision="fp32", **kw)
     np.testing.assert_array_equal(got32, got.astype(np.float32).astype(np.float64))
 
 
@@ -158,7 +158,7 @@ def test_fp32_min_level_runs_and_stays_close(oracle):
     fixed, moving, _ = pair_256(5, h=96, w=120)
     kw = dict(alpha=(1.5, 1.5), min_level=4, iterations=15)
     base, env_max, env_epe = envelope(oracle, fixed, moving, kw)
-    mx, ep = flow_diff(G.get_displacement(fixed, moving, **kw), base)
+    mx, ep = flow_diff(G.get_displacement(fixed, moving, precision="fp32", **kw), base)
     assert mx <= 2 * env_max + 1e-3 and ep <= 2 * env_epe + 1e-4, (mx, ep, env_max, env_epe)
 
 
@@ -170,7 +170,7 @@ def test_frames_taller_than_512_rows(oracle, h, w):
     kw = dict(alpha=(1.5, 1.5), iterations=10, levels=100)
     base, env_max, env_epe = envelope(oracle, fixed, moving, kw, seeds=(1,))
     assert_parity(G.get_displacement(fixed, moving, precision="fp64", **kw), base)
-    mx, ep = flow_diff(G.get_displacement(fixed, moving, **kw), base)
+    mx, ep = flow_diff(G.get_displacement(fixed, moving, precision="fp32", **kw), base)
     assert mx <= 2 * env_max + 1e-3 and ep <= 2 * env_epe + 1e-4, (mx, ep, env_max, env_epe)
 
 
@@ -199,7 +199,7 @@ def test_fp32_pair_256_within_reference_envelope(oracle):
     fixed, moving, truth = pair_256(0)
     kw = dict(alpha=(1.5, 1.5), levels=100)
     base, env_max, env_epe = envelope(oracle, fixed, moving, kw)
-    got = G.get_displacement(fixed, moving, **kw)
+    got = G.get_displacement(fixed, moving, precision="fp32", **kw)
     mx, ep = flow_diff(got, base)
     assert mx <= 2 * env_max and ep <= 2 * env_epe, (mx, ep, env_max, env_epe)
     # accuracy against the known displacement matches the oracle's
@@ -213,7 +213,7 @@ def test_fp32_matches_fp64_small(oracle, golden_dir):
     """On small frames the amplification is weak: fp32 stays close."""
     f = np.load(f"{golden_dir}/full.npz")
     kw = dict(alpha=(1.5, 1.5))
-    got = G.get_displacement(f["a_fixed"], f["a_moving"], **kw)
+    got = G.get_displacement(f["a_fixed"], f["a_moving"], precision="fp32", **kw)
     mx, ep = flow_diff(got, oracle.get_displacement(f["a_fixed"], f["a_moving"], **kw))
     assert mx <= 2e-2 and ep <= 2e-3, (mx, ep)
 
@@ -238,7 +238,7 @@ def test_many_channels_generic_path(oracle):
     kw = dict(alpha=(1.5, 1.5), iterations=20)
     ref, env_max, env_epe = envelope(oracle, f5, m5.astype(np.float32), kw)
     assert_parity(G.get_displacement(f5, m5.astype(np.float32), precision="fp64", **kw), ref)
-    mx, ep = flow_diff(G.get_displacement(f5, m5.astype(np.float32), **kw), ref)
+    mx, ep = flow_diff(G.get_displacement(f5, m5.astype(np.float32), precision="fp32", **kw), ref)
     assert mx <= 2 * env_max and ep <= 2 * env_epe, (mx, ep, env_max, env_epe)
 
 

@@ -36,7 +36,7 @@ def test_gnc_golden(oracle, golden_dir):
     assert_parity(got, oracle.get_displacement(f["b_fixed"], f["b_moving"], **GOLDEN_KW))
     # the committed vector comes from the reference source run without numba
     assert flow_diff(got, f["g_flow"])[0] < 1e-3
-    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], **GOLDEN_KW)
+    got32 = G.get_displacement(f["b_fixed"], f["b_moving"], precision="fp32", **GOLDEN_KW)
     np.testing.assert_array_equal(got32, got.astype(np.float32).astype(np.float64))
 
 

@@ -112,7 +112,8 @@ def test_stream_compensator_fp32_and_no_w_update():
 
     raw = _video(np.uint16, T=12)
     ref_raw = raw[:4].astype(np.float64).mean(0)
-    sc = StreamCompensator(ref_raw, batch=5, update_initialization_w=False, alpha=(1.5, 1.5), iterations=20)
+    sc = StreamCompensator(ref_raw, batch=5, update_initialization_w=False, alpha=(1.5, 1.5), iterations=20,
+                          precision="fp32")
     flows = {}
     res = sc.run(raw, None, flow_sink=lambda t0, f: flows.__setitem__(t0, f))
     sc.close()
@@ -120,7 +121,7 @@ def test_stream_compensator_fp32_and_no_w_update():
     ref_proc = P.preprocess(ref_raw, None, np.array([1.0, 1.0, 0.1])).astype(np.float32)
     for t0 in sorted(flows):
         proc = P.preprocess(raw[t0:t0 + 5], ref_raw, np.array([1.0, 1.0, 0.1])).astype(np.float32)
-        want = G.get_displacement_batch(ref_proc, proc, alpha=(1.5, 1.5), iterations=20)
+        want = G.get_displacement_batch(ref_proc, proc, alpha=(1.5, 1.5), iterations=20, precision="fp32")
         np.testing.assert_array_equal(flows[t0], want)
     assert res["h2d_bytes"] == raw.nbytes  # uint16 travels as 2 bytes per value
 

@@ -40,7 +40,7 @@ def test_level_solve_matches_lexicographic_oracle(oracle, h, w, K, its, lag):
     J, wgt, u, v = level_inputs(rng, h, w, K, oracle)
     a_data = np.linspace(0.45, 0.6, K)
     ref = oracle.compute_flow(*J, wgt, u, v, 1.7, 2.3, its, lag, a_data, 1.0, 1.25, 0.8)
-    du, dv = G.level_solver(*J, wgt, u, v, (1.7, 2.3), its, lag, 0, a_data, 1.0, 1.25, 0.8)
+    du, dv = G.level_solver(*J, wgt, u, v, (1.7, 2.3), its, lag, 0, a_data, 1.0, 1.25, 0.8, precision="fp32")
     got = np.stack([du, dv], axis=2)
     err = np.abs(got[1:-1, 1:-1] - ref[1:-1, 1:-1]).max()
     scale = np.abs(ref).max()
@@ -55,7 +55,7 @@ def test_red_black_order_is_not_the_reference(oracle):
     a = np.array([0.45])
     lex = oracle.compute_flow(*J, wgt, u, v, 1.5, 1.5, 50, 5, a, 1.0, 1.0, 1.0)
     rb = oracle.compute_flow(*J, wgt, u, v, 1.5, 1.5, 50, 5, a, 1.0, 1.0, 1.0, order=oracle.ORDER_RED_BLACK)
-    du, dv = G.level_solver(*J, wgt, u, v, (1.5, 1.5), 50, 5, 0, a, 1.0, 1.0, 1.0)
+    du, dv = G.level_solver(*J, wgt, u, v, (1.5, 1.5), 50, 5, 0, a, 1.0, 1.0, 1.0, precision="fp32")
     gpu = np.stack([du, dv], axis=2)
     e_gpu = np.abs(gpu - lex)[1:-1, 1:-1].max()
     e_rb = np.abs(rb - lex)[1:-1, 1:-1].max()
