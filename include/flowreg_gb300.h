@@ -129,7 +129,11 @@ int frg_plan_set_level_tables(frg_plan* plan, int level, int kind, int taps, con
  * wavefront pass (0: the most the shared-memory ring holds, reported as gmax)
  * and sor_threads threads per CTA (0: the level's rows rounded up to 32,
  * reported as rows; else a multiple of 32 in [rows, 1024]).  Levels that do
- * not use the fused kernel report gmax 0 and accept only (0, 0). */
+ * not use the fused kernel report gmax 0 and accept only (0, 0).  Levels of an
+ * FP64 plan that run the float64 chained SOR take sor_G = 0 and sor_threads =
+ * the rows per CTA strip: 64, 128 or 256 with at most 8 strips, or 0 to choose
+ * from each call's batch size (the tallest strips that still give every SM a
+ * CTA). */
 int frg_plan_set_level_tuning(frg_plan* plan, int level, int sor_G, int sor_threads);
 int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_threads, int* gmax, int* rows);
 /* Which fused SOR kernel a level runs: 0 the diagonal ring in shared memory

@@ -258,15 +258,20 @@ class Plan:
         _lib.check(self.lib.frg_plan_set_level_variant(self.handle, level, variant), "frg_plan_set_level_variant")
 
     def autotune(self, moving_t, n_levels: int = 5, reps: int = 2):
-        """Picks, for the `n_levels` finest levels that use a fused SOR kernel,
-        the kernel variant, the iterations per wavefront pass and (ring variant)
-        the threads per CTA that make full calls on `moving_t` (a
-        representative device batch) fastest: coordinate descent from the
-        finest level, each candidate timed with CUDA events (best of `reps`).
-        The flows do not depend on the choice.
+        """Launch-shape tuning on `moving_t` (a representative device batch);
+        the flows do not depend on the choice.  fp32 plans: see
+        _autotune_fp32.  fp64 plans: for the `n_levels` finest levels, the
+        rows per CTA strip of the float64 SOR (256, 128 or 64; 0 = chosen
+        from the batch size), each candidate timed with CUDA events on full
+        calls (best of `reps`), coordinate descent from the finest level.
         Returns {level: (variant, sor_G, sor_threads, ms)}."""
-        tun = self.level_tuning()
-        out_t = torch.empty((moving_t.shape[0], self.H, self.W, 2), dtype=torch.float32, device=moving_t.device)
+        if self.fp64:
+            return self._autotune_fp64(moving_t, n_levels, reps)
+        return self._autotune_fp32(moving_t, n_levels, reps)
+
+    def _timer(self, moving_t, reps):
+        odt = torch.float64 if self.fp64 else torch.float32
+        out_t = torch.empty((moving_t.shape[0], self.H, self.W, 2), dtype=odt, device=moving_t.device)
 
         def timed():
             best = float("inf")
@@ -281,6 +286,37 @@ class Plan:
 
         self.displacement(moving_t, None, out_t)
         torch.cuda.synchronize()
+        return timed
+
+    def _autotune_fp64(self, moving_t, n_levels, reps):
+        timed = self._timer(moving_t, reps)
+        tun = self.level_tuning()
+        chosen = {}
+        for i in list(range(len(tun) - 1, -1, -1))[:n_levels]:
+            best = None
+            for rows in (0, 256, 128, 64):
+                try:
+                    self.set_level_tuning(i, 0, rows)
+                except ValueError:
+                    continue
+                ms = timed()
+                if best is None or ms < best[3]:
+                    best = (0, 0, rows, ms)
+            if best is not None:
+                self.set_level_tuning(i, 0, best[2])
+                chosen[i] = best
+        return chosen
+
+    def _autotune_fp32(self, moving_t, n_levels: int = 5, reps: int = 2):
+        """Picks, for the `n_levels` finest levels that use a fused SOR kernel,
+        the kernel variant, the iterations per wavefront pass and (ring variant)
+        the threads per CTA that make full calls on `moving_t` (a
+        representative device batch) fastest: coordinate descent from the
+        finest level, each candidate timed with CUDA events (best of `reps`).
+        The flows do not depend on the choice.
+        Returns {level: (variant, sor_G, sor_threads, ms)}."""
+        tun = self.level_tuning()
+        timed = self._timer(moving_t, reps)
         chosen = {}
         levels = [i for i in range(len(tun) - 1, -1, -1) if tun[i][2] > 0][:n_levels]
         for i in levels:

@@ -277,6 +277,7 @@ struct LevelPlan {
     double* wdiag64 = nullptr;  // (K, D*P) the same, diagonal-major, for the float64 chained SOR
     double* ref64 = nullptr;    // (K, h, w) reference level in float64, for its tensor
     bool chain64 = false;       // fp64 plan: this level runs the float64 chained SOR
+    int rows64 = 0;             // its rows per CTA strip (64, 128, 256); 0: chosen per call from the batch size
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
     int sor_threads = 0;  // fused SOR threads per CTA (0: the level's rows, P)
     int sor_variant = 0;  // fused SOR kernel: 0 diagonal ring in shared memory, 1 rows with the state in registers
@@ -392,6 +393,7 @@ struct frg_plan {
     // FP64 plans with a_smooth = 1, gradient or gray-value constancy and no GNC: the
     // levels the float64 chained SOR serves run it on diagonal-major float64 buffers
     bool dpath = false;
+    int n_sms = 0;            // multiprocessors of the plan's device
     double* dJ = nullptr;     // (T, 6, K, D*P)
     double* dlap = nullptr;   // (T, 2, D*P)
     double* dcoef = nullptr;  // (T, 5, D*P)
@@ -661,6 +663,12 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
                 params->const_assumption != 2 && params->gnc_stages == 0;
     const int n_passes = fill_passes(params->iterations, params->update_lag, kGMax, nullptr, 0);
     size_t max_dp64 = 0;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&pl->n_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            pl->n_sms = 1;
+    }
 
     // schedule: core/optical_flow.py:494-518
     const int m = height, n = width;
@@ -901,6 +909,14 @@ int frg_plan_set_level_tuning(frg_plan* plan, int level, int sor_G, int sor_thre
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     LevelPlan& L = plan->levels[level];
+    if (L.chain64) {
+        // float64 chained SOR: sor_threads = rows per CTA strip (0: chosen from the batch size)
+        if (sor_G != 0) return fail(FRG_EINVAL, "the float64 SOR has no pass-length setting (sor_G must be 0)");
+        if (sor_threads != 0 && !sor_chain64_rows_ok(L.g, sor_threads))
+            return fail(FRG_EINVAL, "sor_threads must be 0, 64, 128 or 256 with at most 8 strips for this level");
+        L.rows64 = sor_threads;
+        return FRG_OK;
+    }
     if (sor_kind(plan->K, L.g) != kSorFused) {
         if (sor_G != 0 || sor_threads != 0) return fail(FRG_EINVAL, "this level does not use the fused SOR kernel");
         return FRG_OK;
@@ -918,6 +934,13 @@ int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_
 {
     if (!plan || level < 0 || level >= (int)plan->levels.size()) return fail(FRG_EINVAL, "bad level");
     const LevelPlan& L = plan->levels[level];
+    if (L.chain64) {
+        if (sor_G) *sor_G = 0;
+        if (sor_threads) *sor_threads = L.rows64;
+        if (gmax) *gmax = 0;
+        if (rows) *rows = L.g.P;
+        return FRG_OK;
+    }
     const bool fused = sor_kind(plan->K, L.g) == kSorFused;
     if (sor_G) *sor_G = L.sor_G;
     if (sor_threads) *sor_threads = L.sor_threads;
@@ -1255,9 +1278,10 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
                 int rc = record_event(&pl->prof, st);
                 if (rc) return rc;
             }
+            const int rows = L.rows64 ? L.rows64 : sor_chain64_default_rows(L.g, T, pl->n_sms);
             FRG_LAUNCH(launch_sor_chain64(pl->dJ, 6LL * K * dp, L.wdiag64, 0, pl->dlap, 2 * dp, pl->dcoef, 5 * dp,
                                           pl->ddu, pl->ddv, dp, T, K, L.g, cp, np, pl->a_data64, wx, wy, pl->p.omega,
-                                          st, pl->xdu + (w + 2) + 1, pl->xdv + (w + 2) + 1, mn, w + 2));
+                                          st, pl->xdu + (w + 2) + 1, pl->xdv + (w + 2) + 1, mn, w + 2, rows));
             if (timed) {
                 int rc = record_event(&pl->prof, st);
                 if (rc) return rc;

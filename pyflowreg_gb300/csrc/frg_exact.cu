@@ -21,6 +21,22 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// float -> double on the integer pipe: the conversion instruction runs on the
+// float64 pipe (GB300: 1/64 of the float32 rate), while a normal float's bits
+// map to the double's by a re-biased exponent and a shifted fraction.  Exact;
+// zeros likewise; subnormals, infinities and NaN take the conversion.
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) {
+        if ((b << 1) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+        return (double)f;
+    }
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b >> 3) & 0xfffffu);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
 // ---------------------------------------------------------------------------
 // Resize with numba typing (util/resize_util.py:116-141): float32 input and
 // products, float64 accumulator, float32 result (stored as float or double).
@@ -39,7 +55,7 @@ __global__ void kx_resize_h(const Tin* __restrict__ src, long long fs, long long
     double s = 0.0;
     for (int p = 0; p < P; ++p) {
         const float a = (float)row[(long long)ix[(long long)x * P + p] * cs];
-        s = dadd(s, (double)__fmul_rn(a, wx[(long long)x * P + p]));
+        s = dadd(s, f2d(__fmul_rn(a, wx[(long long)x * P + p])));
     }
     dst[((long long)fp * ih + y) * ow + x] = (float)s;
 }
@@ -68,7 +84,7 @@ __global__ void kx_resize_v(const float* __restrict__ src, int n_planes, int ih,
     const float* col = src + (long long)fp * ih * ow + x;
     double s = 0.0;
     for (int p = 0; p < P; ++p)
-        s = dadd(s, (double)__fmul_rn(col[(long long)iy[(long long)y * P + p] * ow], wy[(long long)y * P + p]));
+        s = dadd(s, f2d(__fmul_rn(col[(long long)iy[(long long)y * P + p] * ow], wy[(long long)y * P + p])));
     *out = (Tout)(float)s;
 }
 
@@ -154,7 +170,9 @@ __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ 
             for (int j = 0; j < 4; ++j) {
                 const int xx = xclamp(ix - 1 + j, 0, w - 1);
                 const float w2 = __fmul_rn(cx_cubic[fy * 4 + i], cx_cubic[fx * 4 + j]);
-                acc = dadd(acc, dmul((double)src[(long long)yy * w + xx], (double)w2));
+                // the product of two floats is exact in double, so the fused form rounds as
+                // dadd(acc, dmul(...)) does
+                acc = __fma_rn(f2d(src[(long long)yy * w + xx]), f2d(w2), acc);
             }
         }
         *dst = (float)acc;
@@ -368,12 +386,12 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
     auto A = [&](int yy, int xx) { return a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
     auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
     auto gx2 = [&](int yy, int xx) {
-        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), C.h2x_f);
-        return dmul(dsub((double)Bf(yy, xx + 1), (double)Bf(yy, xx - 1)), C.ihx2);
+        if (f2_f32) return f2d(__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), C.h2x_f));
+        return dmul(dsub(f2d(Bf(yy, xx + 1)), f2d(Bf(yy, xx - 1))), C.ihx2);
     };
     auto gy2 = [&](int yy, int xx) {
-        if (f2_f32) return (double)__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), C.h2y_f);
-        return dmul(dsub((double)Bf(yy + 1, xx), (double)Bf(yy - 1, xx)), C.ihy2);
+        if (f2_f32) return f2d(__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), C.h2y_f));
+        return dmul(dsub(f2d(Bf(yy + 1, xx)), f2d(Bf(yy - 1, xx))), C.ihy2);
     };
     auto FX = [&](int yy, int xx) {
         yy = xclamp(yy, 1, h);
@@ -388,7 +406,7 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
     auto FT = [&](int yy, int xx) {
         yy = xclamp(yy, 1, h);
         xx = xclamp(xx, 1, w);
-        return dsub((double)Bf(yy, xx), A(yy, xx));
+        return dsub(f2d(Bf(yy, xx)), A(yy, xx));
     };
     if (gray) {
         const double fxv = FX(yo, xo), fyv = FY(yo, xo), ftv = FT(yo, xo);
@@ -408,14 +426,14 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
     const double fyy1 = dmul(dadd(dsub(A(yo - 1, xo), dadd(a0, a0)), A(yo + 1, xo)), C.ihyy);
     double fxx2, fyy2;
     if (f2_f32) {
-        fxx2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)),
-                                 C.hxx_f);
-        fyy2 = (double)__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)),
-                                 C.hyy_f);
+        fxx2 = f2d(__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)),
+                             C.hxx_f));
+        fyy2 = f2d(__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo - 1, xo), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo + 1, xo)),
+                             C.hyy_f));
     } else {
-        const double b0 = (double)Bf(yo, xo);
-        fxx2 = dmul(dadd(dsub((double)Bf(yo, xo - 1), dadd(b0, b0)), (double)Bf(yo, xo + 1)), C.ihxx);
-        fyy2 = dmul(dadd(dsub((double)Bf(yo - 1, xo), dadd(b0, b0)), (double)Bf(yo + 1, xo)), C.ihyy);
+        const double b0 = f2d(Bf(yo, xo));
+        fxx2 = dmul(dadd(dsub(f2d(Bf(yo, xo - 1)), dadd(b0, b0)), f2d(Bf(yo, xo + 1))), C.ihxx);
+        fyy2 = dmul(dadd(dsub(f2d(Bf(yo - 1, xo)), dadd(b0, b0)), f2d(Bf(yo + 1, xo))), C.ihyy);
     }
     const double fxx = dmul(0.5, dadd(fxx1, fxx2));
     const double fyy = dmul(0.5, dadd(fyy1, fyy2));

@@ -125,12 +125,17 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
 // state du, dv [D*P] are diagonal-major doubles; the final pass writes du, dv
 // at out + r * out_rs + c.  Levels of at most 2048 (padded) rows (over 256 as
 // clusters of row strips), K <= 4, w >= 3, at most kMaxChain passes of G <= kGMax.
+// rows: the most rows per CTA (64, 128 or 256; 0 = 256), the level split into at
+// most 8 strips; every split gives the same bits.
 bool sor_chain64_supports(int K, const DiagGeom& g, int n_passes);
+bool sor_chain64_rows_ok(const DiagGeom& g, int rows);
+int sor_chain64_default_rows(const DiagGeom& g, int n_frames, int n_sms);
 cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W, long long W_fs, const double* lap,
                                long long lap_fs, double* coef, long long coef_fs, double* du, double* dv,
                                long long st_fs, int n_frames, int K, DiagGeom g, const ChainPass* passes,
                                int n_passes, const double* a_data, double wx, double wy, double omega,
-                               cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs);
+                               cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs,
+                               int rows = 0);
 // x^b elementwise by the float64 solver's table-driven power (frg_dpow.cuh);
 // upload_dpow_tables must have run on the current device.
 cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cudaStream_t st);

@@ -21,10 +21,11 @@
 // folded once per pass when the pixel enters and wait in a shared-memory ring
 // of 2G - 1 slots until its last update of the pass.
 //
-// One thread per row, at most 256 rows per CTA (the float64 state and
-// prefetch need up to 255 registers per thread); taller levels run as a
-// thread-block cluster of row strips whose edge rows exchange their values
-// through distributed shared memory, with a cluster barrier per step.
+// One thread per row, at most 256, 128 or 64 rows per CTA (a launch choice:
+// the shorter strips fit three or six CTAs per SM, or spread a single frame
+// over more SMs); taller levels run as a thread-block cluster of row strips
+// whose edge rows exchange their values through distributed shared memory,
+// with a cluster barrier per step.
 #include "frg_internal.h"
 #include "frg_dpow.cuh"
 
@@ -86,7 +87,7 @@ cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cu
 
 namespace {
 
-constexpr int kLane64 = 256;       // rows (threads) per CTA
+constexpr int kLane64 = 256;       // most rows (threads) per CTA
 constexpr int kG64 = kGMax;        // iterations pipelined per pass, as a template maximum
 constexpr int kSmem64 = 232448;    // 227 KB of dynamic shared memory per CTA
 constexpr int kMaxStrips64 = 8;    // portable cluster size
@@ -123,31 +124,59 @@ struct Chain64Table {
 
 constexpr int kPkZero = 1, kPkTick = 2, kPkCoef = 4, kPkStore = 8;
 
+// The fold's inputs of one pixel (J, W, lap; or the stored coefficients),
+// loaded at the start of the step whose end folds them: a step of float64
+// work takes several microseconds, far longer than the loads.
 template <int K>
-struct Raw64 {
+struct FoldIn64 {
     double j[6 * K];
     double w[K];
-    double lu, lv, du, dv;
+    double lu, lv;
 };
 
-template <int K>
+// Pass-start state, prefetched two steps ahead: du, dv of pixel (r, c) entering
+// the ring and of pixel (r + 1, c - 1) below its left neighbour.
 struct Pre64 {
-    Raw64<K> raw;   // pixel (r, c) entering the ring
-    double nu, nv;  // pass-start du, dv of pixel (r + 1, c - 1)
+    double du, dv, nu, nv;
 };
 
 struct Coef64 {
     double A12, BU, BV, iDu, iDv;
 };
 
+// 1 / x for a normal x: the hardware approximation (rcp.approx.ftz.f64, about
+// 2^-22 relative) refined by two Newton steps y += y (1 - x y), each doubling
+// the correct bits, to within an ulp: 4 float64 operations where a division
+// costs about 7.
+__device__ __forceinline__ double rcp64(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = __fma_rn(-x, y, 1.0);
+    y = __fma_rn(y, e, y);
+    e = __fma_rn(-x, y, 1.0);
+    return __fma_rn(y, e, y);
+}
+
+// omega / den, 0 when den is 0 (core/level_solver.py:352, 363); subnormal,
+// infinite or NaN denominators take the division.
+__device__ __forceinline__ double omega_over(double omega, double den)
+{
+    if (den == 0.0) return 0.0;
+    const int ex = __double2hiint(den) & 0x7ff00000;
+    if (ex == 0 || ex == 0x7ff00000) return __ddiv_rn(omega, den);
+    return __dmul_rn(omega, rcp64(den));
+}
+
 // Coefficients of one pixel for a pass (core/level_solver.py:229-255, 309-364):
-// with psi at a tick from the pixel's pass-start du, dv (E as a chain of fused
-// multiply-adds; the reference adds J23 dv twice), psi = 1 on the first pass,
-// or the stored coefficients of the group's first pass.
+// with psi at a tick from the pixel's pass-start du, dv (E in nested fused
+// multiply-adds; the reference adds J23 dv twice, hence 2 J23), psi = 1 on the
+// first pass, or the stored coefficients of the group's first pass.
 //   A12 = sum_k W psi J12,  BU = lap_u - sum_k W psi J13,  BV = lap_v - sum_k W psi J23,
-//   iDu = omega / (wsum + sum_k W psi J11) (0 when the denominator is 0), iDv likewise.
+//   iDu = omega / (wsum + sum_k W psi J11) (0 when the denominator is 0), iDv likewise
+//   (omega times the reciprocal: within an ulp or two of the quotient).
 template <int K, bool CO>
-__device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const Raw64<K>& r)
+__device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldIn64<K>& r, double du, double dv)
 {
     Coef64 o;
     if (CO && (pk & kPkCoef)) {
@@ -166,12 +195,12 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const Raw64
         const double j12 = r.j[3 * K + k], j13 = r.j[4 * K + k], j23 = r.j[5 * K + k];
         double wp = r.w[k];
         if (tick) {
-            const double a = r.du, b = r.dv;
-            double E = __fma_rn(__dadd_rn(j13, j13), a, j33);
-            E = __fma_rn(__dadd_rn(j23, j23), b, E);
-            E = __fma_rn(__dmul_rn(__dadd_rn(j12, j12), a), b, E);
-            E = __fma_rn(__dmul_rn(j22, b), b, E);
-            E = __fma_rn(__dmul_rn(j11, a), a, E);
+            const double a = du, b = dv;
+            // E = a (J11 a + 2 J12 b + 2 J13) + b (J22 b + 2 J23) + J33: 8 float64 operations
+            double t = __fma_rn(j11, a, __dadd_rn(j13, j13));
+            t = __fma_rn(__dadd_rn(j12, j12), b, t);
+            const double q = __fma_rn(j22, b, __dadd_rn(j23, j23));
+            double E = __fma_rn(t, a, __fma_rn(q, b, j33));
             E = fmax(E, 0.0);
             wp = __dmul_rn(wp, __dmul_rn(A.a_data[k], dpow_tab(__dadd_rn(E, 0.00001), A.a_m1[k])));
         }
@@ -184,8 +213,8 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const Raw64
     o.A12 = a12;
     o.BU = __dsub_rn(r.lu, c13);
     o.BV = __dsub_rn(r.lv, c23);
-    o.iDu = den_u != 0.0 ? __ddiv_rn(A.omega, den_u) : 0.0;
-    o.iDv = den_v != 0.0 ? __ddiv_rn(A.omega, den_v) : 0.0;
+    o.iDu = omega_over(A.omega, den_u);
+    o.iDv = omega_over(A.omega, den_v);
     return o;
 }
 
@@ -216,8 +245,16 @@ size_t chain64_smem(int nt)
            (size_t)(2 * (nt / 32) * 2 * kG64 + 2 * 2 * kG64) * sizeof(double2);
 }
 
-template <int K, bool CO, bool CL>
-__global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Table T)
+// NTM: the most rows (threads) of one CTA, 256, 128 or 64.  The launch bounds
+// ask for 1, 3 or 6 CTAs per SM (at most 255 or 170 registers per thread), so
+// shorter strips keep 12 warps per SM where 256-row CTAs keep 8.
+template <int NT>
+struct StripBounds {
+    static constexpr int blocks = NT >= 256 ? 1 : (NT >= 128 ? 3 : 6);
+};
+
+template <int K, bool CO, bool CL, int NTM>
+__global__ void __launch_bounds__(NTM, StripBounds<NTM>::blocks) k_sor_chain64(Sor64Args A, Chain64Table T)
 {
     constexpr int G = kG64;
     constexpr int S = 2 * G - 1;
@@ -252,34 +289,40 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
         return w + (G_p > 1 ? 2 * (G_p - 1) : 1);
     };
 
-    // inputs of the pixel entering at column c of a pass with flags pk, and the
-    // pass-start value of the pixel below its left neighbour
-    auto fetch = [&](int c, int pk, Pre64<K>& p) {
+    // pass-start state of the pixel entering at column c of a pass with flags pk,
+    // and of the pixel below its left neighbour
+    auto fetch_state = [&](int c, int pk, Pre64& p) {
         const bool zero = (pk & kPkZero) != 0;
         const int o = (r + c) * P;
         if (row_ok && c >= 0 && c < w) {
-            if (CO && (pk & kPkCoef)) {
-#pragma unroll
-                for (int q = 0; q < 5; ++q) p.raw.j[q] = coefr[q * pl + o];
-            } else {
-#pragma unroll
-                for (int q = 0; q < 6 * K; ++q) p.raw.j[q] = Jr[q * pl + o];
-#pragma unroll
-                for (int k = 0; k < K; ++k) p.raw.w[k] = Wr[k * pl + o];
-                p.raw.lu = lapr[o];
-                p.raw.lv = lapr[pl + o];
-            }
-            p.raw.du = zero ? 0.0 : dur[o];
-            p.raw.dv = zero ? 0.0 : dvr[o];
+            p.du = zero ? 0.0 : dur[o];
+            p.dv = zero ? 0.0 : dvr[o];
         }
         if (has_below && c >= 1 && c <= w) {
             p.nu = zero ? 0.0 : dur[o + 1];
             p.nv = zero ? 0.0 : dvr[o + 1];
         }
     };
-    auto fold_into = [&](int c, int pk, const Pre64<K>& p, int slot) {
+    // fold inputs of the pixel at column c of a pass with flags pk
+    auto fetch_fold = [&](int c, int pk, FoldIn64<K>& f) {
+        const int o = (r + c) * P;
         if (row_ok && c >= 0 && c < w) {
-            const Coef64 cf = fold64<K, CO>(A, pk, p.raw);
+            if (CO && (pk & kPkCoef)) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) f.j[q] = coefr[q * pl + o];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 6 * K; ++q) f.j[q] = Jr[q * pl + o];
+#pragma unroll
+                for (int k = 0; k < K; ++k) f.w[k] = Wr[k * pl + o];
+                f.lu = lapr[o];
+                f.lv = lapr[pl + o];
+            }
+        }
+    };
+    auto fold_into = [&](int c, int pk, const FoldIn64<K>& f, const Pre64& p, int slot) {
+        if (row_ok && c >= 0 && c < w) {
+            const Coef64 cf = fold64<K, CO>(A, pk, f, p.du, p.dv);
             if (CO && (pk & kPkStore)) {
                 const int o = (r + c) * P;
                 coefr[o] = cf.A12;
@@ -306,10 +349,14 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
     int pk_cur = T.pk[0];
     int pk_nxt = last > 0 ? T.pk[1] : 0;
     int cend = span(pk_cur);
-    Pre64<K> pre[2];
-    fetch(-r, pk_cur, pre[0]);
-    fetch(1 - r, pk_cur, pre[1]);
-    fold_into(-r, pk_cur, pre[0], 0);
+    Pre64 pre[2];
+    fetch_state(-r, pk_cur, pre[0]);
+    fetch_state(1 - r, pk_cur, pre[1]);
+    {
+        FoldIn64<K> f0;
+        fetch_fold(-r, pk_cur, f0);
+        fold_into(-r, pk_cur, f0, pre[0], 0);
+    }
     double2 V0[G], V1[G], V2[G];
 #pragma unroll
     for (int gi = 0; gi < G; ++gi) V0[gi] = V1[gi] = V2[gi] = make_double2(0.0, 0.0);
@@ -323,8 +370,8 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
         for (int q = 0; q < 2; ++q) {
             const int s = s0 + q;
             if (s < nsteps) {
-                Pre64<K>& cur = pre[q];      // the pixel entering at step s
-                Pre64<K>& nxt = pre[q ^ 1];  // the pixel entering at step s + 1
+                Pre64& cur = pre[q];      // the pixel entering at step s
+                Pre64& nxt = pre[q ^ 1];  // the pixel entering at step s + 1
                 const int slot1 = slot0 + 1 == S ? 0 : slot0 + 1;
                 const int tau = s - r;
                 if (tau >= cend && cp < last) {
@@ -339,10 +386,14 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
                 const int Gp = pk_cur >> 8;
                 const bool final_out = !more && odu != nullptr;
                 const int c0 = tau - cstart;
-                const double2 ps0 = make_double2(cur.raw.du, cur.raw.dv);
-                const double2 ps1 = make_double2(nxt.raw.du, nxt.raw.dv);
+                const int c_f = f_nx ? tau + 1 - cend : c0 + 1;  // the pixel folded at the end of this step
+                const int pk_f = f_nx ? pk_nxt : pk_cur;
+                FoldIn64<K> fin;
+                fetch_fold(c_f, pk_f, fin);
+                const double2 ps0 = make_double2(cur.du, cur.dv);
+                const double2 ps1 = make_double2(nxt.du, nxt.dv);
                 const double2 dn1 = make_double2(nxt.nu, nxt.nv);
-                fetch(e_nx ? tau + 2 - cend : c0 + 2, e_nx ? pk_nxt : pk_cur, cur);
+                fetch_state(e_nx ? tau + 2 - cend : c0 + 2, e_nx ? pk_nxt : pk_cur, cur);
                 const int pin = (s + 1) & 1;  // parity written at step s - 1
 #pragma unroll
                 for (int gj = 0; gj < G; ++gj) {
@@ -382,7 +433,7 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
                         }
                     }
                 }
-                fold_into(f_nx ? tau + 1 - cend : c0 + 1, f_nx ? pk_nxt : pk_cur, nxt, slot1);
+                fold_into(c_f, pk_f, fin, nxt, slot1);
                 const int pout = s & 1;
                 if (lane == 31) {
 #pragma unroll
@@ -416,22 +467,23 @@ __global__ void __launch_bounds__(kLane64) k_sor_chain64(Sor64Args A, Chain64Tab
     }
 }
 
-// Row strips of a level: one CTA up to 256 rows, else nc <= 8 CTAs of nt rows.
-void split64(const DiagGeom& g, int* nc, int* nt)
+// Row strips of a level with at most `rows` rows per CTA (256, 128 or 64): one
+// CTA when the level fits, else nc CTAs of nt rows (a cluster when nc > 1).
+void split64(const DiagGeom& g, int rows, int* nc, int* nt)
 {
-    const int n = (g.P + kLane64 - 1) / kLane64;
+    const int n = (g.P + rows - 1) / rows;
     *nc = n;
     *nt = ((g.P + n - 1) / n + 31) / 32 * 32;
 }
 
-template <int K, bool CO, bool CL>
+template <int K, bool CO, bool CL, int NTM>
 cudaError_t run_chain64_t(const Sor64Args& A, const Chain64Table& T, int n_frames, int nt, cudaStream_t st)
 {
     const size_t smem = chain64_smem(nt);
-    const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_chain64<K, CO, CL>, kSmem64);
+    const cudaError_t e = ensure_max_dyn_smem((const void*)k_sor_chain64<K, CO, CL, NTM>, kSmem64);
     if (e != cudaSuccess) return e;
     if constexpr (!CL) {
-        k_sor_chain64<K, CO, false><<<n_frames, nt, smem, st>>>(A, T);
+        k_sor_chain64<K, CO, false, NTM><<<n_frames, nt, smem, st>>>(A, T);
         return cudaGetLastError();
     } else {
         cudaLaunchConfig_t cfg = {};
@@ -446,27 +498,57 @@ cudaError_t run_chain64_t(const Sor64Args& A, const Chain64Table& T, int n_frame
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, k_sor_chain64<K, CO, true>, A, T);
+        return cudaLaunchKernelEx(&cfg, k_sor_chain64<K, CO, true, NTM>, A, T);
     }
+}
+
+template <int K, int NTM>
+cudaError_t run_chain64_n(const Sor64Args& A, const Chain64Table& T, bool co, int n_frames, int nt, cudaStream_t st)
+{
+    if (A.nc == 1)
+        return co ? run_chain64_t<K, true, false, NTM>(A, T, n_frames, nt, st)
+                  : run_chain64_t<K, false, false, NTM>(A, T, n_frames, nt, st);
+    return co ? run_chain64_t<K, true, true, NTM>(A, T, n_frames, nt, st)
+              : run_chain64_t<K, false, true, NTM>(A, T, n_frames, nt, st);
 }
 
 template <int K>
 cudaError_t run_chain64(const Sor64Args& A, const Chain64Table& T, bool co, int n_frames, int nt, cudaStream_t st)
 {
-    if (A.nc == 1)
-        return co ? run_chain64_t<K, true, false>(A, T, n_frames, nt, st)
-                  : run_chain64_t<K, false, false>(A, T, n_frames, nt, st);
-    return co ? run_chain64_t<K, true, true>(A, T, n_frames, nt, st)
-              : run_chain64_t<K, false, true>(A, T, n_frames, nt, st);
+    if (nt <= 64) return run_chain64_n<K, 64>(A, T, co, n_frames, nt, st);
+    if (nt <= 128) return run_chain64_n<K, 128>(A, T, co, n_frames, nt, st);
+    return run_chain64_n<K, 256>(A, T, co, n_frames, nt, st);
 }
 
 }  // namespace
+
+bool sor_chain64_rows_ok(const DiagGeom& g, int rows)
+{
+    if (rows != 64 && rows != 128 && rows != kLane64) return false;
+    int nc, nt;
+    split64(g, rows, &nc, &nt);
+    return nc <= kMaxStrips64 && chain64_smem(nt) <= (size_t)kSmem64;
+}
+
+int sor_chain64_default_rows(const DiagGeom& g, int n_frames, int n_sms)
+{
+    // the tallest strips that still give every SM work; shorter strips where a
+    // batch of few frames would leave SMs idle (one frame per call: 8 strips)
+    for (int rows = kLane64; rows >= 64; rows /= 2) {
+        if (!sor_chain64_rows_ok(g, rows)) break;
+        const long long ctas = (long long)n_frames * ((g.P + rows - 1) / rows);
+        if (ctas >= n_sms) return rows;
+    }
+    for (int rows = 64; rows <= kLane64; rows *= 2)
+        if (sor_chain64_rows_ok(g, rows)) return rows;
+    return kLane64;
+}
 
 bool sor_chain64_supports(int K, const DiagGeom& g, int n_passes)
 {
     if (K < 1 || K > 4 || (g.P & 31) || g.w < 3 || n_passes < 1 || n_passes > kMaxChain) return false;
     int nc, nt;
-    split64(g, &nc, &nt);
+    split64(g, kLane64, &nc, &nt);
     // 32-bit offsets within a frame: the largest plane index read is (6K + 2) planes of D * P
     const long long plane = (long long)g.D * g.P;
     return nc <= kMaxStrips64 && plane * (6 * K + 2) < 0x7fffffffLL && chain64_smem(nt) <= (size_t)kSmem64;
@@ -476,11 +558,14 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
                                long long lap_fs, double* coef, long long coef_fs, double* du, double* dv,
                                long long st_fs, int n_frames, int K, DiagGeom g, const ChainPass* passes,
                                int n_passes, const double* a_data, double wx, double wy, double omega,
-                               cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs)
+                               cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs,
+                               int rows)
 {
     if (!sor_chain64_supports(K, g, n_passes) || n_frames < 1) return cudaErrorInvalidValue;
+    if (rows == 0) rows = kLane64;
+    if (!sor_chain64_rows_ok(g, rows)) return cudaErrorInvalidValue;
     int nc = 0, nt = 0;
-    split64(g, &nc, &nt);
+    split64(g, rows, &nc, &nt);
     if ((long long)n_frames * nc > 0x7fffffffLL) return cudaErrorInvalidValue;
     Chain64Table T;
     T.n = n_passes;

@@ -11,7 +11,7 @@ reference's own code.
 
 Run it where the reference source is available:
 
-    python tests/golden/make_golden.py [path/to/pyflowreg/src]
+    python tests/golden/make_golden.py <path/to/pyflowreg/src>
 
 The outputs are small (< 100 KB each) and are committed; tests never import
 the reference.
@@ -26,7 +26,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py <path/to/pyflowreg/src>")
+REF_SRC = sys.argv[1]
 
 
 def blobs(rng, h, w, n=12, bg=0.05):

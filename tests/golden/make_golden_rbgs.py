@@ -14,7 +14,7 @@ the reference torch backend that the differentiable mode is checked against
 
 Run where the reference source is available (tests never import it):
 
-    python tests/golden/make_golden_rbgs.py [path/to/pyflowreg/src]
+    python tests/golden/make_golden_rbgs.py <path/to/pyflowreg/src>
 """
 
 from __future__ import annotations
@@ -28,7 +28,9 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden_rbgs.py <path/to/pyflowreg/src>")
+REF_SRC = sys.argv[1]
 
 
 class _TorchWithGrad:
