@@ -4,13 +4,17 @@ One step = one pass of get_displacement over one batch of frames (default
 400, pyflowreg's OFOptions.buffer_size) against the reference frame (mean of
 the first 50 frames), with pyflowreg's default flow options (alpha 1.5,
 eta 0.8, 50 iterations, update_lag 5, a_data 0.45, gradient constancy,
-quality preset -> min_level 0, channel weights 0.5/0.5).
+quality preset -> min_level 0, channel weights 0.5/0.5), in the reference's
+float64 precision (the parity path; --precision fp32 times the float32 path).
 
 Prints one JSON line.  ``value`` is frames/s with the batch resident in HBM
 (the batch's frame ranges on the lanes of the cached plan, each lane running
-the steps on its own stream); ``e2e`` is the same with the batch in pinned
-host memory and the flows copied back, copies inside the timed region (one
-chunk per lane, on copy streams overlapping compute).
+the steps on its own stream); ``e2e`` is the same batch through the
+reference-facing call with host arrays (numpy frames in, numpy flows out,
+host<->device copies inside the timed region).  ``parity`` compares the timed
+flows with the CPU oracle on a sample; ``fp32_fast_path`` is the float32
+path on the same batch; ``reference_gpu`` times pyflowreg's own GPU level
+solver on the same frame size.
 ``--impl reference`` times the CPU oracle (a restatement of pyflowreg's
 numba path; pyflowreg itself cannot run here) on the host cores instead.
 
@@ -50,6 +54,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
+                    help="the timed path: fp64 (the reference's precision, within the parity tolerance) or fp32")
+    ap.add_argument("--no-fp32-secondary", dest="fp32_secondary", action="store_false",
+                    help="skip the secondary float32 measurement")
+    ap.add_argument("--reference-gpu-frames", type=int, default=2,
+                    help="frames of pyflowreg's own GPU level solver timed beside the CPU baseline; 0 skips")
+    ap.add_argument("--cpu-fastmath", action="store_true",
+                    help="also time the -ffast-math build of the oracle (numba fastmath analogue)")
     ap.add_argument("--frames", type=int, default=400, help="frames per step and rank")
     ap.add_argument("--plain-frames", type=int, default=8, help="frames timed in the one-frame-per-call form")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames of the CPU baseline sample (0: one per core)")
@@ -191,6 +203,7 @@ def run_uneven(args, dev):
             frames.append(preprocess_torch(vid.frame(t), ref_raw).contiguous())
     opts = dict(OPTIONS)
     opts.pop("min_level", None)
+    opts["precision"] = "fp32"
     ub = UnevenBatch({k: v[2] for k, v in refs.items()}, graphs=True, **opts)
     ub.register(frames)  # plans, graph capture
     torch.cuda.synchronize()
@@ -205,7 +218,7 @@ def run_uneven(args, dev):
     ms = e0.elapsed_time(e1) / reps
     ub.close()
     counts = {f"{k[0]}x{k[1]}x{k[2]}": v for k, v in sorted(counters.items())}
-    return {"workload": f"{len(frames)} frames of mixed size and channels, one register() call",
+    return {"workload": f"{len(frames)} frames of mixed size and channels, one register() call", "precision": "fp32",
             "frames_per_size": counts, "ms_per_batch": ms, "frames_per_s": len(frames) / (ms / 1e3),
             "graphs": True, "streams": 4}
 
@@ -273,6 +286,7 @@ def run_stream(args, dev):
         del frames_raw
     opts = dict(OPTIONS)
     opts.pop("min_level", None)
+    opts["precision"] = "fp32"
     sr = StreamRegistrar(refp, batch=B, **opts)
     sink_count = [0]
     # frames compared with the oracle: one per batch after the first, at its middle; each
@@ -299,6 +313,7 @@ def run_stream(args, dev):
     dt = time.perf_counter() - t0
     sr.close()
     stream = {"workload": f"{N} x 2048x2048x2 frames, batches of {B}, pinned host in/out, copies on a side stream",
+              "precision": "fp32",
               "frames_per_s": N / dt, "seconds": dt, "h2d_bytes": info["h2d_bytes"], "d2h_bytes": info["d2h_bytes"],
               "timing": "wall clock around StreamRegistrar.run after a warm-up run"}
     if n_epe:
@@ -359,7 +374,8 @@ def run_compensate(raw_u16, ref_raw, B, opts):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     sc.close()
-    return {"workload": f"{N} x 2048x2048x2 uint16 frames through the streamed compensate loop, batches of {B}: "
+    return {"precision": opts.get("precision", "fp64"),
+            "workload": f"{N} x 2048x2048x2 uint16 frames through the streamed compensate loop, batches of {B}: "
                         "preprocess, initial field, flows, compensation warp, statistics, registered frames and "
                         "flows to the host",
             "frames_per_s": N / dt, "seconds": dt, "frames_written": writer.frames,
@@ -441,13 +457,15 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of the SOR kernel from the committed ncu summary."""
+def profiled_traffic(fp64=False):
+    """DRAM bytes per algorithmic byte of the SOR kernel (float64 or float32)
+    from the committed ncu summary."""
     path = os.path.join(REPO, "profiles", "dram_traffic.txt")
+    key = "k_sor_chain64" if fp64 else "k_sor"
     try:
         for line in open(path):
             parts = line.split()
-            if len(parts) >= 3 and parts[0] == "k_sor" and parts[1] == "bytes_per_algorithmic_byte":
+            if len(parts) >= 3 and parts[0] == key and parts[1] == "bytes_per_algorithmic_byte":
                 return float(parts[2])
     except OSError:
         pass
@@ -457,49 +475,105 @@ def profiled_traffic():
 # --------------------------------------------------------------------------
 # GB300 arm
 # --------------------------------------------------------------------------
-def run_gb300(args):
+def run_reference_gpu(args, dev, levels):
+    """pyflowreg's own GPU path on this GPU: the flowreg_torch backend
+    (core/__init__.py:140-197) runs get_displacement with its level solver
+    level_solver_rbgs_torch (torch/core/level_solver.py:11-199) on the device
+    in float64, each level's arrays copied to the device and du, dv back.
+    That solver, loaded unmodified from the installed pyflowreg, is timed here
+    on one 512x512x2 frame's levels with those copies; the numba pyramid,
+    warp, tensor and median the backend runs around it on the CPU are not
+    (numba is absent), so the figure bounds the backend's frame rate from
+    above."""
+    import importlib.util
+
     import torch
-    import torch.distributed as dist
 
-    import pyflowreg_gb300 as G
-    from pyflowreg_gb300 import _lib
+    path = os.path.join(REPO, "baseline", "_ref", "pyflowreg", "torch", "core", "level_solver.py")
+    if not os.path.exists(path):
+        return {"unavailable": "pyflowreg is not installed in baseline/_ref"}
+    spec = importlib.util.spec_from_file_location("pyflowreg_reference_torch_level_solver", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    rng = np.random.default_rng(0)
+    inputs = []
+    for (h, w, ax, ay) in levels:
+        m, n = h + 2, w + 2
+        J = [np.abs(rng.standard_normal((m, n, K))) for _ in range(3)] + \
+            [0.1 * rng.standard_normal((m, n, K)) for _ in range(3)]
+        wgt = np.full((m, n, K), 0.5)
+        u = 0.1 * rng.standard_normal((m, n))
+        v = 0.1 * rng.standard_normal((m, n))
+        inputs.append((J, wgt, u, v, (ax, ay), W / w, H / h))
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
+    def frame():
+        for J, wgt, u, v, alpha, hx, hy in inputs:
+            t = [torch.as_tensor(a, dtype=torch.float64, device=dev) for a in (*J, wgt, u, v)]
+            du, dv = mod.level_solver_rbgs_torch(*t, alpha, OPTIONS["iterations"], OPTIONS["update_lag"],
+                                                 OPTIONS["a_data"], OPTIONS["a_smooth"], hx, hy)
+            du.cpu().numpy()
+            dv.cpu().numpy()
 
-    T = args.frames
-    ref, frames = make_workload(T, dev, seed=1, frame0=50 + rank * T)
-    wt = weight_tensor(dev)
-    params = G.make_params(K=K, **OPTIONS)
-    plan = G.get_plan(params, H, W, K, T)
-    plan.set_reference(ref, wt)
-    out = torch.empty((T, H, W, 2), dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream()
+    frame()
+    torch.cuda.synchronize()
+    n_frames = max(1, args.reference_gpu_frames)
+    t0 = time.perf_counter()
+    for _ in range(n_frames):
+        frame()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / n_frames
+    return {"value": 1.0 / dt, "unit": "frames/s", "ms_per_frame": dt * 1e3, "frames": n_frames,
+            "what": "level_solver_rbgs_torch (pyflowreg's flowreg_torch backend, float64, unmodified) on every "
+                    "level of one 512x512x2 frame, with the backend's per-level host<->device copies; the "
+                    "backend's CPU pyramid, warp, tensor and median are not included (upper bound of its "
+                    "frame rate)"}
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
 
-    tuning = None
-    if not args.no_autotune:
-        # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
-        chosen = plan.autotune(frames, n_levels=4, reps=1)
-        tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
-                  {"kernel": {0: "diagonal_ring", 1: "rows_in_registers", 2: "rows_in_registers_chained"}[v], "G": g,
-                   "threads": t or plan.level_tuning()[i][3]}
-                  for i, (v, g, t, _) in chosen.items()}
-    # The batch's frame ranges go to the plan's lanes (independent plans, each on
-    # its own stream), and each lane runs the steps one after the other without
-    # waiting for the other lanes at step boundaries: one lane's last wave of a
-    # level overlaps another lane's work, also across steps.  One lane per
-    # plan when the batch is small (or per rank under torchrun).
+def fp64_peak(dev):
+    """Float64 throughput of this GPU: cuBLAS DGEMM (n = 4096), best of 3, in
+    TFLOP/s.  The float64 pipe is the roof of the float64 solver."""
+    import torch
+
+    n = 4096
+    a = torch.randn((n, n), dtype=torch.float64, device=dev)
+    b = torch.randn((n, n), dtype=torch.float64, device=dev)
+    torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
+
+
+def profiled_fp64_ops():
+    """Float64 flops (FMA = 2) per pixel update of the float64 SOR kernel, fold
+    included, from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "k_sor_chain64" and parts[1] == "fp64_ops_per_pixel_update":
+                return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+def time_lanes(plan, frames, out, steps, warmup, stream, barrier=lambda: None):
+    """Runs `steps` batched calls on the plan's lanes (each lane its frame range
+    on its own stream, steps back to back without a join at step boundaries);
+    returns the CUDA-event milliseconds of the timed steps."""
+    import torch
+
     lane_plans = list(getattr(plan, "plans", [plan]))
     lane_streams = list(getattr(plan, "streams", [stream]))
+    T = frames.shape[0]
     per_lane = -(-T // len(lane_plans))
     lanes = [(lane_plans[i], lane_streams[i], i * per_lane, min(T, (i + 1) * per_lane))
              for i in range(len(lane_plans)) if i * per_lane < T]
@@ -515,136 +589,140 @@ def run_gb300(args):
         for lp, ls, t0, t1 in lanes:
             stream.wait_stream(ls)
 
-    run_steps(max(args.warmup, 3))
+    run_steps(max(warmup, 3))
     torch.cuda.synchronize()
-
-    lib = _lib.load()
-    sampler = ClockSampler(local)
-    plan.set_profiling(True)
-    n0 = lib.frg_launch_count()
     barrier()
     torch.cuda.synchronize()
-    sampler.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    run_steps(args.steps)
+    run_steps(steps)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
+    return ev0.elapsed_time(ev1), len(lanes)
+
+
+def sor_profile(G, params, plan, ref, wt, frames, out, stream):
+    """CUDA-event time and model bytes of the SOR launches of one single-plan
+    call of the batch, with the GPU to itself (lanes overlap their launches)."""
+    import torch
+
+    T = frames.shape[0]
+    rplan = G.Plan(params, H, W, K, T)
+    rplan.set_reference(ref, wt)
+    for i in range(len(plan.level_tuning())):
+        g, t_, gmax, _ = plan.level_tuning()[i]
+        if rplan.fp64:
+            rplan.set_level_tuning(i, 0, t_)
+            continue
+        v, nv = plan.level_variant(i)
+        if nv > 0:
+            rplan.set_level_variant(i, v)
+        if gmax > 0:
+            rplan.set_level_tuning(i, g, t_)
+    rplan.displacement(frames, None, out)
+    torch.cuda.synchronize()
+    rplan.set_profiling(True)
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    rplan.displacement(frames, None, out)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    sor_n, sor_ms, sor_bytes = rplan.profile()
+    rplan.close()
+    return sor_n, sor_ms, sor_bytes, r0.elapsed_time(r1)
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    import pyflowreg_gb300 as G
+    from pyflowreg_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    T = args.frames
+    ref, frames = make_workload(T, dev, seed=1, frame0=50 + rank * T)
+    wt = weight_tensor(dev)
+    stream = torch.cuda.current_stream()
+    precision = args.precision
+    params = G.make_params(K=K, precision=precision, **OPTIONS)
+    plan = G.get_plan(params, H, W, K, T)
+    plan.set_reference(ref, wt)
+    fp64 = plan.fp64
+    out = torch.empty((T, H, W, 2), dtype=torch.float64 if fp64 else torch.float32, device=dev)
+
+    tuning = None
+    if not args.no_autotune:
+        # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
+        chosen = plan.autotune(frames, n_levels=4, reps=1)
+        if fp64:
+            tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
+                      {"kernel": "k_sor_chain64", "rows_per_cta": t or "by batch size"}
+                      for i, (v, g, t, _) in chosen.items()}
+        else:
+            tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
+                      {"kernel": {0: "diagonal_ring", 1: "rows_in_registers", 2: "rows_in_registers_chained"}[v],
+                       "G": g, "threads": t or plan.level_tuning()[i][3]}
+                      for i, (v, g, t, _) in chosen.items()}
+
+    # ---- value: the batch resident in HBM, the plan's lanes on their own streams
+    lib = _lib.load()
+    sampler = ClockSampler(local)
+    n0 = lib.frg_launch_count()
+    sampler.start()
+    ms, n_lanes = time_lanes(plan, frames, out, args.steps, args.warmup, stream, barrier)
     clocks = sampler.stop()
     launches = lib.frg_launch_count() - n0
-    sor_n, sor_ms, sor_bytes = plan.profile()
-    plan.set_profiling(False)
-    ms = ev0.elapsed_time(ev1)
     if world > 1:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * T * args.steps / (ms / 1e3)
+    out_kept = out.clone()
 
-    # The SOR kernel's own efficiency: lanes overlap their launches, so each
-    # launch's duration in the timed region includes the other lanes' work.
-    # One single-plan call of the same batch with the same tuning, right after
-    # the timed region, gives the per-launch figure with the GPU to itself.
-    lane_sor = (sor_n, sor_ms, sor_bytes)
-    if hasattr(plan, "plans"):
-        rplan = G.Plan(params, H, W, K, T)
-        rplan.set_reference(ref, wt)
-        for i in range(len(plan.level_tuning())):
-            v, nv = plan.level_variant(i)
-            if nv > 0:
-                rplan.set_level_variant(i, v)
-            g, t_, gmax, _ = plan.level_tuning()[i]
-            if gmax > 0:
-                rplan.set_level_tuning(i, g, t_)
-        rplan.displacement(frames, None, out)
-        torch.cuda.synchronize()
-        rplan.set_profiling(True)
-        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        r0.record(stream)
-        rplan.displacement(frames, None, out)
-        r1.record(stream)
-        torch.cuda.synchronize()
-        sor_n, sor_ms, sor_bytes = rplan.profile()
-        rcall_ms = r0.elapsed_time(r1)
-        rplan.close()
-    else:
-        rcall_ms = ms / args.steps
+    # ---- the SOR kernel on its own: one single-plan call of the same batch
+    sor_n, sor_ms, sor_bytes, rcall_ms = sor_profile(G, params, plan, ref, wt, frames, out, stream)
 
-    # e2e through the public API: every step uploads its batch from pinned host
-    # memory and reads its flows back into pinned host memory.  The batch moves
-    # in one chunk per lane of the plan (the frame ranges the lanes register
-    # independently): a lane starts as soon as its chunk is on the device and
-    # its flows go back as soon as it is done, so only the first chunk's upload
-    # and the last chunk's read-back are not hidden behind compute.  Uploads and
-    # read-backs run on two copy streams (two device slots, events between the
-    # streams); the timed region runs from before the first upload to after the
-    # last read-back.
-    host_in = frames.cpu().pin_memory()
-    host_out = [torch.empty((T, H, W, 2), dtype=torch.float32).pin_memory() for _ in range(2)]
-    dev_in = [torch.empty_like(frames) for _ in range(2)]
-    dev_out = [torch.empty((T, H, W, 2), dtype=torch.float32, device=dev) for _ in range(2)]
-    lane_plans = list(getattr(plan, "plans", [plan]))
-    lane_streams = list(getattr(plan, "streams", [torch.cuda.Stream(device=dev)]))
-    n_ch = len(lane_plans)
-    per_ch = -(-T // n_ch)
-    chunks = [(i * per_ch, min(T, (i + 1) * per_ch)) for i in range(n_ch) if i * per_ch < T]
-    up_s, down_s = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
-
-    def e2e_run(n_steps):
-        ev = lambda: [[torch.cuda.Event() for _ in chunks] for _ in range(2)]  # noqa: E731
-        ev_in, ev_comp, ev_out = ev(), ev(), ev()
-        e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e_start.record(up_s)
-        down_s.wait_event(e_start)
-
-        def upload(k):
-            sl = k & 1
-            with torch.cuda.stream(up_s):
-                for i, (t0, t1) in enumerate(chunks):
-                    if k >= 2:
-                        up_s.wait_event(ev_comp[sl][i])  # the lane of step k - 2 has consumed this slot
-                    dev_in[sl][t0:t1].copy_(host_in[t0:t1], non_blocking=True)
-                    ev_in[sl][i].record(up_s)
-
-        upload(0)
-        for k in range(n_steps):
-            sl = k & 1
-            if k + 1 < n_steps:
-                upload(k + 1)
-            for i, (t0, t1) in enumerate(chunks):
-                ls = lane_streams[i]
-                ls.wait_event(ev_in[sl][i])
-                if k >= 2:
-                    ls.wait_event(ev_out[sl][i])  # dev_out[sl] of this chunk read back
-                lane_plans[i].displacement(dev_in[sl][t0:t1], None, dev_out[sl][t0:t1], stream=ls)
-                ev_comp[sl][i].record(ls)
-                with torch.cuda.stream(down_s):
-                    down_s.wait_event(ev_comp[sl][i])
-                    host_out[sl][t0:t1].copy_(dev_out[sl][t0:t1], non_blocking=True)
-                    ev_out[sl][i].record(down_s)
-        up_s.wait_stream(down_s)
-        e_end.record(up_s)
-        torch.cuda.synchronize()
-        return e_start.elapsed_time(e_end)
-
-    e2e_run(2)
+    # ---- e2e: the reference-facing batch call with host arrays (pageable numpy in, numpy out);
+    # its host<->device copies (pinned staging, overlapped lane by lane) are inside the timed region
+    fx_np = ref.cpu().numpy()
+    mv_np = frames.cpu().numpy()
+    w_np = wt.cpu().numpy()
+    G.get_displacement_batch(fx_np, mv_np, weight=w_np, precision=precision, **OPTIONS)  # warm-up
     barrier()
-    e_ms = e2e_run(args.steps)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_out = G.get_displacement_batch(fx_np, mv_np, weight=w_np, precision=precision, **OPTIONS)
+    torch.cuda.synchronize()
+    e_s = time.perf_counter() - t0
     barrier()
     if world > 1:
-        t = torch.tensor([e_ms], device=dev)
+        t = torch.tensor([e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e_ms = float(t.item())
-    e2e_value = world * T * args.steps / (e_ms / 1e3)
+        e_s = float(t.item())
+    e2e_value = world * T * args.steps / e_s
+    e2e_equal = bool(np.array_equal(host_out, out_kept.cpu().numpy()))
+    del host_out
 
-    # plain form: one frame per call (the same kernels, batch of one)
+    # ---- plain form: one frame per call (the same kernels, batch of one)
     plain = None
     if args.plain_frames > 0:
         pplan = G.Plan(params, H, W, K, 1)
         pplan.set_reference(ref, wt)
-        pout = torch.empty((1, H, W, 2), dtype=torch.float32, device=dev)
+        pout = torch.empty((1, H, W, 2), dtype=out.dtype, device=dev)
         pplan.displacement(frames[:1], None, pout)
         torch.cuda.synchronize()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -655,18 +733,20 @@ def run_gb300(args):
         torch.cuda.synchronize()
         p_ms = p0.elapsed_time(p1)
         plain = {"value": args.plain_frames / (p_ms / 1e3), "unit": "frames/s", "frames": args.plain_frames,
-                 "ms_per_frame": p_ms / args.plain_frames}
+                 "ms_per_frame": p_ms / args.plain_frames, "precision": precision}
         pplan.close()
 
-    n_lanes = len(getattr(plan, "plans", [plan]))
+    # ---- roofline of the SOR kernel
     peak, peak_src = measured_peak()
     achieved = (sor_bytes / (sor_ms / 1e3) / 1e9) if sor_ms > 0 else None
     per_launch_bytes = sor_bytes / max(sor_n, 1)
-    ratio = profiled_traffic()
+    ratio = profiled_traffic(fp64)
+    bpp = 72 if fp64 else 36
     roofline = {
-        "kernel": "k_sor_chain (exact-order wavefront SOR, one thread per row, state in registers, fold in "
-                  "the loader, every pass of a level in one launch; k_sor_regs / k_sor_fused on levels it does "
-                  "not serve)",
+        "kernel": ("k_sor_chain64 (float64 exact-order chained wavefront SOR, one thread per row, state in "
+                   "registers, coefficients folded once per pass, row strips of 64-256 rows as clusters)" if fp64
+                   else "k_sor_chain (float32 exact-order chained wavefront SOR, one thread per row, state in "
+                   "registers, fold in the loader)"),
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
@@ -677,22 +757,38 @@ def run_gb300(args):
         "algorithmic_bytes_per_launch": per_launch_bytes,
         "launches": sor_n,
         "share_of_step": (sor_ms / rcall_ms) if rcall_ms > 0 else None,
-        "measured_on": ("one single-plan call of the same batch and tuning, right after the timed region"
-                        if n_lanes > 1 else "the timed region"),
-        "timed_region_lanes": ({"launches": lane_sor[0], "achieved_per_launch":
-                                (lane_sor[2] / (lane_sor[1] / 1e3) / 1e9) if lane_sor[1] > 0 else None,
-                                "note": "each launch's own CUDA-event duration while the lanes overlap"}
-                               if n_lanes > 1 else None),
-        "note": "achieved = 36 B per interior pixel per pipelined SOR iteration (streaming model) / "
-                "CUDA-event time of the SOR launches; the kernel keeps G iterations on chip, so "
-                "frac can exceed 1; traffic = measured DRAM/model ratio (profiles/dram_traffic.txt) x model "
-                "bytes per launch",
+        "measured_on": "one single-plan call of the same batch right after the timed region (CUDA events on the "
+                       "launching stream around each SOR launch)",
+        "note": f"achieved = {bpp} B per interior pixel per SOR iteration (streaming model: five coefficients "
+                "and du, dv read, du, dv written) / CUDA-event time of the SOR launches; traffic = measured "
+                "DRAM/model ratio of the committed ncu summary x model bytes per launch",
     }
+    fp64_pipe = None
+    if fp64:
+        ops = profiled_fp64_ops()
+        peak64 = fp64_peak(dev)
+        its = sor_bytes / bpp  # pixel updates in the profiled call
+        ach = (ops * its / (sor_ms / 1e3) / 1e12) if (ops and sor_ms > 0) else None
+        fp64_pipe = {"bound": "fp64 pipe", "achieved_tflops": ach, "peak_tflops": peak64,
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run", "frac": (ach / peak64) if ach else None,
+                     "fp64_flops_per_pixel_update": ops,
+                     "note": "the float64 SOR is bound by the float64 pipe (about 1/64 of the float32 rate on "
+                             "GB300), not by HBM: achieved = float64 flops per pixel update (ncu count of the "
+                             "kernel's DFMA x 2 + DADD + DMUL, fold included, profiles/dram_traffic.txt) x pixel "
+                             "updates / SOR time, against cuBLAS DGEMM on the same GPU"}
 
-    cpu = None
-    parity = None
+    cpu = parity = None
+    reference_gpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, parity = cpu_baseline(args, ref, frames, out)
+        cpu, parity = cpu_baseline(args, ref, frames, out_kept, precision)
+    if rank == 0 and world == 1 and args.reference_gpu_frames > 0:
+        lv = plan.plans[0].levels() if hasattr(plan, "plans") else plan.levels()
+        reference_gpu = run_reference_gpu(args, dev, lv)
+    fp32 = None
+    if rank == 0 and precision == "fp64" and args.fp32_secondary:
+        fp32 = run_fp32_secondary(args, G, ref, wt, frames, stream, parity)
+    if parity is not None:
+        parity.pop("_oracle_flows", None)
     backward = run_diff(args, dev) if (rank == 0 and args.diff_frames > 0) else None
     uneven = run_uneven(args, dev) if (rank == 0 and args.uneven_frames > 0) else None
     stream_2048, compensate_2048 = run_stream(args, dev) if (rank == 0 and args.stream_frames > 0) else (None, None)
@@ -709,28 +805,33 @@ def run_gb300(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32",
+            "dtype": "f64" if fp64 else "f32",
             "data": "synthetic (seeded photon-count blob video, preprocessed on device)",
             "config": {"workload": "512x512x2 video, batched get_displacement against the mean of frames 0-49",
-                       "frames_per_step": T * world, "frames_per_rank": T, "height": H, "width": W,
-                       "channels": K, "options": {**OPTIONS, "alpha": list(OPTIONS["alpha"]),
-                                                  "weight": list(WEIGHT)},
+                       "precision": precision, "frames_per_step": T * world, "frames_per_rank": T, "height": H,
+                       "width": W, "channels": K, "options": {**OPTIONS, "alpha": list(OPTIONS["alpha"]),
+                                                              "weight": list(WEIGHT)},
                        "l2": "inputs larger than L2 (%.0f MB per step)" % (T * H * W * K * 4 / 1e6),
                        "parallelism": f"frames sharded over {world} GPU(s)",
                        "sor_launch_tuning": tuning,
                        "lanes": f"{n_lanes} plans over contiguous parts of the batch, each on its own stream, "
                                 "running the steps without a join between lanes at step boundaries"
                                 if n_lanes > 1 else "one plan"},
-            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": T * H * W * K * 4,
-                    "d2h_bytes_per_step": T * H * W * 2 * 4,
-                    "copies": "pinned host buffers; each step moves in one chunk per lane (uploads and read-backs "
-                              "on two copy streams overlapping compute); timed from the first upload to the last "
-                              "read-back",
-                    "api": "Plan.displacement of each lane of the cached plan (the get_displacement_device plan)"},
+            "e2e": {"value": e2e_value, "unit": "frames/s",
+                    "h2d_bytes_per_step": T * H * W * K * 4 + 2 * H * W * K * 4,
+                    "d2h_bytes_per_step": T * H * W * 2 * (8 if fp64 else 4),
+                    "api": "pyflowreg_gb300.get_displacement_batch(fixed, moving, weight=..., **options): numpy "
+                           "arrays in, numpy flows out (the reference-facing batch call behind the gb300 executor)",
+                    "copies": "pageable numpy -> pinned staging -> device per lane part, read-back into pinned "
+                              "memory and numpy; copies of one part overlap the other parts' compute",
+                    "timing": "wall clock around the calls after a warm-up call",
+                    "flows_equal_device_resident_run": e2e_equal},
             "gpu_launches": int(launches),
             "roofline": roofline,
+            "fp64_pipe": fp64_pipe,
             "plain": plain,
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
+            "fp32_fast_path": fp32,
             "bwd_fwd_ratio": backward["ratio"] if backward else None,
             "backward": backward,
             "uneven_batch": uneven,
@@ -738,6 +839,7 @@ def run_gb300(args):
             "compensate_2048": compensate_2048,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "reference_gpu": reference_gpu,
             "parity": parity,
         }
         print(json.dumps(line), flush=True)
@@ -745,9 +847,38 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(args, ref, frames, gpu_out):
-    """Oracle on the host cores on a bounded sample of the same frames; also
-    the flow difference GPU vs oracle on that sample."""
+def run_fp32_secondary(args, G, ref, wt, frames, stream, parity):
+    """The float32 path on the same batch (secondary: outside the parity
+    tolerance), with its own launch-shape tuning."""
+    import torch
+
+    T = frames.shape[0]
+    params = G.make_params(K=K, precision="fp32", **OPTIONS)
+    plan = G.get_plan(params, H, W, K, T)
+    plan.set_reference(ref, wt)
+    if not args.no_autotune:
+        plan.autotune(frames, n_levels=4, reps=1)
+    out = torch.empty((T, H, W, 2), dtype=torch.float32, device=frames.device)
+    ms, _ = time_lanes(plan, frames, out, args.steps, args.warmup, stream)
+    res = {"value": T * args.steps / (ms / 1e3), "unit": "frames/s", "dtype": "f32",
+           "note": "float32 arithmetic: the algorithm amplifies its rounding to flows up to ~0.7 px from the "
+                   "reference's (parity block)"}
+    if parity is not None and "_oracle_flows" in parity:
+        n = parity["frames"]
+        res["parity"] = flow_diff(out[:n].cpu().numpy().astype(np.float64), parity["_oracle_flows"])
+    return res
+
+
+def flow_diff(a, b):
+    d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
+    return {"max_abs_px": float(np.abs(d).max()), "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean())}
+
+
+def cpu_baseline(args, ref, frames, gpu_out, precision):
+    """The oracle, built -O3 for the host's CPU with the checker's float
+    semantics, timed on the host cores on a bounded sample of the same frames
+    (one frame per thread); the checker's flows on that sample give the
+    parity of the timed GPU flows."""
     from oracle import oracle as O
 
     cores = os.cpu_count() or 1
@@ -759,26 +890,28 @@ def cpu_baseline(args, ref, frames, gpu_out):
     for k in range(K):
         wt[:, :, k] = WEIGHT[k] / sum(WEIGHT)
     t0 = time.perf_counter()
-    flows = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
+    flows = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, variant="o3", **OPTIONS)
     dt = time.perf_counter() - t0
-
-    def diff(a):
-        d = a - flows
-        return {"max_abs_px": float(np.abs(d).max()), "mean_epe_px": float(np.sqrt((d ** 2).sum(-1)).mean())}
-
-    import pyflowreg_gb300 as G
-
-    f64 = G.get_displacement_device(ref, frames[:n].contiguous(), None, weight_tensor(ref.device),
-                                    precision="fp64", **OPTIONS)
-    parity = {"frames": n,
-              "fp64_reference_order": diff(f64.cpu().numpy()),
-              "fp32_fast_path": diff(gpu_out[:n].cpu().numpy().astype(np.float64)),
+    check = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
+    assert np.array_equal(flows, check), "the timed oracle build must return the checker's flows"
+    fast = None
+    if args.cpu_fastmath:
+        t0 = time.perf_counter()
+        fm = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, variant="fastmath", **OPTIONS)
+        fdt = time.perf_counter() - t0
+        fast = {"value": n / fdt, "unit": "frames/s", "flags": O.build_flags().get("fastmath"),
+                "vs_checker": flow_diff(fm, flows),
+                "note": "the analogue of numba's fastmath=True: faster, its flows move within the reference's "
+                        "own rounding envelope"}
+    parity = {"frames": n, "precision": precision, "timed_path": flow_diff(gpu_out[:n].cpu().numpy(), flows),
               "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4},
-              "note": "the fp64 reference-order mode is the parity mode; the fp32 deviation is bounded by "
-                      "the reference's own rounding amplification (the oracle moves by ~0.1 px under a 1e-7 "
-                      "relative input perturbation)"}
+              "oracle": "fp64 lexicographic C restatement of pyflowreg's numba path, pinned to the reference's own "
+                        "source by the golden fixtures",
+              "_oracle_flows": flows}
     cpu = {"value": n / dt, "unit": "frames/s", "cores": cores, "kind": "port",
-           "sample": f"{n} frames of the same batch, one frame per thread (OpenMP), fp64 lexicographic oracle"}
+           "flags": O.build_flags().get("o3"),
+           "sample": f"{n} frames of the same batch, one frame per thread (OpenMP), fp64 lexicographic oracle",
+           "fastmath_build": fast}
     return cpu, parity
 
 
@@ -803,10 +936,10 @@ def run_reference(args):
     for k in range(K):
         wt[:, :, k] = WEIGHT[k] / sum(WEIGHT)
     for _ in range(args.warmup):
-        O.get_displacement_batch(fx, mv[:1], n_threads=1, weight=wt, **OPTIONS)
+        O.get_displacement_batch(fx, mv[:1], n_threads=1, weight=wt, variant="o3", **OPTIONS)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, **OPTIONS)
+        O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, variant="o3", **OPTIONS)
     dt = time.perf_counter() - t0
     value = n * args.steps / dt
     del torch
@@ -827,6 +960,7 @@ def run_reference(args):
         "config": {"workload": "512x512x2 video, batched get_displacement against the mean of frames 0-49",
                    "frames_per_step": n, "height": H, "width": W, "channels": K},
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "flags": O.build_flags().get("o3"),
                          "sample": f"{n} frames per step, one frame per thread"},
         "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "pyflowreg's numba/OpenCV path cannot be installed here; the fp64 C restatement of it "

@@ -4,9 +4,9 @@
 #                        fast-math and no FMA contraction, so float rounding
 #                        follows the C source operation by operation and the
 #                        same source gives the same bits on x86_64 and aarch64;
-#  liboracle_native.so   the timed CPU baseline: the same source and the same
+#  liboracle_o3.so       the timed CPU baseline: the same source and the same
 #                        float semantics (no contraction, no fast-math), built
-#                        with -O3 for the host's own CPU (-march=native), so it
+#                        with -O3 (portable: no -march flags either), so it
 #                        returns the checker's bits, only faster;
 #  liboracle_fastmath.so the same with -ffast-math, the analogue of the
 #                        reference's numba @njit(fastmath=True): timed only,
@@ -20,12 +20,10 @@ src="$here/flowreg_oracle.c"
 base="-std=c11 -fPIC -shared -fopenmp"
 $cc -O2 $base -fno-fast-math -ffp-contract=off -o "$here/_build/liboracle.so.tmp" "$src" -lm
 mv -f "$here/_build/liboracle.so.tmp" "$here/_build/liboracle.so"
-native="-march=native"
-if ! echo 'int main(void){return 0;}' | $cc $native -x c - -o /dev/null 2>/dev/null; then native=""; fi
-nflags="-O3 $native -fno-fast-math -ffp-contract=off"
-fflags="-O3 $native -ffast-math"
-$cc $nflags $base -o "$here/_build/liboracle_native.so.tmp" "$src" -lm
-mv -f "$here/_build/liboracle_native.so.tmp" "$here/_build/liboracle_native.so"
+nflags="-O3 -fno-fast-math -ffp-contract=off"
+fflags="-O3 -ffast-math"
+$cc $nflags $base -o "$here/_build/liboracle_o3.so.tmp" "$src" -lm
+mv -f "$here/_build/liboracle_o3.so.tmp" "$here/_build/liboracle_o3.so"
 $cc $fflags $base -o "$here/_build/liboracle_fastmath.so.tmp" "$src" -lm
 mv -f "$here/_build/liboracle_fastmath.so.tmp" "$here/_build/liboracle_fastmath.so"
-printf 'native: %s %s\nfastmath: %s %s\n' "$cc" "$nflags" "$cc" "$fflags" > "$here/_build/flags.txt"
+printf 'o3: %s %s\nfastmath: %s %s\n' "$cc" "$nflags" "$cc" "$fflags" > "$here/_build/flags.txt"

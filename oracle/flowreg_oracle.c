@@ -575,6 +575,88 @@ int orc_compute_flow(const double *J11, const double *J22, const double *J33, co
     return ORC_OK;
 }
 
+/* compute_flow (core/level_solver.py:158-369) for a_smooth = 1 in lexicographic
+ * order, with every solver value held and every operation rounded in float32
+ * (numpy float32 semantics: no fused multiply-add, powf, IEEE division): the
+ * reference algorithm in single precision.  Its distance from the float64
+ * solver is the rounding envelope of a float32 implementation.  Inputs and the
+ * returned du, dv are float64 arrays; the values are rounded to float32 on
+ * entry. */
+int orc_compute_flow_f32(const double *J11d, const double *J22d, const double *J33d, const double *J12d,
+                         const double *J13d, const double *J23d, const double *wgtd, const double *ud,
+                         const double *vd, int m, int n, int K, double alpha_x, double alpha_y,
+                         int iterations, int update_lag, const double *a_data, double hx, double hy,
+                         double omega_d, double *du_out, double *dv_out)
+{
+    size_t N = (size_t)m * n, NK = N * K;
+    float *buf = malloc((7 * NK + 4 * N) * sizeof(float));
+    if (!buf) return ORC_ENOMEM;
+    float *J11 = buf, *J22 = J11 + NK, *J33 = J22 + NK, *J12 = J33 + NK, *J13 = J12 + NK, *J23 = J13 + NK;
+    float *wgt = J23 + NK, *u = wgt + NK, *v = u + N, *du = v + N, *dv = du + N;
+    float *psi = malloc(NK * sizeof(float));
+    if (!psi) { free(buf); return ORC_ENOMEM; }
+    for (size_t i = 0; i < NK; ++i) {
+        J11[i] = (float)J11d[i]; J22[i] = (float)J22d[i]; J33[i] = (float)J33d[i];
+        J12[i] = (float)J12d[i]; J13[i] = (float)J13d[i]; J23[i] = (float)J23d[i];
+        wgt[i] = (float)wgtd[i]; psi[i] = 1.0f;
+    }
+    for (size_t i = 0; i < N; ++i) { u[i] = (float)ud[i]; v[i] = (float)vd[i]; du[i] = 0.0f; dv[i] = 0.0f; }
+    const float ax = (float)(alpha_x / (hx * hx)), ay = (float)(alpha_y / (hy * hy));
+    const float omega = (float)omega_d;
+    for (int it = 0; it < iterations; ++it) {
+        if ((it + 1) % update_lag == 0) {
+            for (int k = 0; k < K; ++k) {
+                const float ak = (float)a_data[k];
+                for (size_t c = 0; c < N; ++c) {
+                    size_t ck = c * K + k;
+                    float a = du[c], b = dv[c];
+                    float val = J11[ck] * a * a + J22[ck] * b * b + J23[ck] * b
+                              + 2.0f * J12[ck] * a * b + 2.0f * J13[ck] * a + J23[ck] * b + J33[ck];
+                    if (val < 0.0f) val = 0.0f;
+                    psi[ck] = ak * powf(val + 0.00001f, ak - 1.0f);
+                }
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            du[i] = du[n + i]; du[(size_t)(m - 1) * n + i] = du[(size_t)(m - 2) * n + i];
+            dv[i] = dv[n + i]; dv[(size_t)(m - 1) * n + i] = dv[(size_t)(m - 2) * n + i];
+        }
+        for (int j = 0; j < m; ++j) {
+            du[(size_t)j * n] = du[(size_t)j * n + 1]; du[(size_t)j * n + n - 1] = du[(size_t)j * n + n - 2];
+            dv[(size_t)j * n] = dv[(size_t)j * n + 1]; dv[(size_t)j * n + n - 1] = dv[(size_t)j * n + n - 2];
+        }
+        for (int i = 1; i < n - 1; ++i)
+            for (int j = 1; j < m - 1; ++j) {
+                size_t c = (size_t)j * n + i;
+                size_t L = c - 1, R = c + 1, D = c + n, U = c - n;
+                float den_u = 0, den_v = 0, num_u = 0, num_v = 0;
+                num_u += ax * (u[L] + du[L] - u[c]); num_v += ax * (v[L] + dv[L] - v[c]); den_u += ax; den_v += ax;
+                num_u += ax * (u[R] + du[R] - u[c]); num_v += ax * (v[R] + dv[R] - v[c]); den_u += ax; den_v += ax;
+                num_u += ay * (u[D] + du[D] - u[c]); num_v += ay * (v[D] + dv[D] - v[c]); den_u += ay; den_v += ay;
+                num_u += ay * (u[U] + du[U] - u[c]); num_v += ay * (v[U] + dv[U] - v[c]); den_u += ay; den_v += ay;
+                for (int k = 0; k < K; ++k) {
+                    size_t ck = c * K + k;
+                    float wp = wgt[ck] * psi[ck];
+                    num_u -= wp * (J13[ck] + J12[ck] * dv[c]);
+                    den_u += wp * J11[ck];
+                    den_v += wp * J22[ck];
+                }
+                float du_kp1 = den_u != 0.0f ? num_u / den_u : 0.0f;
+                du[c] = (1.0f - omega) * du[c] + omega * du_kp1;
+                float num_v2 = num_v;
+                for (int k = 0; k < K; ++k) {
+                    size_t ck = c * K + k;
+                    num_v2 -= wgt[ck] * psi[ck] * (J23[ck] + J12[ck] * du[c]);
+                }
+                float dv_kp1 = den_v != 0.0f ? num_v2 / den_v : 0.0f;
+                dv[c] = (1.0f - omega) * dv[c] + omega * dv_kp1;
+            }
+    }
+    for (size_t i = 0; i < N; ++i) { du_out[i] = du[i]; dv_out[i] = dv[i]; }
+    free(psi); free(buf);
+    return ORC_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* 5x5 median, scipy.ndimage "mirror" boundary: core/optical_flow.py:607-609 */
 /* ------------------------------------------------------------------------ */
@@ -634,6 +716,8 @@ typedef struct {
     int acc_f32;                 /* resize accumulator: 0 float64 (numba), 1 float32 (plain Python) */
     double gnc_beta;             /* < 0: plain stage; else one GNC stage with this beta */
     int warping_steps;           /* warp / relinearise steps per level of a GNC stage */
+    int solver_f32;              /* 1: the level solver in float32 (orc_compute_flow_f32; a_smooth = 1,
+                                    lexicographic order) */
 } orc_params;
 
 /* resize an (H, W, K) double array, channel by channel, to (h, w, K) */
@@ -761,10 +845,17 @@ int orc_displacement(int H, int W, int K, const double *fixed, const double *mov
         }
         if (rc == ORC_OK) {
             /* level solve (lines 584-606): hx = h_col, hy = h_row */
-            rc = orc_compute_flow(J, J + mn * K, J + 2 * mn * K, J + 3 * mn * K, J + 4 * mn * K,
-                                  J + 5 * mn * K, wpad, un, vn, m, n, K, L->alpha_x, L->alpha_y,
-                                  prm->iterations, prm->update_lag, a_data, prm->a_smooth,
-                                  h_col, h_row, prm->order, prm->omega, -1.0, du, dv);
+            if (prm->solver_f32)
+                rc = (prm->a_smooth != 1.0 || prm->order != 0) ? ORC_EINVAL
+                   : orc_compute_flow_f32(J, J + mn * K, J + 2 * mn * K, J + 3 * mn * K, J + 4 * mn * K,
+                                          J + 5 * mn * K, wpad, un, vn, m, n, K, L->alpha_x, L->alpha_y,
+                                          prm->iterations, prm->update_lag, a_data, h_col, h_row,
+                                          prm->omega, du, dv);
+            else
+                rc = orc_compute_flow(J, J + mn * K, J + 2 * mn * K, J + 3 * mn * K, J + 4 * mn * K,
+                                      J + 5 * mn * K, wpad, un, vn, m, n, K, L->alpha_x, L->alpha_y,
+                                      prm->iterations, prm->update_lag, a_data, prm->a_smooth,
+                                      h_col, h_row, prm->order, prm->omega, -1.0, du, dv);
         }
         if (rc == ORC_OK) {
             /* median on the interiors (lines 607-609), then accumulate (610-611) */

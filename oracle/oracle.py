@@ -37,7 +37,7 @@ ORDER_RED_BLACK = 1
 
 
 _VARIANTS = {"portable": _LIB_PATH,
-             "native": os.path.join(_HERE, "_build", "liboracle_native.so"),
+             "o3": os.path.join(_HERE, "_build", "liboracle_o3.so"),
              "fastmath": os.path.join(_HERE, "_build", "liboracle_fastmath.so")}
 _variant_libs = {}
 
@@ -54,7 +54,7 @@ def build(force: bool = False) -> str:
 
 
 def build_flags() -> dict:
-    """Compiler and flags of the timed builds ("native", "fastmath")."""
+    """Compiler and flags of the timed builds ("o3", "fastmath")."""
     build()
     out = {}
     with open(os.path.join(_HERE, "_build", "flags.txt")) as f:
@@ -85,12 +85,12 @@ class _Params(ctypes.Structure):
         ("a_smooth", ctypes.c_double), ("gray", ctypes.c_int),
         ("order", ctypes.c_int), ("omega", ctypes.c_double),
         ("acc_f32", ctypes.c_int), ("gnc_beta", ctypes.c_double),
-        ("warping_steps", ctypes.c_int),
+        ("warping_steps", ctypes.c_int), ("solver_f32", ctypes.c_int),
     ]
 
 
 def lib(variant: str = "portable"):
-    """The checker ("portable") or one of the timed builds ("native",
+    """The checker ("portable") or one of the timed builds ("o3",
     "fastmath"), see build_oracle.sh."""
     global _lib
     if variant != "portable":
@@ -121,6 +121,7 @@ def _declare(lib_):
     lib_.orc_motion_tensor.argtypes = [P, P, I, I, D, D, I, I, P, P, P, P, P, P]
     lib_.orc_compute_flow.argtypes = [P, P, P, P, P, P, P, P, P, I, I, I, D, D, I, I, P, D,
                                       D, D, I, D, D, P, P]
+    lib_.orc_compute_flow_f32.argtypes = [P, P, P, P, P, P, P, P, P, I, I, I, D, D, I, I, P, D, D, D, P, P]
     lib_.orc_median5_plane.argtypes = [P, I, I, P]
     lib_.orc_median5_plane.restype = None
     lib_.orc_cubic_table.argtypes = [P]
@@ -340,6 +341,27 @@ def compute_flow(J11, J22, J33, J12, J13, J23, weight, u, v, alpha_x, alpha_y, i
     return np.stack([du, dv], axis=2)
 
 
+def compute_flow_f32(J11, J22, J33, J12, J13, J23, weight, u, v, alpha_x, alpha_y, iterations,
+                     update_lag, a_data, hx, hy, omega=1.95):
+    """compute_flow (core/level_solver.py:158-369, a_smooth = 1, lexicographic)
+    in float32 arithmetic; returns (m, n, 2) float64 holding float32 values."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (J11, J22, J33, J12, J13, J23, weight)]
+    if arrs[0].ndim == 2:
+        arrs = [a[:, :, None] for a in arrs]
+    m, n, K = arrs[0].shape
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    ad = np.ascontiguousarray(np.broadcast_to(np.asarray(a_data, dtype=np.float64), (K,)))
+    du = np.empty((m, n), np.float64)
+    dv = np.empty((m, n), np.float64)
+    rc = lib().orc_compute_flow_f32(*[_p(a) for a in arrs], _p(u), _p(v), m, n, K, float(alpha_x),
+                                    float(alpha_y), int(iterations), int(update_lag), _p(ad), float(hx),
+                                    float(hy), float(omega), _p(du), _p(dv))
+    if rc:
+        raise MemoryError("oracle level solver")
+    return np.stack([du, dv], axis=2)
+
+
 def median5(a: np.ndarray) -> np.ndarray:
     """scipy.ndimage.median_filter(a, size=(5, 5), mode='mirror')."""
     a = np.ascontiguousarray(a, dtype=np.float64)
@@ -504,10 +526,12 @@ def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, m
 def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), update_lag=5,
                            iterations=50, min_level=0, levels=50, eta=0.8, a_smooth=1.0,
                            a_data=0.45, const_assumption="gc", uv=None, weight=None,
-                           order=ORDER_LEXICOGRAPHIC, omega=1.95, variant="portable"):
+                           order=ORDER_LEXICOGRAPHIC, omega=1.95, variant="portable", solver_f32=False):
     """Many moving frames (T, H, W[, K]) against one fixed frame, OpenMP over
-    frames.  variant: "portable" (the checker), or a timed build ("native",
-    "fastmath"; see build_oracle.sh)."""
+    frames.  variant: "portable" (the checker), or a timed build ("o3",
+    "fastmath"; see build_oracle.sh).  solver_f32: every level solve in
+    float32 arithmetic (the reference algorithm in single precision, for the
+    rounding envelope of a float32 implementation; a_smooth = 1 only)."""
     moving_frames = np.asarray(moving_frames)
     fixed3, m0, weight, a_data_arr = normalize_inputs(fixed, moving_frames[0], weight, a_data)
     m, n, K = fixed3.shape
@@ -515,7 +539,7 @@ def get_displacement_batch(fixed, moving_frames, n_threads=None, alpha=(2, 2), u
     mov = np.ascontiguousarray(moving_frames.astype(np.float64).reshape(T, m, n, K))
     plan = _Plan(m, n, _alpha_pair(alpha), levels, eta, min_level)
     prm = _Params(int(iterations), int(update_lag), float(a_smooth), _const_mode(const_assumption),
-                  int(order), float(omega), 0)
+                  int(order), float(omega), 0, -1.0, 0, 1 if solver_f32 else 0)
     uvd = None if uv is None else np.ascontiguousarray(np.asarray(uv, dtype=np.float64)[:, :, :2])
     oh, ow = plan.out_hw
     out = np.empty((T, oh, ow, 2), np.float64)

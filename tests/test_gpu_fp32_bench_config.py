@@ -3,10 +3,10 @@ photon-count video, pyflowreg's default options), on two frame pairs whose
 true displacement is known (the noise-free unwarped frame against the Poisson
 frame warped by the known field):
 
-* the float32 flow stays within twice the oracle's own movement under a
-  1e-7 relative change of the moving frame (about one float32 ulp): the
-  algorithm amplifies rounding at that level to ~0.1 px, which bounds how
-  close any float32 implementation can come;
+* the float32 flow stays within twice the distance between the oracle's
+  float32 and float64 level solvers (the reference algorithm computed in
+  single precision: the algorithm amplifies float32 rounding to ~0.1 px,
+  which bounds how close any float32 implementation can come);
 * its end-point error against the true displacement equals the oracle's
   within 5 %: float32 costs no accuracy against the truth;
 * the float64 path meets the parity bar on the same pairs.
@@ -45,17 +45,16 @@ def test_fp32_at_bench_config_within_reference_envelope(oracle):
     fixed, moving, truth = _pairs([50, 51])
     wt = np.full((512, 512, 2), 0.5)
     wt_t = torch.full((512, 512, 2), 0.5, device="cuda")
-    rng = np.random.default_rng(3)
     for f, m, tr in zip(fixed, moving, truth):
         fx = f.cpu().numpy().astype(np.float64)
         mv = m.cpu().numpy().astype(np.float64)
-        mv_p = (mv * (1 + 1e-7 * rng.standard_normal(mv.shape))).astype(np.float32).astype(np.float64)
-        base, pert = oracle.get_displacement_batch(fx, np.stack([mv, mv_p]), n_threads=2, weight=wt, **OPTS)
-        env_max, env_epe = _diff(pert, base)
+        base = oracle.get_displacement_batch(fx, mv[None], n_threads=1, weight=wt, **OPTS)[0]
+        single = oracle.get_displacement_batch(fx, mv[None], n_threads=1, weight=wt, solver_f32=True, **OPTS)[0]
+        env_max, env_epe = _diff(single, base)
         got32 = G.get_displacement_device(f, m[None], None, wt_t, precision="fp32", **OPTS)[0].cpu().numpy()
         got64 = G.get_displacement_device(f, m[None], None, wt_t, **OPTS)[0].cpu().numpy()
         mx, ep = _diff(got32, base)
-        assert mx <= 2 * env_max + 1e-3 and ep <= 2 * env_epe + 1e-4, (mx, ep, env_max, env_epe)
+        assert mx <= 2 * env_max and ep <= 2 * env_epe, (mx, ep, env_max, env_epe)
         e_or = _diff(base, tr)[1]
         e_32 = _diff(got32, tr)[1]
         assert abs(e_32 - e_or) <= 0.05 * e_or, (e_32, e_or)

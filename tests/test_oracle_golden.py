@@ -114,8 +114,8 @@ def test_schedule_matches_reference_level_counts(oracle):
     assert len(oracle.level_schedule(1024, 1024, 100, 0.8, 0)[0]) == 22
 
 
-def test_native_timed_build_returns_the_checkers_bits(oracle):
-    """The CPU baseline is timed on the -O3 -march=native build; it has the
+def test_o3_timed_build_returns_the_checkers_bits(oracle):
+    """The CPU baseline is timed on the -O3 build; it has the
     checker's float semantics (no contraction, no fast-math), so its flows are
     bit-identical to the portable build's."""
     from pyflowreg_gb300.synthetic import pair_256
@@ -124,7 +124,86 @@ def test_native_timed_build_returns_the_checkers_bits(oracle):
     kw = dict(alpha=(1.5, 1.5), iterations=12, update_lag=5, weight=None)
     mv = np.stack([moving, moving[::-1]]).astype(np.float64)
     a = oracle.get_displacement_batch(fixed, mv, n_threads=2, **kw)
-    b = oracle.get_displacement_batch(fixed, mv, n_threads=2, variant="native", **kw)
+    b = oracle.get_displacement_batch(fixed, mv, n_threads=2, variant="o3", **kw)
     np.testing.assert_array_equal(a, b)
     flags = oracle.build_flags()
-    assert "-O3" in flags["native"] and "-ffp-contract=off" in flags["native"]
+    assert "-O3" in flags["o3"] and "-ffp-contract=off" in flags["o3"]
+
+
+def _compute_flow_numpy_f32(J, wgt, u, v, ax, ay, iterations, update_lag, a_data, omega):
+    """compute_flow (core/level_solver.py:158-369, a_smooth = 1) as the
+    reference writes it, loop by loop, on numpy float32 scalars, with the C
+    library's powf for the power (numpy's own float32 power may take a SIMD
+    routine with other last-bit rounding)."""
+    import ctypes
+    import ctypes.util
+
+    libm = ctypes.CDLL(ctypes.util.find_library("m"))
+    libm.powf.argtypes = [ctypes.c_float, ctypes.c_float]
+    libm.powf.restype = ctypes.c_float
+    f = np.float32
+    J11, J22, J33, J12, J13, J23 = [x.astype(f) for x in J]
+    wgt, u, v = wgt.astype(f), u.astype(f), v.astype(f)
+    m, n, K = J11.shape
+    du = np.zeros((m, n), f)
+    dv = np.zeros((m, n), f)
+    psi = np.ones((m, n, K), f)
+    ax, ay, omega = f(ax), f(ay), f(omega)
+    for it in range(iterations):
+        if (it + 1) % update_lag == 0:
+            for k in range(K):
+                ak = f(a_data)
+                for i in range(m):
+                    for j in range(n):
+                        a, b = du[i, j], dv[i, j]
+                        val = (J11[i, j, k] * a * a + J22[i, j, k] * b * b + J23[i, j, k] * b
+                               + f(2) * J12[i, j, k] * a * b + f(2) * J13[i, j, k] * a + J23[i, j, k] * b
+                               + J33[i, j, k])
+                        val = max(val, f(0))
+                        psi[i, j, k] = ak * f(libm.powf(val + f(0.00001), ak - f(1)))
+        for x in (du, dv):
+            x[0, :] = x[1, :]
+            x[-1, :] = x[-2, :]
+            x[:, 0] = x[:, 1]
+            x[:, -1] = x[:, -2]
+        for j in range(1, n - 1):
+            for i in range(1, m - 1):
+                num_u = num_v = den_u = den_v = f(0)
+                for (ii, jj, t) in ((i, j - 1, ax), (i, j + 1, ax), (i + 1, j, ay), (i - 1, j, ay)):
+                    num_u += t * (u[ii, jj] + du[ii, jj] - u[i, j])
+                    num_v += t * (v[ii, jj] + dv[ii, jj] - v[i, j])
+                    den_u += t
+                    den_v += t
+                for k in range(K):
+                    wp = wgt[i, j, k] * psi[i, j, k]
+                    num_u -= wp * (J13[i, j, k] + J12[i, j, k] * dv[i, j])
+                    den_u += wp * J11[i, j, k]
+                    den_v += wp * J22[i, j, k]
+                du_kp1 = num_u / den_u if den_u != 0 else f(0)
+                du[i, j] = (f(1) - omega) * du[i, j] + omega * du_kp1
+                num_v2 = num_v
+                for k in range(K):
+                    num_v2 -= wgt[i, j, k] * psi[i, j, k] * (J23[i, j, k] + J12[i, j, k] * du[i, j])
+                dv_kp1 = num_v2 / den_v if den_v != 0 else f(0)
+                dv[i, j] = (f(1) - omega) * dv[i, j] + omega * dv_kp1
+    return np.stack([du, dv], axis=2)
+
+
+def test_float32_solver_is_the_reference_loop_in_numpy_float32(oracle):
+    """The float32 level solver (the rounding envelope of the float32 path)
+    equals the reference's loops evaluated on numpy float32 scalars, bit for
+    bit, and stays near the float64 solver."""
+    rng = np.random.default_rng(11)
+    m, n, K = 9, 8, 2
+    J = [np.abs(rng.standard_normal((m, n, K))) for _ in range(3)] + \
+        [0.3 * rng.standard_normal((m, n, K)) for _ in range(3)]
+    wgt = np.full((m, n, K), 0.5)
+    u = 0.2 * rng.standard_normal((m, n))
+    v = 0.2 * rng.standard_normal((m, n))
+    hx, hy = 1.3, 0.9
+    ax, ay = 1.5 / (hx * hx), 1.5 / (hy * hy)
+    got = oracle.compute_flow_f32(*J, wgt, u, v, 1.5, 1.5, 10, 5, 0.45, hx, hy)
+    ref = _compute_flow_numpy_f32(J, wgt, u, v, ax, ay, 10, 5, 0.45, 1.95)
+    np.testing.assert_array_equal(got, ref.astype(np.float64))
+    f64 = oracle.compute_flow(*J, wgt, u, v, 1.5, 1.5, 10, 5, 0.45, 1.0, hx, hy)
+    assert 0 < np.abs(got - f64).max() <= 1e-6 * np.abs(f64).max()
