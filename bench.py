@@ -135,7 +135,10 @@ def run_diff(args, dev):
     modes = {}
     all_modes = {"implicit": dict(checkpoint="ticks", gradient="implicit"),
                  "unrolled": dict(checkpoint="ticks", gradient="unrolled"),
-                 "unrolled_store_sweeps": dict(checkpoint="sweeps", gradient="unrolled")}
+                 "unrolled_store_sweeps": dict(checkpoint="sweeps", gradient="unrolled"),
+                 "unrolled_stepwise": dict(checkpoint="ticks", gradient="unrolled", adjoint="stepwise"),
+                 "unrolled_store_sweeps_stepwise": dict(checkpoint="sweeps", gradient="unrolled",
+                                                        adjoint="stepwise")}
     for name in args.diff_modes.split(","):
         kw = all_modes[name]
         plan = diff.DiffPlan(H, W, 1, F, dtype=torch.float32, **kw, **opts)
@@ -169,7 +172,8 @@ def run_diff(args, dev):
             "dtype": "f32", "pixel_order": "gauss_seidel",
             "headline": "unrolled: the exact gradient (every half-sweep reversed, psi ticks differentiated); "
                         "checkpoints per level (resized frames, input flow, solver state at each psi tick), "
-                        "each tick window and J recomputed in the backward.  'implicit' holds psi at its last "
+                        "each tick window and J recomputed in the backward, each window's adjoint in one tiled "
+                        "launch ('_stepwise': one launch per half-sweep).  'implicit' holds psi at its last "
                         "tick and differentiates the level's fixed point with one SOR solve on the same "
                         "operator: cheaper, but at a_data = 0.45 it misses most of the exact derivative",
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}

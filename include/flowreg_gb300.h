@@ -339,6 +339,12 @@ typedef struct frg_diff_plan frg_diff_plan;
  * dL/dM = -lam x^T with x the level's final state.  Exact for a converged
  * forward; an approximation of the unrolled gradient otherwise. */
 #define FRG_DIFF_IMPLICIT 2
+/* Backward flag FRG_DIFF_STEPWISE_ADJOINT: run the unrolled adjoint one
+ * launch per half-sweep.  By default each tick window's half-sweeps run in
+ * one launch over tiles with halos held in shared memory (the same
+ * per-pixel arithmetic, so the flow's gradients agree to rounding in the
+ * alpha sums); windows too large for shared memory run stepwise anyway. */
+#define FRG_DIFF_STEPWISE_ADJOINT 4
 
 int frg_diff_plan_create(const frg_params* params, int height, int width, int channels, int max_frames, int flags,
                          frg_diff_plan** out);

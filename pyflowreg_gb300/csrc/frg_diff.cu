@@ -633,6 +633,190 @@ __global__ void kd_rb_adj_step(int color, const T* __restrict__ coef, StateSrc<T
     block_add2(gax, gay, block_slot(galpha));
 }
 
+// One pixel's step of kd_rb_adj_window: the arithmetic of kd_rb_adj_step on
+// shared-memory planes of the tile's region (index li, row pitch Rw).  With
+// ACC the coefficient gradients go to g and the (sx, sy)-scaled alpha
+// gradients to (gax, gay).
+template <typename T, bool ACC>
+__device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, bool gather, const StateSrc<T>& pre,
+                                              long long f, int h, int w, int hw2, T ax, T ay, T omega, int gs,
+                                              const T* sA12, const T* sB1, const T* sB2, const T* sDu, const T* sDv,
+                                              T* sLu, T* sLv, T* sAu, T* sAv, T (&g)[5], T& gax, T& gay, T sx, T sy)
+{
+    const bool hasL = gx > 0, hasR = gx < w - 1, hasT = gy > 0, hasB = gy < h - 1;
+    T lamu = sLu[li], lamv = sLv[li];
+    if (gather) {
+        T su = 0, sv = 0;
+        if (hasL) { su += ax * sAu[li - 1]; sv += ax * sAv[li - 1]; }
+        if (hasR) { su += ax * sAu[li + 1]; sv += ax * sAv[li + 1]; }
+        if (hasT) { su += ay * sAu[li - Rw]; sv += ay * sAv[li - Rw]; }
+        if (hasB) { su += ay * sAu[li + Rw]; sv += ay * sAv[li + Rw]; }
+        lamu += su;
+        lamv += sv;
+    }
+    const T A12 = sA12[li], B1 = sB1[li], B2 = sB2[li];
+    const T den_u = sDu[li], den_v = sDv[li];
+    const T av = omega * lamv / den_v;
+    const T lue = gs ? lamu - A12 * av : lamu;
+    const T au = omega * lue / den_u;
+    const int xl = hasL ? gx - 1 : gx, xr = hasR ? gx + 1 : gx, yt = hasT ? gy - 1 : gy, yb = hasB ? gy + 1 : gy;
+    const T duc = sval(pre, f, 0, gy, gx, h, w, hw2), dvc = sval(pre, f, 1, gy, gx, h, w, hw2);
+    const T Xdu = sval(pre, f, 0, gy, xl, h, w, hw2) + sval(pre, f, 0, gy, xr, h, w, hw2);
+    const T Ydu = sval(pre, f, 0, yt, gx, h, w, hw2) + sval(pre, f, 0, yb, gx, h, w, hw2);
+    const T Xdv = sval(pre, f, 1, gy, xl, h, w, hw2) + sval(pre, f, 1, gy, xr, h, w, hw2);
+    const T Ydv = sval(pre, f, 1, yt, gx, h, w, hw2) + sval(pre, f, 1, yb, gx, h, w, hw2);
+    const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) / den_u;
+    const T dun = ((T)1 - omega) * duc + omega * ru;
+    const T du_for_v = gs ? dun : duc;
+    const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) / den_v;
+    const T self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
+    sLu[li] = ((T)1 - omega) * lue + self * au - (gs ? (T)0 : A12 * av);
+    sLv[li] = ((T)1 - omega) * lamv - A12 * au + self * av;
+    sAu[li] = au;
+    sAv[li] = av;
+    if (ACC) {
+        g[0] -= au * ru;
+        g[1] -= av * rv;
+        g[2] -= au * dvc + av * du_for_v;
+        g[3] -= au;
+        g[4] -= av;
+        const T rr = (T)2 * (au * ru + av * rv);
+        gax += (au * Xdu + av * Xdv - rr) * sx;
+        gay += (au * Ydu + av * Ydv - rr) * sy;
+    }
+}
+
+// Adjoint of all nh half-sweeps of one tick window in one launch (temporal
+// blocking), with kd_rb_adj_step's arithmetic.  A CTA owns a TX x TY tile of
+// one frame and keeps in shared memory the tile grown by nh pixels on every
+// side: per pixel A12, B1e, B2e, the two clamped denominators, lam and the
+// pixel's latest (au, av).  lam of the tile after the window depends on the
+// pixels within j + 1 of the tile at half-sweep j, so step j (from nh - 1 down
+// to 0) updates the moving pixels of that shrinking region: the tile's own
+// pixels and a halo that neighbouring tiles also compute.  Every step reads,
+// per moving pixel, its state and its neighbours' before the half-sweep from
+// the window's stored half-sweeps (hist + j * slot, compressed; s0, NULL:
+// zero, before the first), which the backward wrote with the recomputed or
+// the forward's sweeps.  Thread t owns one horizontal pixel pair of the tile
+// (one pixel of each colour): the pair's coefficient gradients and its alpha
+// gradients stay in registers for the whole window.  The window ends with the
+// closing gather of the tile's colour-1 pixels (kd_rb_adj_gather); the tile's
+// lam goes to lam_out, which is not lam_in (tiles read each other's halo), and
+// its coefficient gradients overwrite gcoef.  blockDim.x = TX * TY / 2.
+template <typename T>
+__global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ coef, const T* __restrict__ s0,
+                                                         const T* __restrict__ hist, long long slot,
+                                                         const T* __restrict__ lam_in, T* __restrict__ lam_out, int h,
+                                                         int w, int nh, int TX, int TY, T ax, T ay, T omega, T eps,
+                                                         int gs, T* __restrict__ gcoef, double sx, double sy,
+                                                         double* __restrict__ galpha)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* const sm = reinterpret_cast<T*>(smraw);
+    const int Rw = TX + 2 * nh, Rh = TY + 2 * nh, R = Rw * Rh;
+    T* const sA12 = sm;
+    T* const sB1 = sm + R;
+    T* const sB2 = sm + 2 * R;
+    T* const sDu = sm + 3 * R;
+    T* const sDv = sm + 4 * R;
+    T* const sLu = sm + 5 * R;
+    T* const sLv = sm + 6 * R;
+    T* const sAu = sm + 7 * R;
+    T* const sAv = sm + 8 * R;
+    const long long f = blockIdx.z, hw = (long long)h * w;
+    const int hw2 = (w + 1) >> 1;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int rx0 = x0 - nh, ry0 = y0 - nh;
+    {
+        const T* cf = coef + f * 5 * hw;
+        const T* liu = lam_in + f * 2 * hw;
+        const T* liv = liu + hw;
+        const T sw = ax + ax + ay + ay;
+        for (int i = threadIdx.x; i < R; i += blockDim.x) {
+            const int gy = ry0 + i / Rw, gx = rx0 + i % Rw;
+            if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
+                const long long p = (long long)gy * w + gx;
+                sA12[i] = cf[2 * hw + p];
+                sB1[i] = cf[3 * hw + p];
+                sB2[i] = cf[4 * hw + p];
+                sDu[i] = tmax(cf[p] + sw, eps);
+                sDv[i] = tmax(cf[hw + p] + sw, eps);
+                sLu[i] = liu[p];
+                sLv[i] = liv[p];
+            }
+        }
+    }
+    __syncthreads();
+    const int hp = TX >> 1;
+    const int oy = threadIdx.x / hp, ox = 2 * (threadIdx.x - (threadIdx.x / hp) * hp);
+    const int py = y0 + oy;
+    T g[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
+    T gax = 0, gay = 0;
+    T dummy[5];
+    T dax = 0, day = 0;
+    const T tsx = (T)sx, tsy = (T)sy;
+    for (int j = nh - 1; j >= 0; --j) {
+        const int c = j & 1;
+        const T* own = j >= 2 ? hist + (long long)(j - 2) * slot : nullptr;
+        const T* oth = j >= 1 ? hist + (long long)(j - 1) * slot : nullptr;
+        const StateSrc<T> pre{s0, c == 0 ? own : oth, c == 0 ? oth : own};
+        const bool gather = j < nh - 1;
+        {
+            const int px = x0 + ox + ((c - (x0 + ox + py)) & 1);
+            if (py < h && px < w) {
+                const int li = (py - ry0) * Rw + (px - rx0);
+                if (c == 0)
+                    adj_window_px<T, true>(px, py, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1,
+                                           sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[0], gax, gay, tsx, tsy);
+                else
+                    adj_window_px<T, true>(px, py, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1,
+                                           sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[1], gax, gay, tsx, tsy);
+            }
+        }
+        const int d = j + 1;
+        const int Ap = (TX + 2 * d) >> 1, Ah = TY + 2 * d;
+        const int ax0 = x0 - d, ay0 = y0 - d;
+        for (int i = threadIdx.x; i < Ah * Ap; i += blockDim.x) {
+            const int r = i / Ap;
+            const int gy = ay0 + r;
+            int gx = ax0 + 2 * (i - r * Ap);
+            gx += (c - gx - gy) & 1;
+            if (gy < 0 || gy >= h || gx < 0 || gx >= w) continue;
+            if (gy >= y0 && gy < y0 + TY && gx >= x0 && gx < x0 + TX) continue;
+            const int li = (gy - ry0) * Rw + (gx - rx0);
+            adj_window_px<T, false>(gx, gy, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1, sB2,
+                                    sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
+        }
+        __syncthreads();
+    }
+    // the closing gather (colour 1), then the tile's lam and coefficient gradients
+    if (py < h) {
+        T* lou = lam_out + f * 2 * hw;
+        T* gc = gcoef + f * 5 * hw;
+        for (int c = 0; c < 2; ++c) {
+            const int px = x0 + ox + ((c - (x0 + ox + py)) & 1);
+            if (px >= w) continue;
+            const int li = (py - ry0) * Rw + (px - rx0);
+            T lu = sLu[li], lv = sLv[li];
+            if (c == 1) {
+                T su = 0, sv = 0;
+                if (px > 0) { su += ax * sAu[li - 1]; sv += ax * sAv[li - 1]; }
+                if (px < w - 1) { su += ax * sAu[li + 1]; sv += ax * sAv[li + 1]; }
+                if (py > 0) { su += ay * sAu[li - Rw]; sv += ay * sAv[li - Rw]; }
+                if (py < h - 1) { su += ay * sAu[li + Rw]; sv += ay * sAv[li + Rw]; }
+                lu += su;
+                lv += sv;
+            }
+            const long long p = (long long)py * w + px;
+            lou[p] = lu;
+            lou[hw + p] = lv;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) gc[k * hw + p] = g[c][k];
+        }
+    }
+    block_add2(gax, gay, block_slot(galpha));
+}
+
 // The closing gather of a window: pixels of colour `color` (which did not move
 // in the window's first half-sweep) add w * a_0 of their moving neighbours.
 template <typename T>
@@ -989,6 +1173,35 @@ cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pr
     return cudaGetLastError();
 }
 
+// Tile edge of kd_rb_adj_window for windows of nh half-sweeps: 32 or 16
+// (square tiles), the largest whose shared memory, 9 planes of the tile grown
+// by nh on every side, fits; 0 when none does (the window then runs one launch
+// per half-sweep).
+int rb_adj_window_tile(int nh, int elem_bytes)
+{
+    for (int t : {32, 16}) {
+        const size_t bytes = (size_t)9 * (t + 2 * nh) * (t + 2 * nh) * elem_bytes;
+        if (bytes <= kAdjWindowSmem) return t;
+    }
+    return 0;
+}
+
+template <typename T>
+cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long slot, const T* lam_in, T* lam_out,
+                          int F, int h, int w, int nh, int tile, double ax, double ay, double omega, double eps, int gs,
+                          T* gcoef, double sx, double sy, double* galpha, cudaStream_t st)
+{
+    const size_t bytes = (size_t)9 * (tile + 2 * nh) * (tile + 2 * nh) * sizeof(T);
+    if (tile < 2 || (tile & 1) || bytes > kAdjWindowSmem) return cudaErrorInvalidValue;
+    const cudaError_t e = ensure_max_dyn_smem((const void*)kd_rb_adj_window<T>, (int)kAdjWindowSmem);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((w + tile - 1) / tile, (h + tile - 1) / tile, F);
+    kd_rb_adj_window<T><<<grid, tile * tile / 2, bytes, st>>>(coef, s0, hist, slot, lam_in, lam_out, h, w, nh, tile,
+                                                             tile, (T)ax, (T)ay, (T)omega, (T)eps, gs, gcoef, sx, sy,
+                                                             galpha);
+    return cudaGetLastError();
+}
+
 cudaError_t reduce_slots(double* part, int F, long long n_slots, double* galpha, cudaStream_t st)
 {
     kd_reduce_slots<<<F, 256, 0, st>>>(part, n_slots, galpha);
@@ -1052,6 +1265,9 @@ cudaError_t median_adj(const T* d, const T* g, int32_t* am, int F, int h, int w,
                                         int, double, double, double, double, int, T*, double, double, double*,  \
                                         cudaStream_t);                                                          \
     template cudaError_t rb_adj_gather<T>(int, T*, const T*, int, int, int, double, double, cudaStream_t);      \
+    template cudaError_t rb_adj_window<T>(const T*, const T*, const T*, long long, const T*, T*, int, int, int, int,  \
+                                          int, double, double, double, double, int, T*, double, double, double*,     \
+                                          cudaStream_t);                                                              \
     template cudaError_t tick_adj<T>(const T*, const T*, const T*, const T*, const T*, int, int, int, int,       \
                                      const double*, double, double, double, int, T*, T*, T*, double, double,    \
                                      double*, cudaStream_t);                                                    \

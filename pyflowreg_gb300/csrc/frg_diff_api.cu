@@ -131,6 +131,7 @@ struct frg_diff_plan {
     void* galpha = nullptr;  // (F, 2) doubles, when the caller passes none
     double* partA = nullptr; // per-block alpha partials of the half-sweep adjoints (F, H, ceil(ceil(W/2)/128), 2)
     double* partB = nullptr; // per-block alpha partials of the per-pixel adjoints (F, H, ceil(W/128), 2)
+    double* partC = nullptr; // per-tile alpha partials of the tiled window adjoints (F, ceil(H/16), ceil(W/16), 2)
     void* gJ = nullptr;      // (F, 6, K, hw)
     void* G = nullptr;       // (F, K, 5, hw)
     void* gf1 = nullptr;     // (F, K, hw)
@@ -279,7 +280,7 @@ int run_forward(frg_diff_plan* pl, int F, const T* fixed, const T* moving, const
 
 template <typename T>
 int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, double* g_alpha, int lagged,
-                 int implicit, cudaStream_t st)
+                 int implicit, int stepwise, cudaStream_t st)
 {
     using namespace frg::diff;
     const int F = pl->last_F, K = pl->K, H = pl->H, W = pl->W;
@@ -294,6 +295,7 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
     const int W2 = (W + 1) / 2;
     DCUDA(cudaMemsetAsync(pl->partA, 0, (size_t)F * H * ((W2 + 127) / 128) * 2 * sizeof(double), st));
     DCUDA(cudaMemsetAsync(pl->partB, 0, (size_t)F * H * ((W + 127) / 128) * 2 * sizeof(double), st));
+    DCUDA(cudaMemsetAsync(pl->partC, 0, (size_t)F * ((H + 15) / 16) * ((W + 15) / 16) * 2 * sizeof(double), st));
     int go = 0;
     DCUDA(cudaMemcpyAsync(pl->gout[go], g_flow, (size_t)F * 2 * H * W * es, cudaMemcpyDeviceToDevice, st));
     for (int li = (int)pl->levels.size() - 1; li >= 0; --li) {
@@ -322,8 +324,11 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
         DCUDA(cudaMemsetAsync(gJ, 0, (size_t)F * 6 * K * hw * es, st));
         // u_out = u_in + median(du): the level's input flow receives g_out directly
         DCUDA(cudaMemcpyAsync(guv, gout, plane2 * es, cudaMemcpyDeviceToDevice, st));
+        int lam_i = 0;
         T* lam = (T*)pl->lam[0];
         T* s = (T*)pl->st;
+        // tiled window adjoints (one launch per window) unless stepwise is asked for or a window does not fit
+        const int tile = stepwise ? 0 : rb_adj_window_tile(2 * pl->win, (int)es);
         if (implicit) {
             // psi of the last tick, the level's final state, then one SOR solve of M lam = g
             const int k = pl->n_ticks - 1, start = k * lag, n_it = I - start;
@@ -378,26 +383,38 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
                 else
                     DCUDA(cudaMemcpyAsync(lam, gout, plane2 * es, cudaMemcpyDeviceToDevice, st));
             }
-            DCUDA(cudaMemsetAsync(gcoef, 0, (size_t)F * 5 * hw * es, st));
-            T* abuf[2] = {(T*)pl->abuf[0], (T*)pl->abuf[1]};
-            const T* aprev = nullptr;
-            for (int j = n_half - 1; j >= 0; --j) {
-                // before half-sweep j: its own colour last moved at j - 2, the other at j - 1
-                const T* own = j >= 2 ? base + (size_t)(j - 2) * slot : nullptr;
-                const T* oth = j >= 1 ? base + (size_t)(j - 1) * slot : nullptr;
-                const int c = j & 1;
-                const T* c0 = c == 0 ? own : oth;
-                const T* c1 = c == 0 ? oth : own;
-                T* anext = abuf[j & 1];
-                DLAUNCH(1, rb_adj_step<T>(c, coef, s0, c0, c1, lam, aprev, anext, F, h, w, L.ax, L.ay, om, kEps,
-                                          pl->gs, gcoef, sx, sy, pl->partA, st));
-                aprev = anext;
+            if (tile) {
+                // the window's half-sweeps in one tiled launch, lam into the other buffer
+                T* lam_next = (T*)pl->lam[lam_i ^ 1];
+                DLAUNCH(1, rb_adj_window<T>(coef, s0, base, (long long)slot, lam, lam_next, F, h, w, n_half, tile,
+                                            L.ax, L.ay, om, kEps, pl->gs, gcoef, sx, sy, pl->partC, st));
+                lam_i ^= 1;
+                lam = lam_next;
+            } else {
+                DCUDA(cudaMemsetAsync(gcoef, 0, (size_t)F * 5 * hw * es, st));
+                T* abuf[2] = {(T*)pl->abuf[0], (T*)pl->abuf[1]};
+                const T* aprev = nullptr;
+                for (int j = n_half - 1; j >= 0; --j) {
+                    // before half-sweep j: its own colour last moved at j - 2, the other at j - 1
+                    const T* own = j >= 2 ? base + (size_t)(j - 2) * slot : nullptr;
+                    const T* oth = j >= 1 ? base + (size_t)(j - 1) * slot : nullptr;
+                    const int c = j & 1;
+                    const T* c0 = c == 0 ? own : oth;
+                    const T* c1 = c == 0 ? oth : own;
+                    T* anext = abuf[j & 1];
+                    DLAUNCH(1, rb_adj_step<T>(c, coef, s0, c0, c1, lam, aprev, anext, F, h, w, L.ax, L.ay, om, kEps,
+                                              pl->gs, gcoef, sx, sy, pl->partA, st));
+                    aprev = anext;
+                }
+                DLAUNCH(1, rb_adj_gather<T>(1, lam, aprev, F, h, w, L.ax, L.ay, st));
             }
-            DLAUNCH(1, rb_adj_gather<T>(1, lam, aprev, F, h, w, L.ax, L.ay, st));
             DLAUNCH(1, tick_adj<T>(J, Wl, s0, uv, gcoef, F, K, h, w, pl->a_data, kEps, L.ax, L.ay, lagged, gJ,
                                    s0 ? lam : (T*)nullptr, guv, sx, sy, pl->partB, st));
         }
         DLAUNCH(1, reduce_slots(pl->partA, F, (long long)h * (((w + 1) / 2 + 127) / 128), galpha, st));
+        if (tile && !implicit)
+            DLAUNCH(1, reduce_slots(pl->partC, F, (long long)((h + tile - 1) / tile) * ((w + tile - 1) / tile), galpha,
+                                    st));
         DLAUNCH(1, reduce_slots(pl->partB, F, (long long)h * ((w + 127) / 128), galpha, st));
         T* gf1 = (T*)pl->gf1;
         T* gf2w = (T*)pl->gf2w;
@@ -525,7 +542,8 @@ int frg_diff_plan_create(const frg_params* params, int height, int width, int ch
          (rc = dalloc(pl, &pl->gcoef, F * 5 * hw * es)) || (rc = dalloc(pl, &pl->guv, F * 2 * hw * es)) ||
          (rc = dalloc(pl, &pl->galpha, F * 2 * sizeof(double))) ||
          (rc = dalloc_t(pl, &pl->partA, F * height * (size_t)(((width + 1) / 2 + 127) / 128) * 2)) ||
-         (rc = dalloc_t(pl, &pl->partB, F * height * (size_t)((width + 127) / 128) * 2)) || (rc = dalloc(pl, &pl->gJ, F * 6 * K * hw * es)) ||
+         (rc = dalloc_t(pl, &pl->partB, F * height * (size_t)((width + 127) / 128) * 2)) ||
+         (rc = dalloc_t(pl, &pl->partC, F * (size_t)((height + 15) / 16) * ((width + 15) / 16) * 2)) || (rc = dalloc(pl, &pl->gJ, F * 6 * K * hw * es)) ||
          (rc = dalloc(pl, &pl->G, F * 5 * K * hw * es)) || (rc = dalloc(pl, &pl->gf1, F * K * hw * es)) ||
          (rc = dalloc(pl, &pl->gf2w, F * K * hw * es)) || (rc = dalloc(pl, &pl->gf2l, F * K * hw * es)) ||
          (rc = dalloc(pl, &pl->gout[0], F * 2 * hw * es)) || (rc = dalloc(pl, &pl->gout[1], F * 2 * hw * es)) ||
@@ -605,14 +623,16 @@ int frg_diff_backward(frg_diff_plan* pl, const void* g_flow, void* g_fixed, void
                       int flags, void* stream)
 {
     if (!pl || !g_flow) return host_fail(FRG_EINVAL, "NULL argument");
-    if (flags & ~(FRG_DIFF_LAGGED_PSI | FRG_DIFF_IMPLICIT)) return host_fail(FRG_EINVAL, "unknown flags");
+    if (flags & ~(FRG_DIFF_LAGGED_PSI | FRG_DIFF_IMPLICIT | FRG_DIFF_STEPWISE_ADJOINT))
+        return host_fail(FRG_EINVAL, "unknown flags");
     if (!pl->have_forward) return host_fail(FRG_EINVAL, "no forward pass to differentiate");
     cudaStream_t st = (cudaStream_t)stream;
     const int lagged = (flags & FRG_DIFF_LAGGED_PSI) ? 1 : 0, implicit = (flags & FRG_DIFF_IMPLICIT) ? 1 : 0;
+    const int stepwise = (flags & FRG_DIFF_STEPWISE_ADJOINT) ? 1 : 0;
     return pl->dbl ? run_backward<double>(pl, (const double*)g_flow, (double*)g_fixed, (double*)g_moving, g_alpha,
-                                          lagged, implicit, st)
+                                          lagged, implicit, stepwise, st)
                    : run_backward<float>(pl, (const float*)g_flow, (float*)g_fixed, (float*)g_moving, g_alpha, lagged,
-                                         implicit, st);
+                                         implicit, stepwise, st);
 }
 
 int frg_diff_warp(int precision, int n_frames, int channels, int height, int width, const void* src,

@@ -295,6 +295,18 @@ cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pr
 template <typename T>
 cudaError_t rb_adj_gather(int color, T* lam, const T* aprev, int F, int h, int w, double ax, double ay,
                           cudaStream_t st);
+// All half-sweeps of one window in one launch (tiles with halos in shared
+// memory): hist + j * slot holds the pixels half-sweep j moved, s0 the state
+// before the window (NULL: zero); lam_in -> lam_out (distinct arrays), gcoef
+// overwritten, galpha: one pair per CTA (F * ceil(h / tile) * ceil(w / tile)),
+// summed by reduce_slots.  rb_adj_window_tile gives the tile edge for nh
+// half-sweeps and an element size, 0 when the window does not fit.
+constexpr size_t kAdjWindowSmem = 200 * 1024;
+int rb_adj_window_tile(int nh, int elem_bytes);
+template <typename T>
+cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long slot, const T* lam_in, T* lam_out,
+                          int F, int h, int w, int nh, int tile, double ax, double ay, double omega, double eps, int gs,
+                          T* gcoef, double sx, double sy, double* galpha, cudaStream_t st);
 template <typename T>
 cudaError_t tick_adj(const T* J, const T* W, const T* stt, const T* uv, const T* gcoef, int F, int K, int h, int w,
                      const double* a_data, double eps, double ax, double ay, int lagged, T* gJ, T* lam, T* guv,

@@ -37,6 +37,7 @@ PIXEL_ORDERS = {"gauss_seidel": 0, "torch": 1}
 CHECKPOINTS = {"ticks": 0, "sweeps": 2}
 LAGGED_PSI = 1
 IMPLICIT = 2
+STEPWISE_ADJOINT = 4
 
 
 def _ptr(t):
@@ -77,12 +78,16 @@ class DiffPlan:
     one forward solve, equals the unrolled lagged gradient when the forward
     has converged, and approximates it otherwise.
 
+    adjoint "tiled" (default) runs each tick window's unrolled adjoint in one
+    launch over tiles whose halos live in shared memory; "stepwise" runs one
+    launch per half-sweep.  Both do the same per-pixel arithmetic.
+
     A plan keeps the checkpoints of its last forward only, so the backward of
     a forward must run before the next forward on the same plan (checked)."""
 
     def __init__(self, H: int, W: int, K: int, max_frames: int, dtype=torch.float32, *, levels=100, eta=0.8,
                  iterations=50, update_lag=5, a_data=0.45, omega=1.95, pixel_order="gauss_seidel",
-                 checkpoint="ticks", psi_gradient="exact", gradient="unrolled", device=None):
+                 checkpoint="ticks", psi_gradient="exact", gradient="unrolled", adjoint="tiled", device=None):
         if dtype not in _PREC:
             raise ValueError("dtype must be torch.float32 or torch.float64")
         if pixel_order not in PIXEL_ORDERS:
@@ -93,8 +98,10 @@ class DiffPlan:
             raise ValueError("psi_gradient must be 'exact' or 'lagged'")
         if gradient not in ("unrolled", "implicit"):
             raise ValueError("gradient must be 'unrolled' or 'implicit'")
+        if adjoint not in ("tiled", "stepwise"):
+            raise ValueError("adjoint must be 'tiled' or 'stepwise'")
         self.backward_flags = (LAGGED_PSI if psi_gradient == "lagged" else 0) | (
-            IMPLICIT if gradient == "implicit" else 0)
+            IMPLICIT if gradient == "implicit" else 0) | (STEPWISE_ADJOINT if adjoint == "stepwise" else 0)
         self.lib = _lib.load()
         self.H, self.W, self.K, self.max_frames, self.dtype = int(H), int(W), int(K), int(max_frames), dtype
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())

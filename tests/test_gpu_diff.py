@@ -89,6 +89,39 @@ def test_gradients_match_unrolled_autograd_fp64(K, h, w, its, lag, order, ckpt, 
         assert err <= 1e-5 * max(scale, 1e-12), (err, scale)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("K,h,w,its,lag,order,ckpt", [
+    (1, 75, 100, 23, 5, GS, "ticks"), (2, 70, 66, 12, 3, GS, "sweeps"), (1, 97, 41, 9, 1, GS, "ticks"),
+    (1, 64, 130, 50, 5, GS, "sweeps"), (1, 50, 70, 10, 5, "torch", "ticks")])
+def test_tiled_window_adjoint_equals_stepwise(dtype, K, h, w, its, lag, order, ckpt):
+    """The tiled window adjoint (one launch per tick window, tiles of 32 with
+    halos in shared memory) against the one-launch-per-half-sweep adjoint:
+    both run the same per-pixel arithmetic, so the frame gradients agree to
+    the last bits and the alpha gradients to the rounding of their sums.
+    Shapes span several tiles, with ragged edges, short last windows and
+    update_lag 1, 3 and 5."""
+    from pyflowreg_gb300.diff import flow
+
+    fixed, moving, _, _ = _frames([21, 22], K, h, w)
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(5)
+    r = torch.tensor(rng.standard_normal((2, 2, h, w)), device=dev, dtype=dtype)
+    grads = {}
+    for adj in ("stepwise", "tiled"):
+        plan = _plan(h, w, K, 2, dtype, iterations=its, update_lag=lag, pixel_order=order, checkpoint=ckpt,
+                     adjoint=adj)
+        f_t = torch.tensor(fixed, device=dev, dtype=dtype, requires_grad=True)
+        m_t = torch.tensor(moving, device=dev, dtype=dtype, requires_grad=True)
+        a_t = torch.tensor([1.5, 1.2], dtype=torch.float64, device=dev, requires_grad=True)
+        (flow(f_t, m_t, a_t, plan) * r).sum().backward()
+        grads[adj] = (f_t.grad.double().cpu(), m_t.grad.double().cpu(), a_t.grad.cpu())
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
+    for name, gs, gt in zip(("fixed", "moving", "alpha"), grads["stepwise"], grads["tiled"]):
+        scale = float(gs.abs().max())
+        err = float((gs - gt).abs().max())
+        assert scale > 0 and err <= tol * scale, (name, err, scale)
+
+
 @pytest.mark.parametrize("K,h,w,ckpt", [(1, 32, 36, "ticks"), (2, 30, 26, "sweeps")])
 def test_implicit_gradient_equals_unrolled_at_convergence_fp64(K, h, w, ckpt):
     """With the forward converged (400 sweeps, psi computed once), the
