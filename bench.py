@@ -562,7 +562,7 @@ def profiled_fp64_ops():
     try:
         for line in open(path):
             parts = line.split()
-            if len(parts) >= 3 and parts[0] == "k_sor_chain64" and parts[1] == "fp64_ops_per_pixel_update":
+            if len(parts) >= 3 and parts[0] == "k_sor_chain64" and parts[1] == "fp64_flops_per_pixel_update":
                 return float(parts[2])
     except OSError:
         pass
