@@ -12,16 +12,22 @@
 //   c_j = 1 + (j + 1/2) / 256, inv_j = double(1 / c_j), r = m inv_j - 1
 //     (one fused multiply-add, |r| <= 2^-9);
 //   log2 x = e - log2(inv_j) + log2(1 + r), log2(1 + r) by its Taylor series
-//     to r^6 (truncation below 2^-65); -log2(inv_j) is tabulated as
-//     Lhi + Llo with Lhi a multiple of 2^-42, so e + Lhi is exact;
-//   y = b log2 x = yh + yl (the product's rounding error kept by an fma);
-//   k = round(128 yh), f = yh - k / 128 + yl, |f| <= 2^-8;
-//   2^y = 2^(k >> 7) * 2^((k & 127) / 128) * (1 + q(f)), q the Taylor series
-//     of 2^f - 1 to f^5 (truncation below 2^-60).
+//     to r^5 (truncation below 2^-56, a tenth of an ulp of the result);
+//     -log2(inv_j) is tabulated as Lhi + Llo with Lhi a multiple of 2^-42, so
+//     e + Lhi is exact;
+//   y = b log2 x = yh + yl: yh = b (e + Lhi) rounded, yl its rounding error
+//     (an fma) plus b (Llo + log2(1 + r)), so |yl| <= |b| 2^-8.5;
+//   k = round(256 yh), f = yh - k / 256 + yl, |f| <= 2^-9 + |b| 2^-8.5;
+//   2^y = 2^(k >> 8) * 2^((k & 255) / 256) * (1 + q(f)), q the Taylor series
+//     of 2^f - 1 to f^5 (truncation below 2^-60 for |b| <= 1).
+// An exact emulation of these steps (rational arithmetic for every rounding)
+// stays within 1 ulp of the correctly rounded power; without the f^5 term of
+// the exp series it is off by up to 11 ulp (f includes yl).
 // Every step is one rounding of a value below the result's ulp except the
 // final two, so the result is within a few ulp of x^b.  Positive normal x
-// with |b log2 x| < 1000 take this path; anything else (0, denormals,
-// infinities, NaN, huge results) goes to pow().
+// with |b log2 x| < 512 take this path; anything else (0, denormals,
+// infinities, NaN, huge results) goes to pow().  Range tests are integer
+// tests on the high words, which keeps them off the float64 pipe.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -29,7 +35,7 @@
 namespace frg {
 
 constexpr int kDpowLogN = 256;   // log table entries: (inv_j, Lhi - 1023, Llo)
-constexpr int kDpowExpN = 128;   // exp table entries: 2^(i / 128)
+constexpr int kDpowExpN = 256;   // exp table entries: 2^(i / 256)
 
 // The tables (device memory of this translation unit; the library is built
 // without relocatable device code, so only frg_sor64.cu includes this header),
@@ -43,7 +49,6 @@ constexpr double kL2 = -0.72134752044448170368;
 constexpr double kL3 = 0.48089834696298780245;
 constexpr double kL4 = -0.36067376022224085184;
 constexpr double kL5 = 0.28853900817779268147;
-constexpr double kL6 = -0.24044917348149390123;
 // (ln 2)^i / i!: 2^f - 1 = sum_i (f ln 2)^i / i!
 constexpr double kE1 = 0.69314718055994530942;
 constexpr double kE2 = 0.24022650695910071233;
@@ -61,8 +66,7 @@ __device__ __forceinline__ double dpow_tab(double x, double b)
     const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
     const double* lt = g_dpow_log + 3 * j;
     const double r = __fma_rn(m, __ldg(lt), -1.0);
-    double p = __fma_rn(r, kL6, kL5);
-    p = __fma_rn(r, p, kL4);
+    double p = __fma_rn(r, kL5, kL4);
     p = __fma_rn(r, p, kL3);
     p = __fma_rn(r, p, kL2);
     p = __fma_rn(r, p, kL1);
@@ -73,20 +77,20 @@ __device__ __forceinline__ double dpow_tab(double x, double b)
     const double yh = __dmul_rn(b, lh);
     double yl = __fma_rn(b, lh, -yh);
     yl = __fma_rn(b, ll, yl);
-    if (!(fabs(yh) < 1000.0)) return pow(x, b);
-    const double t = __fma_rn(yh, 128.0, 6755399441055744.0);  // 1.5 * 2^52: round(128 yh) in the low word
+    if ((__double2hiint(yh) & 0x7fffffff) >= 0x40800000) return pow(x, b);  // |yh| >= 512, or NaN
+    const double t = __fma_rn(yh, 256.0, 6755399441055744.0);  // 1.5 * 2^52: round(256 yh) in the low word
     const int k = __double2loint(t);
     const double kd = __dsub_rn(t, 6755399441055744.0);
-    double f = __fma_rn(kd, -0.0078125, yh);
+    double f = __fma_rn(kd, -0.00390625, yh);
     f = __dadd_rn(f, yl);
     double q = __fma_rn(f, kE5, kE4);
     q = __fma_rn(f, q, kE3);
     q = __fma_rn(f, q, kE2);
     q = __fma_rn(f, q, kE1);
     q = __dmul_rn(f, q);
-    const double E = __ldg(g_dpow_exp + (k & 127));
+    const double E = __ldg(g_dpow_exp + (k & 255));
     const double res = __fma_rn(E, q, E);
-    return __hiloint2double(__double2hiint(res) + (k >> 7) * 0x100000, __double2loint(res));
+    return __hiloint2double(__double2hiint(res) + (k >> 8) * 0x100000, __double2loint(res));
 }
 
 // Host: fills the tables on the current device (once per device).

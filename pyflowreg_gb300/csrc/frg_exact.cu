@@ -472,8 +472,9 @@ __global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__
     for (int k = 0; k < K; ++k) {
         double j[6];
         tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
+        // the cross terms doubled (exact), as the solver's data residual uses them
 #pragma unroll
-        for (int q = 0; q < 6; ++q) Jf[((long long)q * K + k) * plane + di] = j[q];
+        for (int q = 0; q < 6; ++q) Jf[((long long)q * K + k) * plane + di] = q < 3 ? j[q] : dadd(j[q], j[q]);
     }
     const long long n = w + 2;
     const double* uf = u + f * uv_fs;

@@ -60,7 +60,7 @@ cudaError_t upload_dpow_tables()
         lt[3 * j + 1] = Lhi - 1023.0;  // exact: a multiple of 2^-42 below 1024 in magnitude
         lt[3 * j + 2] = Llo;
     }
-    for (int i = 0; i < kDpowExpN; ++i) et[i] = (double)exp2l((long double)i / 128.0L);
+    for (int i = 0; i < kDpowExpN; ++i) et[i] = (double)exp2l((long double)i / (long double)kDpowExpN);
     if ((e = cudaMemcpyToSymbol(g_dpow_log, lt, sizeof(lt))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(g_dpow_exp, et, sizeof(et))) != cudaSuccess) return e;
     done.insert(dev);
@@ -159,12 +159,16 @@ __device__ __forceinline__ double rcp64(double x)
 }
 
 // omega / den, 0 when den is 0 (core/level_solver.py:352, 363); subnormal,
-// infinite or NaN denominators take the division.
+// infinite or NaN denominators take the division.  The tests look at the bits
+// (integer instructions), not at the value (float64 compares).
 __device__ __forceinline__ double omega_over(double omega, double den)
 {
-    if (den == 0.0) return 0.0;
-    const int ex = __double2hiint(den) & 0x7ff00000;
-    if (ex == 0 || ex == 0x7ff00000) return __ddiv_rn(omega, den);
+    const int hi = __double2hiint(den);
+    const int ex = hi & 0x7ff00000;
+    if (ex == 0 || ex == 0x7ff00000) {
+        if (((hi & 0x7fffffff) | __double2loint(den)) == 0) return 0.0;
+        return __ddiv_rn(omega, den);
+    }
     return __dmul_rn(omega, rcp64(den));
 }
 
@@ -175,6 +179,9 @@ __device__ __forceinline__ double omega_over(double omega, double den)
 //   A12 = sum_k W psi J12,  BU = lap_u - sum_k W psi J13,  BV = lap_v - sum_k W psi J23,
 //   iDu = omega / (wsum + sum_k W psi J11) (0 when the denominator is 0), iDv likewise
 //   (omega times the reciprocal: within an ulp or two of the quotient).
+// The tensor holds the cross terms doubled (2 J12, 2 J13, 2 J23, exact), as E
+// uses them; the sums over them are then twice the sums above, exactly, and
+// A12 = sum / 2, BU = fma(-1/2, sum, lap_u) give the same bits.
 template <int K, bool CO>
 __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldIn64<K>& r, double du, double dv)
 {
@@ -196,12 +203,12 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldI
         double wp = r.w[k];
         if (tick) {
             const double a = du, b = dv;
-            // E = a (J11 a + 2 J12 b + 2 J13) + b (J22 b + 2 J23) + J33: 8 float64 operations
-            double t = __fma_rn(j11, a, __dadd_rn(j13, j13));
-            t = __fma_rn(__dadd_rn(j12, j12), b, t);
-            const double q = __fma_rn(j22, b, __dadd_rn(j23, j23));
+            // E = a (J11 a + 2 J12 b + 2 J13) + b (J22 b + 2 J23) + J33: 5 float64 operations
+            double t = __fma_rn(j11, a, j13);
+            t = __fma_rn(j12, b, t);
+            const double q = __fma_rn(j22, b, j23);
             double E = __fma_rn(t, a, __fma_rn(q, b, j33));
-            E = fmax(E, 0.0);
+            if (__double2hiint(E) < 0) E = 0.0;  // max(E, 0) on the sign bit
             wp = __dmul_rn(wp, __dmul_rn(A.a_data[k], dpow_tab(__dadd_rn(E, 0.00001), A.a_m1[k])));
         }
         den_u = __fma_rn(wp, j11, den_u);
@@ -210,9 +217,9 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldI
         c13 = __fma_rn(wp, j13, c13);
         c23 = __fma_rn(wp, j23, c23);
     }
-    o.A12 = a12;
-    o.BU = __dsub_rn(r.lu, c13);
-    o.BV = __dsub_rn(r.lv, c23);
+    o.A12 = __dmul_rn(0.5, a12);
+    o.BU = __fma_rn(-0.5, c13, r.lu);
+    o.BV = __fma_rn(-0.5, c23, r.lv);
     o.iDu = omega_over(A.omega, den_u);
     o.iDv = omega_over(A.omega, den_v);
     return o;
