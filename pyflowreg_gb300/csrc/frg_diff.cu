@@ -633,15 +633,74 @@ __global__ void kd_rb_adj_step(int color, const T* __restrict__ coef, StateSrc<T
     block_add2(gax, gay, block_slot(galpha));
 }
 
+// Asynchronous copy of one element global -> shared (cp.async, 4 or 8 bytes).
+template <typename T>
+__device__ __forceinline__ void cp_async_el(T* dst, const T* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Solver state of one colour before a half-sweep, as kd_rb_adj_window stages
+// it: kind 0 zero, 1 a full array (F, 2, h, w), 2 a compressed array of that
+// colour's pixels (F, 2, h, (w + 1) / 2).
+template <typename T>
+struct StateSlice {
+    const T* p;
+    int kind;
+};
+
+// Copies colour c of a state slice over the window's outer region (origin
+// (rx1, ry1), Rh1 rows of Rp1 pixel pairs; pair k of a row holds columns
+// rx1 + 2k and rx1 + 2k + 1, one of each colour) into dst: plane u at dst,
+// plane v at dst + Rh1 * Rp1, entry row * Rp1 + k.  Pixels outside the level
+// are left alone (never read).  Issues cp.async copies and commits them.
+template <typename T>
+__device__ __forceinline__ void stage_colour(T* dst, int c, StateSlice<T> src, long long f, int h, int w, int hw2,
+                                             int rx1, int ry1, int Rh1, int Rp1, float inv_rp1)
+{
+    const int n = Rh1 * Rp1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int row = (int)(((float)i + 0.5f) * inv_rp1);
+        const int k = i - row * Rp1;
+        const int gy = ry1 + row;
+        const int gx = rx1 + 2 * k + ((c - rx1 - gy) & 1);
+        if (gy < 0 || gy >= h || gx < 0 || gx >= w) continue;
+        if (src.kind == 0) {
+            dst[i] = (T)0;
+            dst[n + i] = (T)0;
+        } else if (src.kind == 1) {
+            const T* q = src.p + ((f * 2) * h + gy) * (long long)w + gx;
+            cp_async_el(dst + i, q);
+            cp_async_el(dst + n + i, q + (long long)h * w);
+        } else {
+            const T* q = src.p + ((f * 2) * h + gy) * (long long)hw2 + (gx >> 1);
+            cp_async_el(dst + i, q);
+            cp_async_el(dst + n + i, q + (long long)h * hw2);
+        }
+    }
+    cp_async_commit();
+}
+
 // One pixel's step of kd_rb_adj_window: the arithmetic of kd_rb_adj_step on
-// shared-memory planes of the tile's region (index li, row pitch Rw).  With
+// shared-memory planes.  li indexes the coefficient / lam / (au, av) planes
+// (row pitch Rw); sb the pixel in the staged states (row pitch Rp1, pair
+// column; p = the pixel's column parity within its pair): its own state in
+// `own`, its neighbours' (the other colour) in `oth`, planes n1 apart.  With
 // ACC the coefficient gradients go to g and the (sx, sy)-scaled alpha
 // gradients to (gax, gay).
 template <typename T, bool ACC>
-__device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, bool gather, const StateSrc<T>& pre,
-                                              long long f, int h, int w, int hw2, T ax, T ay, T omega, int gs,
-                                              const T* sA12, const T* sB1, const T* sB2, const T* sDu, const T* sDv,
-                                              T* sLu, T* sLv, T* sAu, T* sAv, T (&g)[5], T& gax, T& gay, T sx, T sy)
+__device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, int sb, int p, int Rp1, int n1,
+                                              bool gather, const T* own, const T* oth, int h, int w, T ax, T ay,
+                                              T omega, int gs, const T* sA12, const T* sB1, const T* sB2,
+                                              const T* sDu, const T* sDv, T* sLu, T* sLv, T* sAu, T* sAv,
+                                              T (&g)[5], T& gax, T& gay, T sx, T sy)
 {
     const bool hasL = gx > 0, hasR = gx < w - 1, hasT = gy > 0, hasB = gy < h - 1;
     T lamu = sLu[li], lamv = sLv[li];
@@ -659,12 +718,12 @@ __device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, bo
     const T av = omega * lamv / den_v;
     const T lue = gs ? lamu - A12 * av : lamu;
     const T au = omega * lue / den_u;
-    const int xl = hasL ? gx - 1 : gx, xr = hasR ? gx + 1 : gx, yt = hasT ? gy - 1 : gy, yb = hasB ? gy + 1 : gy;
-    const T duc = sval(pre, f, 0, gy, gx, h, w, hw2), dvc = sval(pre, f, 1, gy, gx, h, w, hw2);
-    const T Xdu = sval(pre, f, 0, gy, xl, h, w, hw2) + sval(pre, f, 0, gy, xr, h, w, hw2);
-    const T Ydu = sval(pre, f, 0, yt, gx, h, w, hw2) + sval(pre, f, 0, yb, gx, h, w, hw2);
-    const T Xdv = sval(pre, f, 1, gy, xl, h, w, hw2) + sval(pre, f, 1, gy, xr, h, w, hw2);
-    const T Ydv = sval(pre, f, 1, yt, gx, h, w, hw2) + sval(pre, f, 1, yb, gx, h, w, hw2);
+    const T duc = own[sb], dvc = own[n1 + sb];
+    const int sL = sb - 1 + p, sR = sb + p, sT = sb - Rp1, sB = sb + Rp1;
+    const T Xdu = (hasL ? oth[sL] : duc) + (hasR ? oth[sR] : duc);
+    const T Ydu = (hasT ? oth[sT] : duc) + (hasB ? oth[sB] : duc);
+    const T Xdv = (hasL ? oth[n1 + sL] : dvc) + (hasR ? oth[n1 + sR] : dvc);
+    const T Ydv = (hasT ? oth[n1 + sT] : dvc) + (hasB ? oth[n1 + sB] : dvc);
     const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) / den_u;
     const T dun = ((T)1 - omega) * duc + omega * ru;
     const T du_for_v = gs ? dun : duc;
@@ -688,21 +747,25 @@ __device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, bo
 
 // Adjoint of all nh half-sweeps of one tick window in one launch (temporal
 // blocking), with kd_rb_adj_step's arithmetic.  A CTA owns a TX x TY tile of
-// one frame and keeps in shared memory the tile grown by nh pixels on every
-// side: per pixel A12, B1e, B2e, the two clamped denominators, lam and the
-// pixel's latest (au, av).  lam of the tile after the window depends on the
-// pixels within j + 1 of the tile at half-sweep j, so step j (from nh - 1 down
-// to 0) updates the moving pixels of that shrinking region: the tile's own
-// pixels and a halo that neighbouring tiles also compute.  Every step reads,
-// per moving pixel, its state and its neighbours' before the half-sweep from
-// the window's stored half-sweeps (hist + j * slot, compressed; s0, NULL:
-// zero, before the first), which the backward wrote with the recomputed or
-// the forward's sweeps.  Thread t owns one horizontal pixel pair of the tile
-// (one pixel of each colour): the pair's coefficient gradients and its alpha
-// gradients stay in registers for the whole window.  The window ends with the
-// closing gather of the tile's colour-1 pixels (kd_rb_adj_gather); the tile's
-// lam goes to lam_out, which is not lam_in (tiles read each other's halo), and
-// its coefficient gradients overwrite gcoef.  blockDim.x = TX * TY / 2.
+// one frame (TX = TY = 16 or 32) and keeps in shared memory:
+//  * over the tile grown by nh pixels on every side (Rw x Rh): A12, B1e, B2e,
+//    the two clamped denominators, lam and the pixel's latest (au, av);
+//  * over the tile grown by nh + 1 (Rh1 rows of Rp1 pixel pairs), per colour
+//    two buffers of the solver state before a half-sweep, filled by cp.async
+//    from the window's stored half-sweeps (hist + j * slot, compressed; s0,
+//    NULL: zero, before the first) one step ahead: before half-sweep j the
+//    moving colour holds its values after j - 2 and the other colour after
+//    j - 1, so each step replaces one colour.
+// lam of the tile after the window depends on the pixels within j + 1 of the
+// tile at half-sweep j, so step j (from nh - 1 down to 0) updates the moving
+// pixels of that shrinking region: the tile's own pixels and a halo that
+// neighbouring tiles also compute.  Thread t owns one horizontal pixel pair of
+// the tile (one pixel of each colour): the pair's coefficient gradients and
+// its alpha gradients stay in registers for the whole window.  The window ends
+// with the closing gather of the tile's colour-1 pixels (kd_rb_adj_gather);
+// the tile's lam goes to lam_out, which is not lam_in (tiles read each other's
+// halo), and its coefficient gradients overwrite gcoef.
+// blockDim.x = TX * TY / 2.
 template <typename T>
 __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ coef, const T* __restrict__ s0,
                                                          const T* __restrict__ hist, long long slot,
@@ -714,6 +777,7 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     extern __shared__ __align__(16) unsigned char smraw[];
     T* const sm = reinterpret_cast<T*>(smraw);
     const int Rw = TX + 2 * nh, Rh = TY + 2 * nh, R = Rw * Rh;
+    const int Rp1 = (Rw + 2) >> 1, Rh1 = Rh + 2, n1 = Rh1 * Rp1;
     T* const sA12 = sm;
     T* const sB1 = sm + R;
     T* const sB2 = sm + 2 * R;
@@ -723,71 +787,97 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     T* const sLv = sm + 6 * R;
     T* const sAu = sm + 7 * R;
     T* const sAv = sm + 8 * R;
+    T* const sS = sm + 9 * R;  // state buffers: (colour * 2 + buffer) * 2 * n1
     const long long f = blockIdx.z, hw = (long long)h * w;
     const int hw2 = (w + 1) >> 1;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int rx0 = x0 - nh, ry0 = y0 - nh;
+    const int rx1 = rx0 - 1, ry1 = ry0 - 1;
+    const float inv_rp1 = 1.0f / (float)Rp1;
+    auto slice = [&](int k) -> StateSlice<T> {
+        if (k >= 0) return StateSlice<T>{hist + (long long)k * slot, 2};
+        return StateSlice<T>{s0, s0 ? 1 : 0};
+    };
+    auto buf = [&](int c, int b) { return sS + (c * 2 + b) * 2 * n1; };
+    // the states before the window's last half-sweep nh - 1 (colour 1): colour 1
+    // after nh - 3, colour 0 after nh - 2
+    stage_colour<T>(buf(1, 0), 1, slice(nh - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
+    stage_colour<T>(buf(0, 0), 0, slice(nh - 2), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
     {
         const T* cf = coef + f * 5 * hw;
         const T* liu = lam_in + f * 2 * hw;
         const T* liv = liu + hw;
         const T sw = ax + ax + ay + ay;
+        const float inv_rw = 1.0f / (float)Rw;
         for (int i = threadIdx.x; i < R; i += blockDim.x) {
-            const int gy = ry0 + i / Rw, gx = rx0 + i % Rw;
+            const int ry = (int)(((float)i + 0.5f) * inv_rw);
+            const int gy = ry0 + ry, gx = rx0 + (i - ry * Rw);
             if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
-                const long long p = (long long)gy * w + gx;
-                sA12[i] = cf[2 * hw + p];
-                sB1[i] = cf[3 * hw + p];
-                sB2[i] = cf[4 * hw + p];
-                sDu[i] = tmax(cf[p] + sw, eps);
-                sDv[i] = tmax(cf[hw + p] + sw, eps);
-                sLu[i] = liu[p];
-                sLv[i] = liv[p];
+                const long long q = (long long)gy * w + gx;
+                sA12[i] = cf[2 * hw + q];
+                sB1[i] = cf[3 * hw + q];
+                sB2[i] = cf[4 * hw + q];
+                sDu[i] = tmax(cf[q] + sw, eps);
+                sDv[i] = tmax(cf[hw + q] + sw, eps);
+                sLu[i] = liu[q];
+                sLv[i] = liv[q];
             }
         }
     }
+    cp_async_wait_all();
     __syncthreads();
     const int hp = TX >> 1;
-    const int oy = threadIdx.x / hp, ox = 2 * (threadIdx.x - (threadIdx.x / hp) * hp);
+    const int oy = threadIdx.x / hp, ox = 2 * (threadIdx.x - oy * hp);
     const int py = y0 + oy;
     T g[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
     T gax = 0, gay = 0;
     T dummy[5];
     T dax = 0, day = 0;
     const T tsx = (T)sx, tsy = (T)sy;
+    int cur[2] = {0, 0};
     for (int j = nh - 1; j >= 0; --j) {
         const int c = j & 1;
-        const T* own = j >= 2 ? hist + (long long)(j - 2) * slot : nullptr;
-        const T* oth = j >= 1 ? hist + (long long)(j - 1) * slot : nullptr;
-        const StateSrc<T> pre{s0, c == 0 ? own : oth, c == 0 ? oth : own};
+        const T* own = buf(c, cur[c]);
+        const T* oth = buf(c ^ 1, cur[c ^ 1]);
+        // the other colour's state for step j - 1 (its values after j - 3), one step ahead
+        if (j >= 1)
+            stage_colour<T>(buf(c ^ 1, cur[c ^ 1] ^ 1), c ^ 1, slice(j - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1,
+                            inv_rp1);
         const bool gather = j < nh - 1;
         {
             const int px = x0 + ox + ((c - (x0 + ox + py)) & 1);
             if (py < h && px < w) {
                 const int li = (py - ry0) * Rw + (px - rx0);
+                const int sb = (py - ry1) * Rp1 + ((px - rx1) >> 1);
+                const int pp = (px - rx1) & 1;
                 if (c == 0)
-                    adj_window_px<T, true>(px, py, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1,
-                                           sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[0], gax, gay, tsx, tsy);
+                    adj_window_px<T, true>(px, py, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
+                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[0], gax, gay, tsx, tsy);
                 else
-                    adj_window_px<T, true>(px, py, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1,
-                                           sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[1], gax, gay, tsx, tsy);
+                    adj_window_px<T, true>(px, py, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
+                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[1], gax, gay, tsx, tsy);
             }
         }
         const int d = j + 1;
         const int Ap = (TX + 2 * d) >> 1, Ah = TY + 2 * d;
         const int ax0 = x0 - d, ay0 = y0 - d;
+        const float inv_ap = 1.0f / (float)Ap;
         for (int i = threadIdx.x; i < Ah * Ap; i += blockDim.x) {
-            const int r = i / Ap;
+            const int r = (int)(((float)i + 0.5f) * inv_ap);
             const int gy = ay0 + r;
             int gx = ax0 + 2 * (i - r * Ap);
             gx += (c - gx - gy) & 1;
             if (gy < 0 || gy >= h || gx < 0 || gx >= w) continue;
             if (gy >= y0 && gy < y0 + TY && gx >= x0 && gx < x0 + TX) continue;
             const int li = (gy - ry0) * Rw + (gx - rx0);
-            adj_window_px<T, false>(gx, gy, li, Rw, gather, pre, f, h, w, hw2, ax, ay, omega, gs, sA12, sB1, sB2,
-                                    sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
+            const int sb = (gy - ry1) * Rp1 + ((gx - rx1) >> 1);
+            const int pp = (gx - rx1) & 1;
+            adj_window_px<T, false>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs, sA12,
+                                    sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
         }
+        cp_async_wait_all();
         __syncthreads();
+        cur[c ^ 1] ^= 1;
     }
     // the closing gather (colour 1), then the tile's lam and coefficient gradients
     if (py < h) {
@@ -807,11 +897,11 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
                 lu += su;
                 lv += sv;
             }
-            const long long p = (long long)py * w + px;
-            lou[p] = lu;
-            lou[hw + p] = lv;
+            const long long q = (long long)py * w + px;
+            lou[q] = lu;
+            lou[hw + q] = lv;
 #pragma unroll
-            for (int k = 0; k < 5; ++k) gc[k * hw + p] = g[c][k];
+            for (int k = 0; k < 5; ++k) gc[k * hw + q] = g[c][k];
         }
     }
     block_add2(gax, gay, block_slot(galpha));
@@ -1173,16 +1263,22 @@ cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pr
     return cudaGetLastError();
 }
 
-// Tile edge of kd_rb_adj_window for windows of nh half-sweeps: 32 or 16
-// (square tiles), the largest whose shared memory, 9 planes of the tile grown
-// by nh on every side, fits; 0 when none does (the window then runs one launch
-// per half-sweep).
+// Shared memory of kd_rb_adj_window for square tiles of edge t and windows of
+// nh half-sweeps: 9 planes over the tile grown by nh, 4 state planes (2 per
+// colour buffer pair, half a plane each) over the tile grown by nh + 1.
+size_t adj_window_smem(int t, int nh, int elem_bytes)
+{
+    const size_t r = (size_t)(t + 2 * nh) * (t + 2 * nh), r1 = (size_t)(t + 2 * nh + 2) * (t + 2 * nh + 2);
+    return (9 * r + 4 * r1) * elem_bytes;
+}
+
+// Tile edge of kd_rb_adj_window for windows of nh half-sweeps: 32 or 16, the
+// largest whose shared memory fits; 0 when none does (the window then runs one
+// launch per half-sweep).
 int rb_adj_window_tile(int nh, int elem_bytes)
 {
-    for (int t : {32, 16}) {
-        const size_t bytes = (size_t)9 * (t + 2 * nh) * (t + 2 * nh) * elem_bytes;
-        if (bytes <= kAdjWindowSmem) return t;
-    }
+    for (int t : {32, 16})
+        if (adj_window_smem(t, nh, elem_bytes) <= kAdjWindowSmem) return t;
     return 0;
 }
 
@@ -1191,8 +1287,8 @@ cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long s
                           int F, int h, int w, int nh, int tile, double ax, double ay, double omega, double eps, int gs,
                           T* gcoef, double sx, double sy, double* galpha, cudaStream_t st)
 {
-    const size_t bytes = (size_t)9 * (tile + 2 * nh) * (tile + 2 * nh) * sizeof(T);
-    if (tile < 2 || (tile & 1) || bytes > kAdjWindowSmem) return cudaErrorInvalidValue;
+    const size_t bytes = adj_window_smem(tile, nh, (int)sizeof(T));
+    if ((tile != 16 && tile != 32) || nh < 1 || bytes > kAdjWindowSmem) return cudaErrorInvalidValue;
     const cudaError_t e = ensure_max_dyn_smem((const void*)kd_rb_adj_window<T>, (int)kAdjWindowSmem);
     if (e != cudaSuccess) return e;
     const dim3 grid((w + tile - 1) / tile, (h + tile - 1) / tile, F);
