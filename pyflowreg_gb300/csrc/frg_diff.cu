@@ -599,20 +599,20 @@ __global__ void kd_rb_adj_step(int color, const T* __restrict__ coef, StateSrc<T
         const T* cf = coef + f * 5 * hw + pc;
         const T A12 = cf[2 * hw], B1 = cf[3 * hw], B2 = cf[4 * hw];
         const T sw = ax + ax + ay + ay;
-        const T den_u = tmax(cf[0] + sw, eps), den_v = tmax(cf[hw] + sw, eps);
-        const T av = omega * lamv / den_v;
+        const T idu = (T)1 / tmax(cf[0] + sw, eps), idv = (T)1 / tmax(cf[hw] + sw, eps);
+        const T av = omega * lamv * idv;
         const T lue = gs ? lamu - A12 * av : lamu;
-        const T au = omega * lue / den_u;
+        const T au = omega * lue * idu;
         const int xl = hasL ? x - 1 : x, xr = hasR ? x + 1 : x, yt = hasT ? y - 1 : y, yb = hasB ? y + 1 : y;
         const T duc = sval(pre, f, 0, y, x, h, w, hw2), dvc = sval(pre, f, 1, y, x, h, w, hw2);
         const T Xdu = sval(pre, f, 0, y, xl, h, w, hw2) + sval(pre, f, 0, y, xr, h, w, hw2);
         const T Ydu = sval(pre, f, 0, yt, x, h, w, hw2) + sval(pre, f, 0, yb, x, h, w, hw2);
         const T Xdv = sval(pre, f, 1, y, xl, h, w, hw2) + sval(pre, f, 1, y, xr, h, w, hw2);
         const T Ydv = sval(pre, f, 1, yt, x, h, w, hw2) + sval(pre, f, 1, yb, x, h, w, hw2);
-        const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) / den_u;
+        const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) * idu;
         const T dun = ((T)1 - omega) * duc + omega * ru;
         const T du_for_v = gs ? dun : duc;
-        const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) / den_v;
+        const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) * idv;
         // border reflections of this pixel read its own du / dv
         const T self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
         lu[pc] = ((T)1 - omega) * lue + self * au - (gs ? (T)0 : A12 * av);
@@ -714,20 +714,20 @@ __device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, in
         lamv += sv;
     }
     const T A12 = sA12[li], B1 = sB1[li], B2 = sB2[li];
-    const T den_u = sDu[li], den_v = sDv[li];
-    const T av = omega * lamv / den_v;
+    const T idu = sDu[li], idv = sDv[li];
+    const T av = omega * lamv * idv;
     const T lue = gs ? lamu - A12 * av : lamu;
-    const T au = omega * lue / den_u;
+    const T au = omega * lue * idu;
     const T duc = own[sb], dvc = own[n1 + sb];
     const int sL = sb - 1 + p, sR = sb + p, sT = sb - Rp1, sB = sb + Rp1;
     const T Xdu = (hasL ? oth[sL] : duc) + (hasR ? oth[sR] : duc);
     const T Ydu = (hasT ? oth[sT] : duc) + (hasB ? oth[sB] : duc);
     const T Xdv = (hasL ? oth[n1 + sL] : dvc) + (hasR ? oth[n1 + sR] : dvc);
     const T Ydv = (hasT ? oth[n1 + sT] : dvc) + (hasB ? oth[n1 + sB] : dvc);
-    const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) / den_u;
+    const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) * idu;
     const T dun = ((T)1 - omega) * duc + omega * ru;
     const T du_for_v = gs ? dun : duc;
-    const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) / den_v;
+    const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) * idv;
     const T self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
     sLu[li] = ((T)1 - omega) * lue + self * au - (gs ? (T)0 : A12 * av);
     sLv[li] = ((T)1 - omega) * lamv - A12 * au + self * av;
@@ -759,9 +759,12 @@ __device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, in
 // lam of the tile after the window depends on the pixels within j + 1 of the
 // tile at half-sweep j, so step j (from nh - 1 down to 0) updates the moving
 // pixels of that shrinking region: the tile's own pixels and a halo that
-// neighbouring tiles also compute.  Thread t owns one horizontal pixel pair of
-// the tile (one pixel of each colour): the pair's coefficient gradients and
-// its alpha gradients stay in registers for the whole window.  The window ends
+// neighbouring tiles also compute.  They come from a table per colour in ring
+// order (AdjTable: the tile first, entry t the pixel of thread t's horizontal
+// pair, then the rings at distance 1, 2, ...), so a step's pixels are its
+// first cnt[c][j + 1] entries and the threads stay busy as the region shrinks.
+// Thread t keeps its pair's coefficient gradients and its alpha gradients in
+// registers for the whole window.  The denominators are held as reciprocals.  The window ends
 // with the closing gather of the tile's colour-1 pixels (kd_rb_adj_gather);
 // the tile's lam goes to lam_out, which is not lam_in (tiles read each other's
 // halo), and its coefficient gradients overwrite gcoef.
@@ -770,9 +773,9 @@ template <typename T>
 __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ coef, const T* __restrict__ s0,
                                                          const T* __restrict__ hist, long long slot,
                                                          const T* __restrict__ lam_in, T* __restrict__ lam_out, int h,
-                                                         int w, int nh, int TX, int TY, T ax, T ay, T omega, T eps,
-                                                         int gs, T* __restrict__ gcoef, double sx, double sy,
-                                                         double* __restrict__ galpha)
+                                                         int w, int nh, int TX, int TY, AdjTable tab, T ax, T ay,
+                                                         T omega, T eps, int gs, T* __restrict__ gcoef, double sx,
+                                                         double sy, double* __restrict__ galpha)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* const sm = reinterpret_cast<T*>(smraw);
@@ -817,8 +820,8 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
                 sA12[i] = cf[2 * hw + q];
                 sB1[i] = cf[3 * hw + q];
                 sB2[i] = cf[4 * hw + q];
-                sDu[i] = tmax(cf[q] + sw, eps);
-                sDv[i] = tmax(cf[hw + q] + sw, eps);
+                sDu[i] = (T)1 / tmax(cf[q] + sw, eps);
+                sDv[i] = (T)1 / tmax(cf[hw + q] + sw, eps);
                 sLu[i] = liu[q];
                 sLv[i] = liv[q];
             }
@@ -826,14 +829,12 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     }
     cp_async_wait_all();
     __syncthreads();
-    const int hp = TX >> 1;
-    const int oy = threadIdx.x / hp, ox = 2 * (threadIdx.x - oy * hp);
-    const int py = y0 + oy;
-    T g[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
+    T g0[5] = {0, 0, 0, 0, 0}, g1[5] = {0, 0, 0, 0, 0};  // the thread's colour-0 and colour-1 pixels
     T gax = 0, gay = 0;
     T dummy[5];
     T dax = 0, day = 0;
     const T tsx = (T)sx, tsy = (T)sy;
+    const int nin = (TX * TY) >> 1;  // entries 0 .. nin - 1 of a colour: the tile's own pixels, thread t's at t
     int cur[2] = {0, 0};
     for (int j = nh - 1; j >= 0; --j) {
         const int c = j & 1;
@@ -844,49 +845,39 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
             stage_colour<T>(buf(c ^ 1, cur[c ^ 1] ^ 1), c ^ 1, slice(j - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1,
                             inv_rp1);
         const bool gather = j < nh - 1;
-        {
-            const int px = x0 + ox + ((c - (x0 + ox + py)) & 1);
-            if (py < h && px < w) {
-                const int li = (py - ry0) * Rw + (px - rx0);
-                const int sb = (py - ry1) * Rp1 + ((px - rx1) >> 1);
-                const int pp = (px - rx1) & 1;
+        // the moving pixels within j + 1 of the tile: the first cnt entries of this colour's ring table
+        const int2* te = tab.e[c];
+        const int n_act = tab.cnt[c][j + 1];
+        for (int i = threadIdx.x; i < n_act; i += blockDim.x) {
+            const int2 e = te[i];
+            const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
+            if (gy >= h || gx >= w || gy < 0 || gx < 0) continue;
+            const int li = e.y & 0x1fff, sb = (e.y >> 13) & 0x1fff, pp = (e.y >> 26) & 1;
+            if (i < nin) {
                 if (c == 0)
-                    adj_window_px<T, true>(px, py, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
-                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[0], gax, gay, tsx, tsy);
+                    adj_window_px<T, true>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
+                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g0, gax, gay, tsx, tsy);
                 else
-                    adj_window_px<T, true>(px, py, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
-                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g[1], gax, gay, tsx, tsy);
+                    adj_window_px<T, true>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
+                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g1, gax, gay, tsx, tsy);
+            } else {
+                adj_window_px<T, false>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
+                                        sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
             }
-        }
-        const int d = j + 1;
-        const int Ap = (TX + 2 * d) >> 1, Ah = TY + 2 * d;
-        const int ax0 = x0 - d, ay0 = y0 - d;
-        const float inv_ap = 1.0f / (float)Ap;
-        for (int i = threadIdx.x; i < Ah * Ap; i += blockDim.x) {
-            const int r = (int)(((float)i + 0.5f) * inv_ap);
-            const int gy = ay0 + r;
-            int gx = ax0 + 2 * (i - r * Ap);
-            gx += (c - gx - gy) & 1;
-            if (gy < 0 || gy >= h || gx < 0 || gx >= w) continue;
-            if (gy >= y0 && gy < y0 + TY && gx >= x0 && gx < x0 + TX) continue;
-            const int li = (gy - ry0) * Rw + (gx - rx0);
-            const int sb = (gy - ry1) * Rp1 + ((gx - rx1) >> 1);
-            const int pp = (gx - rx1) & 1;
-            adj_window_px<T, false>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs, sA12,
-                                    sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
         }
         cp_async_wait_all();
         __syncthreads();
         cur[c ^ 1] ^= 1;
     }
     // the closing gather (colour 1), then the tile's lam and coefficient gradients
-    if (py < h) {
-        T* lou = lam_out + f * 2 * hw;
-        T* gc = gcoef + f * 5 * hw;
-        for (int c = 0; c < 2; ++c) {
-            const int px = x0 + ox + ((c - (x0 + ox + py)) & 1);
-            if (px >= w) continue;
-            const int li = (py - ry0) * Rw + (px - rx0);
+    T* lou = lam_out + f * 2 * hw;
+    T* gc = gcoef + f * 5 * hw;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const int2 e = tab.e[c][threadIdx.x];
+        const int px = x0 + (int)(short)(e.x & 0xffff), py = y0 + (e.x >> 16);
+        if (py < h && px < w) {
+            const int li = e.y & 0x1fff;
             T lu = sLu[li], lv = sLv[li];
             if (c == 1) {
                 T su = 0, sv = 0;
@@ -900,8 +891,9 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
             const long long q = (long long)py * w + px;
             lou[q] = lu;
             lou[hw + q] = lv;
+            const T* gg = c == 0 ? g0 : g1;
 #pragma unroll
-            for (int k = 0; k < 5; ++k) gc[k * hw + q] = g[c][k];
+            for (int k = 0; k < 5; ++k) gc[k * hw + q] = gg[k];
         }
     }
     block_add2(gax, gay, block_slot(galpha));
@@ -969,12 +961,15 @@ __global__ void kd_implicit_assemble(const T* __restrict__ lam, const T* __restr
 // the tick state through E into lam; the gradient of the level's input flow
 // through B1e, B2e into guv; that of ax, ay into galpha.  lagged = 1 holds psi
 // fixed (no derivative of psi with respect to the tick state or J33).
-template <typename T>
+template <typename T, int KT>
 __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, const T* __restrict__ st,
-                            const T* __restrict__ uv, const T* __restrict__ gcoef, int K, int h, int w, AData ad,
+                            const T* __restrict__ uv, const T* __restrict__ gcoef, int K_, int h, int w, AData ad,
                             T eps, T ax, T ay, int lagged, T* __restrict__ gJ, T* __restrict__ lam,
                             T* __restrict__ guv, double sx, double sy, double* __restrict__ galpha)
 {
+    // KT > 0: the channel count at compile time (psi and E stay in registers); 0: K_ at run time
+    constexpr int KA = KT > 0 ? KT : kMaxK;
+    const int K = KT > 0 ? KT : K_;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     const long long f = blockIdx.z, hw = (long long)h * w;
@@ -987,8 +982,9 @@ __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, co
         T* gJf = gJ + f * 6 * K * hw + pix;
         const long long qs = (long long)K * hw;
         // psi and the raw sums (for the max(., eps) clamps), as kd_tick computes them
-        T psi[kMaxK], Er[kMaxK];
+        T psi[KA], Er[KA];
         T A11 = 0, A22 = 0;
+#pragma unroll
         for (int k = 0; k < K; ++k) {
             const T* j = Jf + k * hw;
             Er[k] = j[0] * (du * du) + j[qs] * (dv * dv) + (T)2 * j[3 * qs] * (du * dv) + (T)2 * j[4 * qs] * du +
@@ -1006,6 +1002,7 @@ __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, co
         const T g22 = gc[hw + pix] * (A22 > eps ? (T)1 : (A22 == eps ? (T)0.5 : (T)0));
         const T g12 = gc[2 * hw + pix], gb1 = gc[3 * hw + pix], gb2 = gc[4 * hw + pix];
         T ldu = 0, ldv = 0;
+#pragma unroll
         for (int k = 0; k < K; ++k) {
             const T* j = Jf + k * hw;
             T* gj = gJf + k * hw;
@@ -1272,6 +1269,47 @@ size_t adj_window_smem(int t, int nh, int elem_bytes)
     return (9 * r + 4 * r1) * elem_bytes;
 }
 
+// The ring tables of kd_rb_adj_window for square tiles of edge t and windows
+// of nh half-sweeps, on the host: per colour c the offsets (dx, dy) from the
+// tile origin of the pixels of that colour within nh of the tile ((dx + dy)
+// & 1 == c: tile origins are even), the tile's own first (entry k: the pixel
+// of colour c of thread k's pair, row k / (t / 2), columns 2 (k % (t / 2)) and
+// one right), then ring by ring; cnt[c][d] = entries within distance d.
+// Entry: x = (dy << 16) | (dx & 0xffff); y = li | sb << 13 | p << 26 with li
+// the pixel in the planes over the tile grown by nh, sb its pair in the state
+// buffers over the tile grown by nh + 1 and p its column parity in the pair.
+bool build_adj_table(int t, int nh, std::vector<int2>& e0, std::vector<int2>& e1, int cnt[2][kAdjMaxNh + 1])
+{
+    if (nh < 1 || nh > kAdjMaxNh || (t & 1)) return false;
+    const int Rw = t + 2 * nh, Rp1 = (Rw + 2) / 2;
+    if (Rw * Rw >= (1 << 13) || (Rw + 2) * Rp1 >= (1 << 13)) return false;
+    auto enc = [&](int dx, int dy) {
+        const int li = (dy + nh) * Rw + (dx + nh);
+        const int sb = (dy + nh + 1) * Rp1 + ((dx + nh + 1) >> 1);
+        const int p = (dx + nh + 1) & 1;
+        return make_int2((int)(((unsigned)dy << 16) | ((unsigned)dx & 0xffffu)), li | (sb << 13) | (p << 26));
+    };
+    for (int c = 0; c < 2; ++c) {
+        std::vector<int2>& e = c == 0 ? e0 : e1;
+        e.clear();
+        for (int k = 0; k < t * t / 2; ++k) {
+            const int oy = k / (t / 2), ox = 2 * (k % (t / 2));
+            const int dx = ox + ((c - ox - oy) & 1);
+            e.push_back(enc(dx, oy));
+        }
+        cnt[c][0] = (int)e.size();
+        for (int d = 1; d <= nh; ++d) {
+            for (int dy = -d; dy < t + d; ++dy)
+                for (int dx = -d; dx < t + d; ++dx) {
+                    const int dist = std::max(std::max(-dx, dx - (t - 1)), std::max(-dy, dy - (t - 1)));
+                    if (dist == d && ((dx + dy) & 1) == c) e.push_back(enc(dx, dy));
+                }
+            cnt[c][d] = (int)e.size();
+        }
+    }
+    return true;
+}
+
 // Tile edge of kd_rb_adj_window for windows of nh half-sweeps: 32 or 16, the
 // largest whose shared memory fits; 0 when none does (the window then runs one
 // launch per half-sweep).
@@ -1284,8 +1322,9 @@ int rb_adj_window_tile(int nh, int elem_bytes)
 
 template <typename T>
 cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long slot, const T* lam_in, T* lam_out,
-                          int F, int h, int w, int nh, int tile, double ax, double ay, double omega, double eps, int gs,
-                          T* gcoef, double sx, double sy, double* galpha, cudaStream_t st)
+                          int F, int h, int w, int nh, int tile, const AdjTable& tab, double ax, double ay,
+                          double omega, double eps, int gs, T* gcoef, double sx, double sy, double* galpha,
+                          cudaStream_t st)
 {
     const size_t bytes = adj_window_smem(tile, nh, (int)sizeof(T));
     if ((tile != 16 && tile != 32) || nh < 1 || bytes > kAdjWindowSmem) return cudaErrorInvalidValue;
@@ -1293,8 +1332,8 @@ cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long s
     if (e != cudaSuccess) return e;
     const dim3 grid((w + tile - 1) / tile, (h + tile - 1) / tile, F);
     kd_rb_adj_window<T><<<grid, tile * tile / 2, bytes, st>>>(coef, s0, hist, slot, lam_in, lam_out, h, w, nh, tile,
-                                                             tile, (T)ax, (T)ay, (T)omega, (T)eps, gs, gcoef, sx, sy,
-                                                             galpha);
+                                                             tile, tab, (T)ax, (T)ay, (T)omega, (T)eps, gs, gcoef, sx,
+                                                             sy, galpha);
     return cudaGetLastError();
 }
 
@@ -1319,8 +1358,16 @@ cudaError_t tick_adj(const T* J, const T* W, const T* stt, const T* uv, const T*
 {
     AData ad;
     for (int k = 0; k < kMaxK; ++k) ad.a[k] = k < K ? a_data[k] : 0.0;
-    kd_tick_adj<T><<<grid_rows(w, h, F), 128, 0, st>>>(J, W, stt, uv, gcoef, K, h, w, ad, (T)eps, (T)ax, (T)ay,
-                                                       lagged, gJ, lam, guv, sx, sy, galpha);
+    const dim3 grid = grid_rows(w, h, F);
+    if (K == 1)
+        kd_tick_adj<T, 1><<<grid, 128, 0, st>>>(J, W, stt, uv, gcoef, K, h, w, ad, (T)eps, (T)ax, (T)ay, lagged, gJ,
+                                                lam, guv, sx, sy, galpha);
+    else if (K == 2)
+        kd_tick_adj<T, 2><<<grid, 128, 0, st>>>(J, W, stt, uv, gcoef, K, h, w, ad, (T)eps, (T)ax, (T)ay, lagged, gJ,
+                                                lam, guv, sx, sy, galpha);
+    else
+        kd_tick_adj<T, 0><<<grid, 128, 0, st>>>(J, W, stt, uv, gcoef, K, h, w, ad, (T)eps, (T)ax, (T)ay, lagged, gJ,
+                                                lam, guv, sx, sy, galpha);
     return cudaGetLastError();
 }
 
@@ -1362,8 +1409,8 @@ cudaError_t median_adj(const T* d, const T* g, int32_t* am, int F, int h, int w,
                                         cudaStream_t);                                                          \
     template cudaError_t rb_adj_gather<T>(int, T*, const T*, int, int, int, double, double, cudaStream_t);      \
     template cudaError_t rb_adj_window<T>(const T*, const T*, const T*, long long, const T*, T*, int, int, int, int,  \
-                                          int, double, double, double, double, int, T*, double, double, double*,     \
-                                          cudaStream_t);                                                              \
+                                          int, const AdjTable&, double, double, double, double, int, T*, double,     \
+                                          double, double*, cudaStream_t);                                             \
     template cudaError_t tick_adj<T>(const T*, const T*, const T*, const T*, const T*, int, int, int, int,       \
                                      const double*, double, double, double, int, T*, T*, T*, double, double,    \
                                      double*, cudaStream_t);                                                    \

@@ -132,6 +132,11 @@ struct frg_diff_plan {
     double* partA = nullptr; // per-block alpha partials of the half-sweep adjoints (F, H, ceil(ceil(W/2)/128), 2)
     double* partB = nullptr; // per-block alpha partials of the per-pixel adjoints (F, H, ceil(W/128), 2)
     double* partC = nullptr; // per-tile alpha partials of the tiled window adjoints (F, ceil(H/16), ceil(W/16), 2)
+    // tiled window adjoint: tile edge (0: stepwise only) and the ring tables of
+    // the full window and of a shorter last window
+    int adj_tile = 0;
+    int adj_nh[2] = {0, 0};
+    frg::diff::AdjTable adj_tab[2];
     void* gJ = nullptr;      // (F, 6, K, hw)
     void* G = nullptr;       // (F, K, 5, hw)
     void* gf1 = nullptr;     // (F, K, hw)
@@ -161,6 +166,42 @@ int dalloc_t(frg_diff_plan* pl, P** out, size_t count)
     int rc = dalloc(pl, &p, count * sizeof(P));
     *out = (P*)p;
     return rc;
+}
+
+// The tiled window adjoint's tile edge and ring tables, for the full tick
+// window and for a shorter last one (when iterations is not a multiple of
+// update_lag); none when the window does not fit (the backward then runs
+// stepwise).
+int make_adj_tables(frg_diff_plan* pl)
+{
+    const int nh_full = 2 * pl->win;
+    const int I = pl->p.iterations, lag = pl->p.update_lag;
+    const int nh_last = 2 * (I - (pl->n_ticks - 1) * lag);
+    const int tile = nh_full <= frg::diff::kAdjMaxNh ? frg::diff::rb_adj_window_tile(nh_full, (int)pl->es) : 0;
+    if (!tile) return FRG_OK;
+    const int nhs[2] = {nh_full, nh_last};
+    for (int q = 0; q < 2; ++q) {
+        if (q == 1 && nh_last == nh_full) {
+            pl->adj_nh[1] = nh_full;
+            pl->adj_tab[1] = pl->adj_tab[0];
+            break;
+        }
+        std::vector<int2> e0, e1;
+        frg::diff::AdjTable& tb = pl->adj_tab[q];
+        if (!frg::diff::build_adj_table(tile, nhs[q], e0, e1, tb.cnt)) return FRG_OK;
+        void* d = nullptr;
+        int rc = dalloc(pl, &d, (e0.size() + e1.size()) * sizeof(int2));
+        if (rc != FRG_OK) return rc;
+        cudaError_t e = cudaMemcpy(d, e0.data(), e0.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy((int2*)d + e0.size(), e1.data(), e1.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return host_fail(FRG_ECUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        tb.e[0] = (const int2*)d;
+        tb.e[1] = (const int2*)d + e0.size();
+        pl->adj_nh[q] = nhs[q];
+    }
+    pl->adj_tile = tile;
+    return FRG_OK;
 }
 
 // Uploads forward tables (ix/wx over out_w, iy/wy over out_h) and their inverses.
@@ -328,7 +369,7 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
         T* lam = (T*)pl->lam[0];
         T* s = (T*)pl->st;
         // tiled window adjoints (one launch per window) unless stepwise is asked for or a window does not fit
-        const int tile = stepwise ? 0 : rb_adj_window_tile(2 * pl->win, (int)es);
+        const int tile = stepwise ? 0 : pl->adj_tile;
         if (implicit) {
             // psi of the last tick, the level's final state, then one SOR solve of M lam = g
             const int k = pl->n_ticks - 1, start = k * lag, n_it = I - start;
@@ -386,7 +427,10 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
             if (tile) {
                 // the window's half-sweeps in one tiled launch, lam into the other buffer
                 T* lam_next = (T*)pl->lam[lam_i ^ 1];
-                DLAUNCH(1, rb_adj_window<T>(coef, s0, base, (long long)slot, lam, lam_next, F, h, w, n_half, tile,
+                const AdjTable& tb = n_half == pl->adj_nh[0] ? pl->adj_tab[0] : pl->adj_tab[1];
+                if (n_half != pl->adj_nh[0] && n_half != pl->adj_nh[1])
+                    return host_fail(FRG_EINVAL, "no ring table for this window");
+                DLAUNCH(1, rb_adj_window<T>(coef, s0, base, (long long)slot, lam, lam_next, F, h, w, n_half, tile, tb,
                                             L.ax, L.ay, om, kEps, pl->gs, gcoef, sx, sy, pl->partC, st));
                 lam_i ^= 1;
                 lam = lam_next;
@@ -549,6 +593,7 @@ int frg_diff_plan_create(const frg_params* params, int height, int width, int ch
          (rc = dalloc(pl, &pl->gout[0], F * 2 * hw * es)) || (rc = dalloc(pl, &pl->gout[1], F * 2 * hw * es)) ||
          (rc = dalloc_t(pl, &pl->am, F * 2 * hw))))
         ;
+    if (rc == FRG_OK) rc = make_adj_tables(pl);
     if (rc != FRG_OK) {
         frg_diff_plan_destroy(pl);
         return rc;

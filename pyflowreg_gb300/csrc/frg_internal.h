@@ -304,11 +304,20 @@ cudaError_t rb_adj_gather(int color, T* lam, const T* aprev, int F, int h, int w
 // summed by reduce_slots.  rb_adj_window_tile gives the tile edge for nh
 // half-sweeps and an element size, 0 when the window does not fit.
 constexpr size_t kAdjWindowSmem = 200 * 1024;
+constexpr int kAdjMaxNh = 40;  // half-sweeps per window the tiled adjoint takes (update_lag <= 20)
+// Ring tables of the tiled adjoint (device pointers per colour, counts per
+// distance), built on the host by build_adj_table.
+struct AdjTable {
+    const int2* e[2];
+    int cnt[2][kAdjMaxNh + 1];
+};
+bool build_adj_table(int tile, int nh, std::vector<int2>& e0, std::vector<int2>& e1, int cnt[2][kAdjMaxNh + 1]);
 int rb_adj_window_tile(int nh, int elem_bytes);
 template <typename T>
 cudaError_t rb_adj_window(const T* coef, const T* s0, const T* hist, long long slot, const T* lam_in, T* lam_out,
-                          int F, int h, int w, int nh, int tile, double ax, double ay, double omega, double eps, int gs,
-                          T* gcoef, double sx, double sy, double* galpha, cudaStream_t st);
+                          int F, int h, int w, int nh, int tile, const AdjTable& tab, double ax, double ay,
+                          double omega, double eps, int gs, T* gcoef, double sx, double sy, double* galpha,
+                          cudaStream_t st);
 template <typename T>
 cudaError_t tick_adj(const T* J, const T* W, const T* stt, const T* uv, const T* gcoef, int F, int K, int h, int w,
                      const double* a_data, double eps, double ax, double ay, int lagged, T* gJ, T* lam, T* guv,
