@@ -688,60 +688,84 @@ __device__ __forceinline__ void stage_colour(T* dst, int c, StateSlice<T> src, l
     cp_async_commit();
 }
 
-// One pixel's step of kd_rb_adj_window: the arithmetic of kd_rb_adj_step on
-// shared-memory planes.  li indexes the coefficient / lam / (au, av) planes
-// (row pitch Rw); sb the pixel in the staged states (row pitch Rp1, pair
-// column; p = the pixel's column parity within its pair): its own state in
-// `own`, its neighbours' (the other colour) in `oth`, planes n1 apart.  With
-// ACC the coefficient gradients go to g and the (sx, sy)-scaled alpha
-// gradients to (gax, gay).
-template <typename T, bool ACC>
-__device__ __forceinline__ void adj_window_px(int gx, int gy, int li, int Rw, int sb, int p, int Rp1, int n1,
-                                              bool gather, const T* own, const T* oth, int h, int w, T ax, T ay,
-                                              T omega, int gs, const T* sA12, const T* sB1, const T* sB2,
-                                              const T* sDu, const T* sDv, T* sLu, T* sLv, T* sAu, T* sAv,
-                                              T (&g)[5], T& gax, T& gay, T sx, T sy)
+// One pixel's step of kd_rb_adj_window, in three parts so that a thread can
+// load two pixels' inputs before it computes either: the arithmetic of
+// kd_rb_adj_step on shared-memory planes.  li indexes the coefficient / lam /
+// (au, av) planes (row pitch Rw); sb the pixel in the staged states (row pitch
+// Rp1, pair column; p = the pixel's column parity within its pair): its own
+// state in `own`, its neighbours' (the other colour) in `oth`, planes n1 apart.
+template <typename T>
+struct AdjPx {
+    T lamu, lamv, A12, B1, B2, idu, idv, duc, dvc, Xdu, Ydu, Xdv, Ydv, self;
+    int li;
+};
+
+template <typename T>
+struct AdjPlanes {
+    const T *A12, *B1, *B2, *iDu, *iDv;
+    T *Lu, *Lv, *Au, *Av;
+};
+
+template <typename T>
+__device__ __forceinline__ void adj_px_load(AdjPx<T>& q, int2 e, int x0, int y0, int h, int w, int Rw, int Rp1, int n1,
+                                            bool gather, const T* own, const T* oth, T ax, T ay, const AdjPlanes<T>& P)
 {
+    const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
+    const int li = e.y & 0x1fff, sb = (e.y >> 13) & 0x1fff, p = (e.y >> 26) & 1;
     const bool hasL = gx > 0, hasR = gx < w - 1, hasT = gy > 0, hasB = gy < h - 1;
-    T lamu = sLu[li], lamv = sLv[li];
+    q.li = li;
+    q.lamu = P.Lu[li];
+    q.lamv = P.Lv[li];
     if (gather) {
         T su = 0, sv = 0;
-        if (hasL) { su += ax * sAu[li - 1]; sv += ax * sAv[li - 1]; }
-        if (hasR) { su += ax * sAu[li + 1]; sv += ax * sAv[li + 1]; }
-        if (hasT) { su += ay * sAu[li - Rw]; sv += ay * sAv[li - Rw]; }
-        if (hasB) { su += ay * sAu[li + Rw]; sv += ay * sAv[li + Rw]; }
-        lamu += su;
-        lamv += sv;
+        if (hasL) { su += ax * P.Au[li - 1]; sv += ax * P.Av[li - 1]; }
+        if (hasR) { su += ax * P.Au[li + 1]; sv += ax * P.Av[li + 1]; }
+        if (hasT) { su += ay * P.Au[li - Rw]; sv += ay * P.Av[li - Rw]; }
+        if (hasB) { su += ay * P.Au[li + Rw]; sv += ay * P.Av[li + Rw]; }
+        q.lamu += su;
+        q.lamv += sv;
     }
-    const T A12 = sA12[li], B1 = sB1[li], B2 = sB2[li];
-    const T idu = sDu[li], idv = sDv[li];
-    const T av = omega * lamv * idv;
-    const T lue = gs ? lamu - A12 * av : lamu;
-    const T au = omega * lue * idu;
-    const T duc = own[sb], dvc = own[n1 + sb];
+    q.A12 = P.A12[li];
+    q.B1 = P.B1[li];
+    q.B2 = P.B2[li];
+    q.idu = P.iDu[li];
+    q.idv = P.iDv[li];
+    q.duc = own[sb];
+    q.dvc = own[n1 + sb];
     const int sL = sb - 1 + p, sR = sb + p, sT = sb - Rp1, sB = sb + Rp1;
-    const T Xdu = (hasL ? oth[sL] : duc) + (hasR ? oth[sR] : duc);
-    const T Ydu = (hasT ? oth[sT] : duc) + (hasB ? oth[sB] : duc);
-    const T Xdv = (hasL ? oth[n1 + sL] : dvc) + (hasR ? oth[n1 + sR] : dvc);
-    const T Ydv = (hasT ? oth[n1 + sT] : dvc) + (hasB ? oth[n1 + sB] : dvc);
-    const T ru = (-(B1 + A12 * dvc) + ax * Xdu + ay * Ydu) * idu;
-    const T dun = ((T)1 - omega) * duc + omega * ru;
-    const T du_for_v = gs ? dun : duc;
-    const T rv = (-(B2 + A12 * du_for_v) + ax * Xdv + ay * Ydv) * idv;
-    const T self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
-    sLu[li] = ((T)1 - omega) * lue + self * au - (gs ? (T)0 : A12 * av);
-    sLv[li] = ((T)1 - omega) * lamv - A12 * au + self * av;
-    sAu[li] = au;
-    sAv[li] = av;
+    q.Xdu = (hasL ? oth[sL] : q.duc) + (hasR ? oth[sR] : q.duc);
+    q.Ydu = (hasT ? oth[sT] : q.duc) + (hasB ? oth[sB] : q.duc);
+    q.Xdv = (hasL ? oth[n1 + sL] : q.dvc) + (hasR ? oth[n1 + sR] : q.dvc);
+    q.Ydv = (hasT ? oth[n1 + sT] : q.dvc) + (hasB ? oth[n1 + sB] : q.dvc);
+    q.self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
+}
+
+// The step itself; with ACC the coefficient gradients go to g and the
+// (sx, sy)-scaled alpha gradients to (gax, gay).  Writes lam and (au, av).
+template <typename T, bool ACC>
+__device__ __forceinline__ void adj_px_step(const AdjPx<T>& q, T ax, T ay, T omega, int gs, const AdjPlanes<T>& P,
+                                            T (&g)[5], T& gax, T& gay, T sx, T sy)
+{
+    const T av = omega * q.lamv * q.idv;
+    const T lue = gs ? q.lamu - q.A12 * av : q.lamu;
+    const T au = omega * lue * q.idu;
+    const T ru = (-(q.B1 + q.A12 * q.dvc) + ax * q.Xdu + ay * q.Ydu) * q.idu;
+    const T dun = ((T)1 - omega) * q.duc + omega * ru;
+    const T du_for_v = gs ? dun : q.duc;
+    const T rv = (-(q.B2 + q.A12 * du_for_v) + ax * q.Xdv + ay * q.Ydv) * q.idv;
+    P.Lu[q.li] = ((T)1 - omega) * lue + q.self * au - (gs ? (T)0 : q.A12 * av);
+    P.Lv[q.li] = ((T)1 - omega) * q.lamv - q.A12 * au + q.self * av;
+    P.Au[q.li] = au;
+    P.Av[q.li] = av;
     if (ACC) {
         g[0] -= au * ru;
         g[1] -= av * rv;
-        g[2] -= au * dvc + av * du_for_v;
+        g[2] -= au * q.dvc + av * du_for_v;
         g[3] -= au;
         g[4] -= av;
         const T rr = (T)2 * (au * ru + av * rv);
-        gax += (au * Xdu + av * Xdv - rr) * sx;
-        gay += (au * Ydu + av * Ydv - rr) * sy;
+        gax += (au * q.Xdu + av * q.Xdv - rr) * sx;
+        gay += (au * q.Ydu + av * q.Ydv - rr) * sy;
     }
 }
 
@@ -791,6 +815,12 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     T* const sAu = sm + 7 * R;
     T* const sAv = sm + 8 * R;
     T* const sS = sm + 9 * R;  // state buffers: (colour * 2 + buffer) * 2 * n1
+    // the ring tables of both colours, after the state buffers (8-byte aligned: R, n1 counts of T)
+    int2* const sTab = reinterpret_cast<int2*>(sS + 8 * n1);
+    const int nt0 = tab.cnt[0][nh], nt1 = tab.cnt[1][nh];
+    for (int i = threadIdx.x; i < nt0; i += blockDim.x) sTab[i] = tab.e[0][i];
+    for (int i = threadIdx.x; i < nt1; i += blockDim.x) sTab[nt0 + i] = tab.e[1][i];
+    const AdjPlanes<T> PL{sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv};
     const long long f = blockIdx.z, hw = (long long)h * w;
     const int hw2 = (w + 1) >> 1;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
@@ -845,25 +875,36 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
             stage_colour<T>(buf(c ^ 1, cur[c ^ 1] ^ 1), c ^ 1, slice(j - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1,
                             inv_rp1);
         const bool gather = j < nh - 1;
-        // the moving pixels within j + 1 of the tile: the first cnt entries of this colour's ring table
-        const int2* te = tab.e[c];
+        // the moving pixels within j + 1 of the tile: the first cnt entries of this colour's ring table;
+        // entry t is this thread's own tile pixel, the others (halo) come two at a time, both loaded
+        // before either is computed (pixels of one colour do not read each other)
+        const int2* te = sTab + (c ? nt0 : 0);
         const int n_act = tab.cnt[c][j + 1];
-        for (int i = threadIdx.x; i < n_act; i += blockDim.x) {
-            const int2 e = te[i];
+        const int bd = blockDim.x;
+        auto inside = [&](int2 e) {
             const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
-            if (gy >= h || gx >= w || gy < 0 || gx < 0) continue;
-            const int li = e.y & 0x1fff, sb = (e.y >> 13) & 0x1fff, pp = (e.y >> 26) & 1;
-            if (i < nin) {
+            return gx >= 0 && gy >= 0 && gx < w && gy < h;
+        };
+        {
+            const int2 e = te[threadIdx.x];
+            if (inside(e)) {
+                AdjPx<T> q;
+                adj_px_load<T>(q, e, x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
                 if (c == 0)
-                    adj_window_px<T, true>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
-                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g0, gax, gay, tsx, tsy);
+                    adj_px_step<T, true>(q, ax, ay, omega, gs, PL, g0, gax, gay, tsx, tsy);
                 else
-                    adj_window_px<T, true>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
-                                           sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, g1, gax, gay, tsx, tsy);
-            } else {
-                adj_window_px<T, false>(gx, gy, li, Rw, sb, pp, Rp1, n1, gather, own, oth, h, w, ax, ay, omega, gs,
-                                        sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv, dummy, dax, day, tsx, tsy);
+                    adj_px_step<T, true>(q, ax, ay, omega, gs, PL, g1, gax, gay, tsx, tsy);
             }
+        }
+        for (int i = nin + threadIdx.x; i < n_act; i += 2 * bd) {
+            const int2 ea = te[i];
+            const bool ha = inside(ea);
+            const bool hb = i + bd < n_act && inside(te[i + bd]);
+            AdjPx<T> qa, qb;
+            if (ha) adj_px_load<T>(qa, ea, x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
+            if (hb) adj_px_load<T>(qb, te[i + bd], x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
+            if (ha) adj_px_step<T, false>(qa, ax, ay, omega, gs, PL, dummy, dax, day, tsx, tsy);
+            if (hb) adj_px_step<T, false>(qb, ax, ay, omega, gs, PL, dummy, dax, day, tsx, tsy);
         }
         cp_async_wait_all();
         __syncthreads();
@@ -874,7 +915,7 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     T* gc = gcoef + f * 5 * hw;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-        const int2 e = tab.e[c][threadIdx.x];
+        const int2 e = sTab[(c ? nt0 : 0) + threadIdx.x];
         const int px = x0 + (int)(short)(e.x & 0xffff), py = y0 + (e.x >> 16);
         if (py < h && px < w) {
             const int li = e.y & 0x1fff;
@@ -1262,11 +1303,12 @@ cudaError_t rb_adj_step(int color, const T* coef, const T* pre_full, const T* pr
 
 // Shared memory of kd_rb_adj_window for square tiles of edge t and windows of
 // nh half-sweeps: 9 planes over the tile grown by nh, 4 state planes (2 per
-// colour buffer pair, half a plane each) over the tile grown by nh + 1.
+// colour buffer pair, half a plane each) over the tile grown by nh + 1, and
+// the two colours' ring tables (one int2 per pixel of the tile grown by nh).
 size_t adj_window_smem(int t, int nh, int elem_bytes)
 {
     const size_t r = (size_t)(t + 2 * nh) * (t + 2 * nh), r1 = (size_t)(t + 2 * nh + 2) * (t + 2 * nh + 2);
-    return (9 * r + 4 * r1) * elem_bytes;
+    return (9 * r + 4 * r1) * elem_bytes + r * sizeof(int2);  // planes, state buffers, ring tables
 }
 
 // The ring tables of kd_rb_adj_window for square tiles of edge t and windows

@@ -75,6 +75,7 @@ struct DLevel {
     void* ck_ticks = nullptr;  // (n_ticks - 1, F, 2, h, w)
     void* ck_sweeps = nullptr; // FRG_DIFF_STORE_SWEEPS: (2 * iterations, F, 2, h, (w + 1) / 2)
     void* ck_final = nullptr;  // FRG_DIFF_STORE_SWEEPS: (F, 2, h, w), the level's final du, dv
+    void* ck_coef = nullptr;   // FRG_DIFF_STORE_SWEEPS: (n_ticks, F, 5, h, w), each tick window's coefficients
     double ax = 0, ay = 0;     // smoothness weights of the last forward
 };
 
@@ -301,6 +302,8 @@ int run_forward(frg_diff_plan* pl, int F, const T* fixed, const T* moving, const
             if (it % lag == 0) {
                 const int k = it / lag;
                 T* ck = k > 0 ? (T*)L.ck_ticks + (size_t)(k - 1) * F * 2 * hw : nullptr;
+                // with stored sweeps each window's coefficients are kept too (the backward reads them)
+                coef = pl->store_sweeps ? (T*)L.ck_coef + (size_t)k * F * 5 * hw : (T*)pl->coef;
                 DLAUNCH(1, tick<T>(J, (const T*)L.Wl, k > 0 ? s : (const T*)nullptr, uv, F, K, h, w, pl->a_data, kEps,
                                    L.ax, L.ay, coef, ck, st));
             }
@@ -402,7 +405,10 @@ int run_backward(frg_diff_plan* pl, const T* g_flow, T* g_fixed, T* g_moving, do
         for (int k = implicit ? -1 : pl->n_ticks - 1; k >= 0; --k) {
             const int start = k * lag, n_it = std::min(lag, I - start), n_half = 2 * n_it;
             const T* s0 = k > 0 ? (const T*)L.ck_ticks + (size_t)(k - 1) * plane2 : nullptr;
-            DLAUNCH(1, tick<T>(J, Wl, s0, uv, F, K, h, w, pl->a_data, kEps, L.ax, L.ay, coef, (T*)nullptr, st));
+            if (pl->store_sweeps)
+                coef = (T*)L.ck_coef + (size_t)k * F * 5 * hw;  // kept by the forward
+            else
+                DLAUNCH(1, tick<T>(J, Wl, s0, uv, F, K, h, w, pl->a_data, kEps, L.ax, L.ay, coef, (T*)nullptr, st));
             // the moved pixels of half-sweep j of this window
             T* base;
             if (pl->store_sweeps) {
@@ -566,7 +572,8 @@ int frg_diff_plan_create(const frg_params* params, int height, int width, int ch
             break;
         if (pl->store_sweeps &&
             ((rc = dalloc(pl, &L.ck_sweeps, (size_t)2 * I * F * 2 * L.h * ((L.w + 1) / 2) * es)) ||
-             (rc = dalloc(pl, &L.ck_final, F * 2 * hw * es))))
+             (rc = dalloc(pl, &L.ck_final, F * 2 * hw * es)) ||
+             (rc = dalloc(pl, &L.ck_coef, (size_t)pl->n_ticks * F * 5 * hw * es))))
             break;
         ph = L.h;
         pw = L.w;
