@@ -647,6 +647,18 @@ __device__ __forceinline__ void cp_async_el(T* dst, const T* src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Two-element vector of T (float2 / double2) for the paired shared-memory planes.
+template <typename T>
+struct Vec2T;
+template <>
+struct Vec2T<float> {
+    using type = float2;
+};
+template <>
+struct Vec2T<double> {
+    using type = double2;
+};
+
 // Solver state of one colour before a half-sweep, as kd_rb_adj_window stages
 // it: kind 0 zero, 1 a full array (F, 2, h, w), 2 a compressed array of that
 // colour's pixels (F, 2, h, (w + 1) / 2).
@@ -658,12 +670,12 @@ struct StateSlice {
 
 // Copies colour c of a state slice over the window's outer region (origin
 // (rx1, ry1), Rh1 rows of Rp1 pixel pairs; pair k of a row holds columns
-// rx1 + 2k and rx1 + 2k + 1, one of each colour) into dst: plane u at dst,
-// plane v at dst + Rh1 * Rp1, entry row * Rp1 + k.  Pixels outside the level
-// are left alone (never read).  Issues cp.async copies and commits them.
+// rx1 + 2k and rx1 + 2k + 1, one of each colour) into dst, one (du, dv) pair
+// per entry row * Rp1 + k.  Pixels outside the level are left alone (never
+// read).  Issues cp.async copies and commits them.
 template <typename T>
-__device__ __forceinline__ void stage_colour(T* dst, int c, StateSlice<T> src, long long f, int h, int w, int hw2,
-                                             int rx1, int ry1, int Rh1, int Rp1, float inv_rp1)
+__device__ __forceinline__ void stage_colour(typename Vec2T<T>::type* dst, int c, StateSlice<T> src, long long f,
+                                             int h, int w, int hw2, int rx1, int ry1, int Rh1, int Rp1, float inv_rp1)
 {
     const int n = Rh1 * Rp1;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -672,72 +684,85 @@ __device__ __forceinline__ void stage_colour(T* dst, int c, StateSlice<T> src, l
         const int gy = ry1 + row;
         const int gx = rx1 + 2 * k + ((c - rx1 - gy) & 1);
         if (gy < 0 || gy >= h || gx < 0 || gx >= w) continue;
+        T* d = reinterpret_cast<T*>(dst + i);
         if (src.kind == 0) {
-            dst[i] = (T)0;
-            dst[n + i] = (T)0;
+            d[0] = (T)0;
+            d[1] = (T)0;
         } else if (src.kind == 1) {
             const T* q = src.p + ((f * 2) * h + gy) * (long long)w + gx;
-            cp_async_el(dst + i, q);
-            cp_async_el(dst + n + i, q + (long long)h * w);
+            cp_async_el(d, q);
+            cp_async_el(d + 1, q + (long long)h * w);
         } else {
             const T* q = src.p + ((f * 2) * h + gy) * (long long)hw2 + (gx >> 1);
-            cp_async_el(dst + i, q);
-            cp_async_el(dst + n + i, q + (long long)h * hw2);
+            cp_async_el(d, q);
+            cp_async_el(d + 1, q + (long long)h * hw2);
         }
     }
     cp_async_commit();
 }
 
-// One pixel's step of kd_rb_adj_window, in three parts so that a thread can
-// load two pixels' inputs before it computes either: the arithmetic of
-// kd_rb_adj_step on shared-memory planes.  li indexes the coefficient / lam /
-// (au, av) planes (row pitch Rw); sb the pixel in the staged states (row pitch
-// Rp1, pair column; p = the pixel's column parity within its pair): its own
-// state in `own`, its neighbours' (the other colour) in `oth`, planes n1 apart.
+// Shared-memory planes of kd_rb_adj_window over the tile grown by nh: C0 =
+// (A12, B1e), C1 = (B2e, 1 / den_u), C2 = 1 / den_v, L = lam, A = the latest
+// (au, av).
+template <typename T>
+struct AdjPlanes {
+    typename Vec2T<T>::type *C0, *C1, *L, *A;
+    T* C2;
+};
+
+// One pixel's step of kd_rb_adj_window: the arithmetic of kd_rb_adj_step on
+// the shared-memory planes.  Entry e of a ring table gives li (the pixel in
+// the planes, row pitch Rw), sb (its pair in the staged states, row pitch Rp1)
+// and p (its column parity in the pair): its own state is in `own`, its
+// neighbours' (the other colour) in `oth`.  EDGE: the tile's outer region
+// reaches the level's border, so neighbours may be missing (the pixel's own
+// value stands in for them, as the border copies of the reference do);
+// without EDGE every neighbour exists.  In two parts, load and step, so that
+// a thread can load two pixels before it computes either.
 template <typename T>
 struct AdjPx {
-    T lamu, lamv, A12, B1, B2, idu, idv, duc, dvc, Xdu, Ydu, Xdv, Ydv, self;
+    typename Vec2T<T>::type lam, c0, c1, st;
+    T idv, Xdu, Ydu, Xdv, Ydv, self;
     int li;
 };
 
-template <typename T>
-struct AdjPlanes {
-    const T *A12, *B1, *B2, *iDu, *iDv;
-    T *Lu, *Lv, *Au, *Av;
-};
-
-template <typename T>
-__device__ __forceinline__ void adj_px_load(AdjPx<T>& q, int2 e, int x0, int y0, int h, int w, int Rw, int Rp1, int n1,
-                                            bool gather, const T* own, const T* oth, T ax, T ay, const AdjPlanes<T>& P)
+template <typename T, bool EDGE>
+__device__ __forceinline__ void adj_px_load(AdjPx<T>& q, int2 e, int x0, int y0, int h, int w, int Rw, int Rp1,
+                                            bool gather, const typename Vec2T<T>::type* own,
+                                            const typename Vec2T<T>::type* oth, T ax, T ay, const AdjPlanes<T>& P)
 {
-    const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
+    using V2 = typename Vec2T<T>::type;
     const int li = e.y & 0x1fff, sb = (e.y >> 13) & 0x1fff, p = (e.y >> 26) & 1;
-    const bool hasL = gx > 0, hasR = gx < w - 1, hasT = gy > 0, hasB = gy < h - 1;
+    bool hasL = true, hasR = true, hasT = true, hasB = true;
+    if (EDGE) {
+        const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
+        hasL = gx > 0;
+        hasR = gx < w - 1;
+        hasT = gy > 0;
+        hasB = gy < h - 1;
+    }
     q.li = li;
-    q.lamu = P.Lu[li];
-    q.lamv = P.Lv[li];
+    q.lam = P.L[li];
     if (gather) {
         T su = 0, sv = 0;
-        if (hasL) { su += ax * P.Au[li - 1]; sv += ax * P.Av[li - 1]; }
-        if (hasR) { su += ax * P.Au[li + 1]; sv += ax * P.Av[li + 1]; }
-        if (hasT) { su += ay * P.Au[li - Rw]; sv += ay * P.Av[li - Rw]; }
-        if (hasB) { su += ay * P.Au[li + Rw]; sv += ay * P.Av[li + Rw]; }
-        q.lamu += su;
-        q.lamv += sv;
+        if (hasL) { const V2 a = P.A[li - 1]; su += ax * a.x; sv += ax * a.y; }
+        if (hasR) { const V2 a = P.A[li + 1]; su += ax * a.x; sv += ax * a.y; }
+        if (hasT) { const V2 a = P.A[li - Rw]; su += ay * a.x; sv += ay * a.y; }
+        if (hasB) { const V2 a = P.A[li + Rw]; su += ay * a.x; sv += ay * a.y; }
+        q.lam.x += su;
+        q.lam.y += sv;
     }
-    q.A12 = P.A12[li];
-    q.B1 = P.B1[li];
-    q.B2 = P.B2[li];
-    q.idu = P.iDu[li];
-    q.idv = P.iDv[li];
-    q.duc = own[sb];
-    q.dvc = own[n1 + sb];
-    const int sL = sb - 1 + p, sR = sb + p, sT = sb - Rp1, sB = sb + Rp1;
-    q.Xdu = (hasL ? oth[sL] : q.duc) + (hasR ? oth[sR] : q.duc);
-    q.Ydu = (hasT ? oth[sT] : q.duc) + (hasB ? oth[sB] : q.duc);
-    q.Xdv = (hasL ? oth[n1 + sL] : q.dvc) + (hasR ? oth[n1 + sR] : q.dvc);
-    q.Ydv = (hasT ? oth[n1 + sT] : q.dvc) + (hasB ? oth[n1 + sB] : q.dvc);
-    q.self = ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1));
+    q.c0 = P.C0[li];
+    q.c1 = P.C1[li];
+    q.idv = P.C2[li];
+    q.st = own[sb];
+    const V2 sl = hasL ? oth[sb - 1 + p] : q.st, sr = hasR ? oth[sb + p] : q.st;
+    const V2 st_ = hasT ? oth[sb - Rp1] : q.st, sbm = hasB ? oth[sb + Rp1] : q.st;
+    q.Xdu = sl.x + sr.x;
+    q.Ydu = st_.x + sbm.x;
+    q.Xdv = sl.y + sr.y;
+    q.Ydv = st_.y + sbm.y;
+    q.self = EDGE ? ax * (T)((hasL ? 0 : 1) + (hasR ? 0 : 1)) + ay * (T)((hasT ? 0 : 1) + (hasB ? 0 : 1)) : (T)0;
 }
 
 // The step itself; with ACC the coefficient gradients go to g and the
@@ -746,21 +771,28 @@ template <typename T, bool ACC>
 __device__ __forceinline__ void adj_px_step(const AdjPx<T>& q, T ax, T ay, T omega, int gs, const AdjPlanes<T>& P,
                                             T (&g)[5], T& gax, T& gay, T sx, T sy)
 {
-    const T av = omega * q.lamv * q.idv;
-    const T lue = gs ? q.lamu - q.A12 * av : q.lamu;
-    const T au = omega * lue * q.idu;
-    const T ru = (-(q.B1 + q.A12 * q.dvc) + ax * q.Xdu + ay * q.Ydu) * q.idu;
-    const T dun = ((T)1 - omega) * q.duc + omega * ru;
-    const T du_for_v = gs ? dun : q.duc;
-    const T rv = (-(q.B2 + q.A12 * du_for_v) + ax * q.Xdv + ay * q.Ydv) * q.idv;
-    P.Lu[q.li] = ((T)1 - omega) * lue + q.self * au - (gs ? (T)0 : q.A12 * av);
-    P.Lv[q.li] = ((T)1 - omega) * q.lamv - q.A12 * au + q.self * av;
-    P.Au[q.li] = au;
-    P.Av[q.li] = av;
+    using V2 = typename Vec2T<T>::type;
+    const T A12 = q.c0.x, B1 = q.c0.y, B2 = q.c1.x, idu = q.c1.y, idv = q.idv;
+    const T duc = q.st.x, dvc = q.st.y;
+    const T av = omega * q.lam.y * idv;
+    const T lue = gs ? q.lam.x - A12 * av : q.lam.x;
+    const T au = omega * lue * idu;
+    const T ru = (-(B1 + A12 * dvc) + ax * q.Xdu + ay * q.Ydu) * idu;
+    const T dun = ((T)1 - omega) * duc + omega * ru;
+    const T du_for_v = gs ? dun : duc;
+    const T rv = (-(B2 + A12 * du_for_v) + ax * q.Xdv + ay * q.Ydv) * idv;
+    V2 nl;
+    nl.x = ((T)1 - omega) * lue + q.self * au - (gs ? (T)0 : A12 * av);
+    nl.y = ((T)1 - omega) * q.lam.y - A12 * au + q.self * av;
+    P.L[q.li] = nl;
+    V2 na;
+    na.x = au;
+    na.y = av;
+    P.A[q.li] = na;
     if (ACC) {
         g[0] -= au * ru;
         g[1] -= av * rv;
-        g[2] -= au * q.dvc + av * du_for_v;
+        g[2] -= au * dvc + av * du_for_v;
         g[3] -= au;
         g[4] -= av;
         const T rr = (T)2 * (au * ru + av * rv);
@@ -769,107 +801,29 @@ __device__ __forceinline__ void adj_px_step(const AdjPx<T>& q, T ax, T ay, T ome
     }
 }
 
-// Adjoint of all nh half-sweeps of one tick window in one launch (temporal
-// blocking), with kd_rb_adj_step's arithmetic.  A CTA owns a TX x TY tile of
-// one frame (TX = TY = 16 or 32) and keeps in shared memory:
-//  * over the tile grown by nh pixels on every side (Rw x Rh): A12, B1e, B2e,
-//    the two clamped denominators, lam and the pixel's latest (au, av);
-//  * over the tile grown by nh + 1 (Rh1 rows of Rp1 pixel pairs), per colour
-//    two buffers of the solver state before a half-sweep, filled by cp.async
-//    from the window's stored half-sweeps (hist + j * slot, compressed; s0,
-//    NULL: zero, before the first) one step ahead: before half-sweep j the
-//    moving colour holds its values after j - 2 and the other colour after
-//    j - 1, so each step replaces one colour.
-// lam of the tile after the window depends on the pixels within j + 1 of the
-// tile at half-sweep j, so step j (from nh - 1 down to 0) updates the moving
-// pixels of that shrinking region: the tile's own pixels and a halo that
-// neighbouring tiles also compute.  They come from a table per colour in ring
-// order (AdjTable: the tile first, entry t the pixel of thread t's horizontal
-// pair, then the rings at distance 1, 2, ...), so a step's pixels are its
-// first cnt[c][j + 1] entries and the threads stay busy as the region shrinks.
-// Thread t keeps its pair's coefficient gradients and its alpha gradients in
-// registers for the whole window.  The denominators are held as reciprocals.  The window ends
-// with the closing gather of the tile's colour-1 pixels (kd_rb_adj_gather);
-// the tile's lam goes to lam_out, which is not lam_in (tiles read each other's
-// halo), and its coefficient gradients overwrite gcoef.
-// blockDim.x = TX * TY / 2.
-template <typename T>
-__global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ coef, const T* __restrict__ s0,
-                                                         const T* __restrict__ hist, long long slot,
-                                                         const T* __restrict__ lam_in, T* __restrict__ lam_out, int h,
-                                                         int w, int nh, int TX, int TY, AdjTable tab, T ax, T ay,
-                                                         T omega, T eps, int gs, T* __restrict__ gcoef, double sx,
-                                                         double sy, double* __restrict__ galpha)
+// The steps of one window, from half-sweep nh - 1 down to 0 (see
+// kd_rb_adj_window).
+template <typename T, bool EDGE>
+__device__ __forceinline__ void adj_window_steps(int nh, int x0, int y0, int h, int w, int Rw, int Rp1, int n1,
+                                                 int nin, const int2* sTab, int nt0, const AdjTable& tab,
+                                                 typename Vec2T<T>::type* sS, const T* s0, const T* hist, long long slot, long long f, int hw2,
+                                                 int rx1, int ry1, int Rh1, float inv_rp1, T ax, T ay, T omega,
+                                                 int gs, const AdjPlanes<T>& PL, T (&g0)[5], T (&g1)[5], T& gax,
+                                                 T& gay, T tsx, T tsy)
 {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T* const sm = reinterpret_cast<T*>(smraw);
-    const int Rw = TX + 2 * nh, Rh = TY + 2 * nh, R = Rw * Rh;
-    const int Rp1 = (Rw + 2) >> 1, Rh1 = Rh + 2, n1 = Rh1 * Rp1;
-    T* const sA12 = sm;
-    T* const sB1 = sm + R;
-    T* const sB2 = sm + 2 * R;
-    T* const sDu = sm + 3 * R;
-    T* const sDv = sm + 4 * R;
-    T* const sLu = sm + 5 * R;
-    T* const sLv = sm + 6 * R;
-    T* const sAu = sm + 7 * R;
-    T* const sAv = sm + 8 * R;
-    T* const sS = sm + 9 * R;  // state buffers: (colour * 2 + buffer) * 2 * n1
-    // the ring tables of both colours, after the state buffers (8-byte aligned: R, n1 counts of T)
-    int2* const sTab = reinterpret_cast<int2*>(sS + 8 * n1);
-    const int nt0 = tab.cnt[0][nh], nt1 = tab.cnt[1][nh];
-    for (int i = threadIdx.x; i < nt0; i += blockDim.x) sTab[i] = tab.e[0][i];
-    for (int i = threadIdx.x; i < nt1; i += blockDim.x) sTab[nt0 + i] = tab.e[1][i];
-    const AdjPlanes<T> PL{sA12, sB1, sB2, sDu, sDv, sLu, sLv, sAu, sAv};
-    const long long f = blockIdx.z, hw = (long long)h * w;
-    const int hw2 = (w + 1) >> 1;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int rx0 = x0 - nh, ry0 = y0 - nh;
-    const int rx1 = rx0 - 1, ry1 = ry0 - 1;
-    const float inv_rp1 = 1.0f / (float)Rp1;
+    using V2 = typename Vec2T<T>::type;
+    T dummy[5];
+    T dax = 0, day = 0;
     auto slice = [&](int k) -> StateSlice<T> {
         if (k >= 0) return StateSlice<T>{hist + (long long)k * slot, 2};
         return StateSlice<T>{s0, s0 ? 1 : 0};
     };
-    auto buf = [&](int c, int b) { return sS + (c * 2 + b) * 2 * n1; };
-    // the states before the window's last half-sweep nh - 1 (colour 1): colour 1
-    // after nh - 3, colour 0 after nh - 2
-    stage_colour<T>(buf(1, 0), 1, slice(nh - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
-    stage_colour<T>(buf(0, 0), 0, slice(nh - 2), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
-    {
-        const T* cf = coef + f * 5 * hw;
-        const T* liu = lam_in + f * 2 * hw;
-        const T* liv = liu + hw;
-        const T sw = ax + ax + ay + ay;
-        const float inv_rw = 1.0f / (float)Rw;
-        for (int i = threadIdx.x; i < R; i += blockDim.x) {
-            const int ry = (int)(((float)i + 0.5f) * inv_rw);
-            const int gy = ry0 + ry, gx = rx0 + (i - ry * Rw);
-            if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
-                const long long q = (long long)gy * w + gx;
-                sA12[i] = cf[2 * hw + q];
-                sB1[i] = cf[3 * hw + q];
-                sB2[i] = cf[4 * hw + q];
-                sDu[i] = (T)1 / tmax(cf[q] + sw, eps);
-                sDv[i] = (T)1 / tmax(cf[hw + q] + sw, eps);
-                sLu[i] = liu[q];
-                sLv[i] = liv[q];
-            }
-        }
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    T g0[5] = {0, 0, 0, 0, 0}, g1[5] = {0, 0, 0, 0, 0};  // the thread's colour-0 and colour-1 pixels
-    T gax = 0, gay = 0;
-    T dummy[5];
-    T dax = 0, day = 0;
-    const T tsx = (T)sx, tsy = (T)sy;
-    const int nin = (TX * TY) >> 1;  // entries 0 .. nin - 1 of a colour: the tile's own pixels, thread t's at t
+    auto buf = [&](int c, int b) { return sS + (c * 2 + b) * n1; };
     int cur[2] = {0, 0};
     for (int j = nh - 1; j >= 0; --j) {
         const int c = j & 1;
-        const T* own = buf(c, cur[c]);
-        const T* oth = buf(c ^ 1, cur[c ^ 1]);
+        const V2* own = buf(c, cur[c]);
+        const V2* oth = buf(c ^ 1, cur[c ^ 1]);
         // the other colour's state for step j - 1 (its values after j - 3), one step ahead
         if (j >= 1)
             stage_colour<T>(buf(c ^ 1, cur[c ^ 1] ^ 1), c ^ 1, slice(j - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1,
@@ -882,6 +836,7 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
         const int n_act = tab.cnt[c][j + 1];
         const int bd = blockDim.x;
         auto inside = [&](int2 e) {
+            if (!EDGE) return true;
             const int gx = x0 + (int)(short)(e.x & 0xffff), gy = y0 + (e.x >> 16);
             return gx >= 0 && gy >= 0 && gx < w && gy < h;
         };
@@ -889,7 +844,7 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
             const int2 e = te[threadIdx.x];
             if (inside(e)) {
                 AdjPx<T> q;
-                adj_px_load<T>(q, e, x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
+                adj_px_load<T, EDGE>(q, e, x0, y0, h, w, Rw, Rp1, gather, own, oth, ax, ay, PL);
                 if (c == 0)
                     adj_px_step<T, true>(q, ax, ay, omega, gs, PL, g0, gax, gay, tsx, tsy);
                 else
@@ -901,8 +856,8 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
             const bool ha = inside(ea);
             const bool hb = i + bd < n_act && inside(te[i + bd]);
             AdjPx<T> qa, qb;
-            if (ha) adj_px_load<T>(qa, ea, x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
-            if (hb) adj_px_load<T>(qb, te[i + bd], x0, y0, h, w, Rw, Rp1, n1, gather, own, oth, ax, ay, PL);
+            if (ha) adj_px_load<T, EDGE>(qa, ea, x0, y0, h, w, Rw, Rp1, gather, own, oth, ax, ay, PL);
+            if (hb) adj_px_load<T, EDGE>(qb, te[i + bd], x0, y0, h, w, Rw, Rp1, gather, own, oth, ax, ay, PL);
             if (ha) adj_px_step<T, false>(qa, ax, ay, omega, gs, PL, dummy, dax, day, tsx, tsy);
             if (hb) adj_px_step<T, false>(qb, ax, ay, omega, gs, PL, dummy, dax, day, tsx, tsy);
         }
@@ -910,6 +865,110 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
         __syncthreads();
         cur[c ^ 1] ^= 1;
     }
+}
+
+// Adjoint of all nh half-sweeps of one tick window in one launch (temporal
+// blocking), with kd_rb_adj_step's arithmetic.  A CTA owns a TX x TY tile of
+// one frame (TX = TY = 16 or 32) and keeps in shared memory:
+//  * over the tile grown by nh pixels on every side (Rw x Rh): (A12, B1e),
+//    (B2e, 1 / den_u), 1 / den_v, lam and the pixel's latest (au, av);
+//  * over the tile grown by nh + 1 (Rh1 rows of Rp1 pixel pairs), per colour
+//    two buffers of the solver state (du, dv) before a half-sweep, filled by
+//    cp.async from the window's stored half-sweeps (hist + j * slot,
+//    compressed; s0, NULL: zero, before the first) one step ahead: before
+//    half-sweep j the moving colour holds its values after j - 2 and the other
+//    colour after j - 1, so each step replaces one colour;
+//  * the two colours' ring tables (AdjTable).
+// lam of the tile after the window depends on the pixels within j + 1 of the
+// tile at half-sweep j, so step j (from nh - 1 down to 0) updates the moving
+// pixels of that shrinking region: the tile's own pixels and a halo that
+// neighbouring tiles also compute.  They come from the ring table of the
+// step's colour (the tile first, entry t the pixel of thread t's horizontal
+// pair, then the rings at distance 1, 2, ...), so a step's pixels are its
+// first cnt[c][j + 1] entries and the threads stay busy as the region shrinks.
+// Thread t keeps its pair's coefficient gradients and its alpha gradients in
+// registers for the whole window.  Tiles whose outer region lies inside the
+// level take a path without border tests.  The window ends with the closing
+// gather of the tile's colour-1 pixels (kd_rb_adj_gather); the tile's lam goes
+// to lam_out, which is not lam_in (tiles read each other's halo), and its
+// coefficient gradients overwrite gcoef.  blockDim.x = TX * TY / 2.
+template <typename T>
+__global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ coef, const T* __restrict__ s0,
+                                                         const T* __restrict__ hist, long long slot,
+                                                         const T* __restrict__ lam_in, T* __restrict__ lam_out, int h,
+                                                         int w, int nh, int TX, int TY, AdjTable tab, T ax, T ay,
+                                                         T omega, T eps, int gs, T* __restrict__ gcoef, double sx,
+                                                         double sy, double* __restrict__ galpha)
+{
+    using V2 = typename Vec2T<T>::type;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* const sm = reinterpret_cast<T*>(smraw);
+    const int Rw = TX + 2 * nh, Rh = TY + 2 * nh, R = Rw * Rh;
+    const int Rp1 = (Rw + 2) >> 1, Rh1 = Rh + 2, n1 = Rh1 * Rp1;
+    // R is even (TX even), so every V2 plane starts on a V2 boundary
+    AdjPlanes<T> PL;
+    PL.C0 = reinterpret_cast<V2*>(sm);
+    PL.C1 = reinterpret_cast<V2*>(sm + 2 * R);
+    PL.C2 = sm + 4 * R;
+    PL.L = reinterpret_cast<V2*>(sm + 5 * R);
+    PL.A = reinterpret_cast<V2*>(sm + 7 * R);
+    V2* const sS = reinterpret_cast<V2*>(sm + 9 * R);  // state buffers: (colour * 2 + buffer) * n1
+    int2* const sTab = reinterpret_cast<int2*>(sS + 4 * n1);
+    const int nt0 = tab.cnt[0][nh], nt1 = tab.cnt[1][nh];
+    for (int i = threadIdx.x; i < nt0; i += blockDim.x) sTab[i] = tab.e[0][i];
+    for (int i = threadIdx.x; i < nt1; i += blockDim.x) sTab[nt0 + i] = tab.e[1][i];
+    const long long f = blockIdx.z, hw = (long long)h * w;
+    const int hw2 = (w + 1) >> 1;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int rx0 = x0 - nh, ry0 = y0 - nh;
+    const int rx1 = rx0 - 1, ry1 = ry0 - 1;
+    const float inv_rp1 = 1.0f / (float)Rp1;
+    auto slice = [&](int k) -> StateSlice<T> {
+        if (k >= 0) return StateSlice<T>{hist + (long long)k * slot, 2};
+        return StateSlice<T>{s0, s0 ? 1 : 0};
+    };
+    // the states before the window's last half-sweep nh - 1 (colour 1): colour 1
+    // after nh - 3 into its buffer 0, colour 0 after nh - 2 into its buffer 0
+    stage_colour<T>(sS + 2 * n1, 1, slice(nh - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
+    stage_colour<T>(sS, 0, slice(nh - 2), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
+    {
+        const T* cf = coef + f * 5 * hw;
+        const T* liu = lam_in + f * 2 * hw;
+        const T* liv = liu + hw;
+        const T sw = ax + ax + ay + ay;
+        const float inv_rw = 1.0f / (float)Rw;
+        for (int i = threadIdx.x; i < R; i += blockDim.x) {
+            const int ry = (int)(((float)i + 0.5f) * inv_rw);
+            const int gy = ry0 + ry, gx = rx0 + (i - ry * Rw);
+            if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
+                const long long q = (long long)gy * w + gx;
+                V2 c0, c1, l;
+                c0.x = cf[2 * hw + q];
+                c0.y = cf[3 * hw + q];
+                c1.x = cf[4 * hw + q];
+                c1.y = (T)1 / tmax(cf[q] + sw, eps);
+                PL.C0[i] = c0;
+                PL.C1[i] = c1;
+                PL.C2[i] = (T)1 / tmax(cf[hw + q] + sw, eps);
+                l.x = liu[q];
+                l.y = liv[q];
+                PL.L[i] = l;
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    T g0[5] = {0, 0, 0, 0, 0}, g1[5] = {0, 0, 0, 0, 0};  // the thread's colour-0 and colour-1 pixels
+    T gax = 0, gay = 0;
+    const T tsx = (T)sx, tsy = (T)sy;
+    const int nin = (TX * TY) >> 1;  // entries 0 .. nin - 1 of a colour: the tile's own pixels, thread t's at t
+    const bool edge = rx1 < 0 || ry1 < 0 || rx1 + 2 * Rp1 > w || ry1 + Rh1 > h;
+    if (edge)
+        adj_window_steps<T, true>(nh, x0, y0, h, w, Rw, Rp1, n1, nin, sTab, nt0, tab, sS, s0, hist, slot, f,
+                                  hw2, rx1, ry1, Rh1, inv_rp1, ax, ay, omega, gs, PL, g0, g1, gax, gay, tsx, tsy);
+    else
+        adj_window_steps<T, false>(nh, x0, y0, h, w, Rw, Rp1, n1, nin, sTab, nt0, tab, sS, s0, hist, slot, f,
+                                   hw2, rx1, ry1, Rh1, inv_rp1, ax, ay, omega, gs, PL, g0, g1, gax, gay, tsx, tsy);
     // the closing gather (colour 1), then the tile's lam and coefficient gradients
     T* lou = lam_out + f * 2 * hw;
     T* gc = gcoef + f * 5 * hw;
@@ -919,19 +978,19 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
         const int px = x0 + (int)(short)(e.x & 0xffff), py = y0 + (e.x >> 16);
         if (py < h && px < w) {
             const int li = e.y & 0x1fff;
-            T lu = sLu[li], lv = sLv[li];
+            V2 l = PL.L[li];
             if (c == 1) {
                 T su = 0, sv = 0;
-                if (px > 0) { su += ax * sAu[li - 1]; sv += ax * sAv[li - 1]; }
-                if (px < w - 1) { su += ax * sAu[li + 1]; sv += ax * sAv[li + 1]; }
-                if (py > 0) { su += ay * sAu[li - Rw]; sv += ay * sAv[li - Rw]; }
-                if (py < h - 1) { su += ay * sAu[li + Rw]; sv += ay * sAv[li + Rw]; }
-                lu += su;
-                lv += sv;
+                if (px > 0) { const V2 a = PL.A[li - 1]; su += ax * a.x; sv += ax * a.y; }
+                if (px < w - 1) { const V2 a = PL.A[li + 1]; su += ax * a.x; sv += ax * a.y; }
+                if (py > 0) { const V2 a = PL.A[li - Rw]; su += ay * a.x; sv += ay * a.y; }
+                if (py < h - 1) { const V2 a = PL.A[li + Rw]; su += ay * a.x; sv += ay * a.y; }
+                l.x += su;
+                l.y += sv;
             }
             const long long q = (long long)py * w + px;
-            lou[q] = lu;
-            lou[hw + q] = lv;
+            lou[q] = l.x;
+            lou[hw + q] = l.y;
             const T* gg = c == 0 ? g0 : g1;
 #pragma unroll
             for (int k = 0; k < 5; ++k) gc[k * hw + q] = gg[k];
