@@ -931,32 +931,45 @@ __global__ void __launch_bounds__(512) kd_rb_adj_window(const T* __restrict__ co
     // after nh - 3 into its buffer 0, colour 0 after nh - 2 into its buffer 0
     stage_colour<T>(sS + 2 * n1, 1, slice(nh - 3), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
     stage_colour<T>(sS, 0, slice(nh - 2), f, h, w, hw2, rx1, ry1, Rh1, Rp1, inv_rp1);
+    // the coefficients and lam over the tile grown by nh, copied asynchronously (the two
+    // denominators raw, turned into reciprocals once they have arrived)
+    const float inv_rw = 1.0f / (float)Rw;
     {
         const T* cf = coef + f * 5 * hw;
         const T* liu = lam_in + f * 2 * hw;
         const T* liv = liu + hw;
-        const T sw = ax + ax + ay + ay;
-        const float inv_rw = 1.0f / (float)Rw;
         for (int i = threadIdx.x; i < R; i += blockDim.x) {
             const int ry = (int)(((float)i + 0.5f) * inv_rw);
             const int gy = ry0 + ry, gx = rx0 + (i - ry * Rw);
             if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
                 const long long q = (long long)gy * w + gx;
-                V2 c0, c1, l;
-                c0.x = cf[2 * hw + q];
-                c0.y = cf[3 * hw + q];
-                c1.x = cf[4 * hw + q];
-                c1.y = (T)1 / tmax(cf[q] + sw, eps);
-                PL.C0[i] = c0;
-                PL.C1[i] = c1;
-                PL.C2[i] = (T)1 / tmax(cf[hw + q] + sw, eps);
-                l.x = liu[q];
-                l.y = liv[q];
-                PL.L[i] = l;
+                T* c0 = reinterpret_cast<T*>(PL.C0 + i);
+                T* c1 = reinterpret_cast<T*>(PL.C1 + i);
+                T* l = reinterpret_cast<T*>(PL.L + i);
+                cp_async_el(c0, cf + 2 * hw + q);
+                cp_async_el(c0 + 1, cf + 3 * hw + q);
+                cp_async_el(c1, cf + 4 * hw + q);
+                cp_async_el(c1 + 1, cf + q);
+                cp_async_el(PL.C2 + i, cf + hw + q);
+                cp_async_el(l, liu + q);
+                cp_async_el(l + 1, liv + q);
+            }
+        }
+        cp_async_commit();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    {
+        const T sw = ax + ax + ay + ay;
+        for (int i = threadIdx.x; i < R; i += blockDim.x) {
+            const int ry = (int)(((float)i + 0.5f) * inv_rw);
+            const int gy = ry0 + ry, gx = rx0 + (i - ry * Rw);
+            if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
+                PL.C1[i].y = (T)1 / tmax(PL.C1[i].y + sw, eps);
+                PL.C2[i] = (T)1 / tmax(PL.C2[i] + sw, eps);
             }
         }
     }
-    cp_async_wait_all();
     __syncthreads();
     T g0[5] = {0, 0, 0, 0, 0}, g1[5] = {0, 0, 0, 0, 0};  // the thread's colour-0 and colour-1 pixels
     T gax = 0, gay = 0;
@@ -1081,6 +1094,15 @@ __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, co
         const T* Jf = J + f * 6 * K * hw + pix;
         T* gJf = gJ + f * 6 * K * hw + pix;
         const long long qs = (long long)K * hw;
+        // with the channel count known, the accumulated tensor gradients are read up front, so
+        // their loads overlap the power and the other loads instead of following them
+        T gjp[KT > 0 ? 6 * KT : 1];
+        if constexpr (KT > 0) {
+#pragma unroll
+            for (int k = 0; k < KT; ++k)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) gjp[k * 6 + q] = gJf[k * hw + q * qs];
+        }
         // psi and the raw sums (for the max(., eps) clamps), as kd_tick computes them
         T psi[KA], Er[KA];
         T A11 = 0, A22 = 0;
@@ -1125,12 +1147,21 @@ __global__ void kd_tick_adj(const T* __restrict__ J, const T* __restrict__ W, co
                 ldu += gE * ((T)2 * j11 * du + (T)2 * j12 * dv + (T)2 * j13);
                 ldv += gE * ((T)2 * j22 * dv + (T)2 * j12 * du + (T)2 * j23);
             }
-            gj[0] += g11k;
-            gj[qs] += g22k;
-            gj[2 * qs] += g33k;
-            gj[3 * qs] += g12k;
-            gj[4 * qs] += g13k;
-            gj[5 * qs] += g23k;
+            if constexpr (KT > 0) {
+                gj[0] = gjp[k * 6 + 0] + g11k;
+                gj[qs] = gjp[k * 6 + 1] + g22k;
+                gj[2 * qs] = gjp[k * 6 + 2] + g33k;
+                gj[3 * qs] = gjp[k * 6 + 3] + g12k;
+                gj[4 * qs] = gjp[k * 6 + 4] + g13k;
+                gj[5 * qs] = gjp[k * 6 + 5] + g23k;
+            } else {
+                gj[0] += g11k;
+                gj[qs] += g22k;
+                gj[2 * qs] += g33k;
+                gj[3 * qs] += g12k;
+                gj[4 * qs] += g13k;
+                gj[5 * qs] += g23k;
+            }
         }
         if (lam && !lagged) {
             lam[f * 2 * hw + pix] += ldu;
