@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--diff-frames", type=int, default=64,
                     help="frames of the differentiation workload (512x512x1); 0 skips it")
-    ap.add_argument("--diff-modes", default="implicit,unrolled,unrolled_store_sweeps",
+    ap.add_argument("--diff-modes", default="unrolled_store_sweeps,unrolled,implicit",
                     help="gradient modes timed in the differentiation workload")
     ap.add_argument("--uneven-frames", type=int, default=256,
                     help="frames of the uneven-size batch (sizes 256^2, 512^2, 796x512, 1024^2; 1-2 channels); 0 skips")
@@ -167,15 +167,18 @@ def run_diff(args, dev):
         plan.close()
         del plan
         torch.cuda.empty_cache()
-    head = modes.get("unrolled") or next(iter(modes.values()))
+    head = modes.get("unrolled_store_sweeps") or modes.get("unrolled") or next(iter(modes.values()))
     return {"workload": f"{F} x 512x512x1 photon-count frames, registration loss (lambda 0.1)",
             "dtype": "f32", "pixel_order": "gauss_seidel",
-            "headline": "unrolled: the exact gradient (every half-sweep reversed, psi ticks differentiated); "
-                        "checkpoints per level (resized frames, input flow, solver state at each psi tick), "
-                        "each tick window and J recomputed in the backward, each window's adjoint in one tiled "
-                        "launch ('_stepwise': one launch per half-sweep).  'implicit' holds psi at its last "
-                        "tick and differentiates the level's fixed point with one SOR solve on the same "
-                        "operator: cheaper, but at a_data = 0.45 it misses most of the exact derivative",
+            "headline": "unrolled_store_sweeps: the exact gradient (every half-sweep reversed, psi ticks "
+                        "differentiated) with per-level checkpoints of the resized frames, input flow, every "
+                        "half-sweep's moved pixels and each psi window's coefficients; the warp and J are "
+                        "recomputed in the backward and each window's adjoint runs in one tiled launch.  "
+                        "'unrolled' checkpoints only the state at each psi tick and recomputes the window's "
+                        "sweeps and coefficients (less memory, more time); '_stepwise' runs the adjoint one "
+                        "launch per half-sweep.  'implicit' holds psi at its last tick and differentiates the "
+                        "level's fixed point with one SOR solve on the same operator: cheaper, but at "
+                        "a_data = 0.45 it misses most of the exact derivative",
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
 
 
