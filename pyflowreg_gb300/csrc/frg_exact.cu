@@ -10,6 +10,7 @@
 // Layout: row-major planes, the level arrays with their one-pixel ring
 // (m = h + 2 rows, n = w + 2 columns), like the reference's numpy arrays.
 #include "frg_internal.h"
+#include "frg_select.cuh"
 
 #include <math.h>
 
@@ -1056,46 +1057,117 @@ __device__ double median25_keys(double v[25])
     return median25d(v);
 }
 
-__global__ void kx_median_accum(const double* __restrict__ du, const double* __restrict__ dv,
-                                const double* __restrict__ u, const double* __restrict__ v, long long uv_fs, int h,
-                                int w, int do_median, double* ou, double* ov, long long o_fs, long long o_rs,
-                                long long o_cs)
+// Median + accumulate on the padded float64 du, dv ((T, h + 2, w + 2) with
+// the level's edge ring), exact like median25_keys: a 32 x 16 output tile with
+// its mirrored 2-pixel halo is staged in shared memory as the doubles and
+// their float keys (high words); each thread takes two vertically adjacent
+// pixels, whose windows share four of their five rows, and median25_pair
+// finds both windows' 13th smallest keys on the float pipe.  A key carried by
+// exactly one value of its window names the median; when several values share
+// it, or a key is not a finite float, median25d decides from the doubles.
+// Needs h, w >= 3 when do_median.
+constexpr int kXMedTx = 32, kXMedTy = 8, kXMedRows = 2 * kXMedTy;
+
+__device__ __forceinline__ int mirror_x(int i, int n)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+    return i;
+}
+
+__global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* __restrict__ du,
+                                                                 const double* __restrict__ dv,
+                                                                 const double* __restrict__ u,
+                                                                 const double* __restrict__ v, long long uv_fs, int h,
+                                                                 int w, int do_median, double* ou, double* ov,
+                                                                 long long o_fs, long long o_rs, long long o_cs)
+{
+    __shared__ double sd[2][kXMedRows + 4][kXMedTx + 4];
+    __shared__ float sk[2][kXMedRows + 4][kXMedTx + 4];
     const int f = blockIdx.z;
-    if (x >= w) return;
+    const int x0 = blockIdx.x * kXMedTx, y0 = blockIdx.y * kXMedRows;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * kXMedTx + tx;
     const long long n = w + 2, mn = (long long)(h + 2) * n;
     const double* duf = du + (long long)f * mn;
     const double* dvf = dv + (long long)f * mn;
-    double mu, mv;
     if (do_median) {
-        double a[25], b[25];
-        int q = 0;
-        for (int dy = -2; dy <= 2; ++dy) {
-            int yy = y + dy;
-            if (yy < 0) yy = -yy;
-            if (yy >= h) yy = 2 * (h - 1) - yy;
-            for (int dx = -2; dx <= 2; ++dx) {
-                int xx = x + dx;
-                if (xx < 0) xx = -xx;
-                if (xx >= w) xx = 2 * (w - 1) - xx;
-                const long long o = (long long)(yy + 1) * n + xx + 1;
-                a[q] = duf[o];
-                b[q] = dvf[o];
-                ++q;
+        for (int i = tid; i < (kXMedRows + 4) * (kXMedTx + 4); i += kXMedTx * kXMedTy) {
+            const int r = i / (kXMedTx + 4), c = i - r * (kXMedTx + 4);
+            const int yy = mirror_x(min(y0 - 2 + r, h + 1), h);
+            const int xx = mirror_x(min(x0 - 2 + c, w + 1), w);
+            const long long o = (long long)(yy + 1) * n + xx + 1;
+            const double a = duf[o], b = dvf[o];
+            sd[0][r][c] = a;
+            sd[1][r][c] = b;
+            sk[0][r][c] = hikey(a);
+            sk[1][r][c] = hikey(b);
+        }
+        __syncthreads();
+    }
+    const int x = x0 + tx, ya = y0 + 2 * ty, yb = ya + 1;
+    if (x >= w || ya >= h) return;
+    double m[2][2];  // [pixel a / b][du / dv]
+    if (do_median) {
+#pragma unroll
+        for (int pl = 0; pl < 2; ++pl) {
+            float c20[20], ea[5], eb[5];
+#pragma unroll
+            for (int dy = 0; dy < 4; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 5; ++dx) c20[dy * 5 + dx] = sk[pl][2 * ty + 1 + dy][tx + dx];
+#pragma unroll
+            for (int dx = 0; dx < 5; ++dx) {
+                ea[dx] = sk[pl][2 * ty][tx + dx];
+                eb[dx] = sk[pl][2 * ty + 5][tx + dx];
+            }
+            float km[2];
+            median25_pair(c20, ea, eb, km[0], km[1]);
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int r0 = 2 * ty + q;
+                int eq = 0;
+                bool finite = true;
+                double pick = 0.0;
+#pragma unroll
+                for (int dy = 0; dy < 5; ++dy)
+#pragma unroll
+                    for (int dx = 0; dx < 5; ++dx) {
+                        const float k = sk[pl][r0 + dy][tx + dx];
+                        finite = finite && fabsf(k) <= 3.402823466e38f;
+                        if (k == km[q]) {
+                            ++eq;
+                            pick = sd[pl][r0 + dy][tx + dx];
+                        }
+                    }
+                if (!(finite && eq == 1)) {
+                    double win[25];
+#pragma unroll
+                    for (int dy = 0; dy < 5; ++dy)
+#pragma unroll
+                        for (int dx = 0; dx < 5; ++dx) win[dy * 5 + dx] = sd[pl][r0 + dy][tx + dx];
+                    pick = median25d(win);
+                }
+                m[q][pl] = pick;
             }
         }
-        mu = median25_keys(a);
-        mv = median25_keys(b);
     } else {
-        const long long o = (long long)(y + 1) * n + x + 1;
-        mu = duf[o];
-        mv = dvf[o];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int y = ya + q < h ? ya + q : ya;
+            const long long o = (long long)(y + 1) * n + x + 1;
+            m[q][0] = duf[o];
+            m[q][1] = dvf[o];
+        }
     }
-    const long long oc = (long long)(y + 1) * n + x + 1;
-    ou[f * o_fs + y * o_rs + x * o_cs] = dadd(u[f * uv_fs + oc], mu);
-    ov[f * o_fs + y * o_rs + x * o_cs] = dadd(v[f * uv_fs + oc], mv);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int y = ya + q;
+        if (y >= h) break;
+        const long long oc = (long long)(y + 1) * n + x + 1;
+        ou[f * o_fs + y * o_rs + x * o_cs] = dadd(u[f * uv_fs + oc], m[q][0]);
+        ov[f * o_fs + y * o_rs + x * o_cs] = dadd(v[f * uv_fs + oc], m[q][1]);
+    }
 }
 
 // 5x5 median (scipy "mirror") of one float64 plane (h, w), h, w >= 3.
@@ -1131,8 +1203,9 @@ cudaError_t launch_x_median_accum(const double* du, const double* dv, const doub
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st)
 {
-    dim3 blk(128), grd((w + 127) / 128, h, n_frames);
-    kx_median_accum<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
+    if (n_frames > 65535) return cudaErrorInvalidValue;
+    dim3 blk(kXMedTx, kXMedTy), grd((w + kXMedTx - 1) / kXMedTx, (h + kXMedRows - 1) / kXMedRows, n_frames);
+    kx_median_rm<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
     return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 // restates is given above it.  All kernels are bounded loops without
 // inter-CTA waits, so none of them can hang.
 #include "frg_internal.h"
+#include "frg_select.cuh"
 
 #include <math.h>
 
@@ -875,59 +876,6 @@ __device__ float median25(float v[25])
     cswap(t[12], t[13]);
     cswap(t[11], t[12]);
     return t[12];
-}
-
-// Medians of two 25-element windows that share their first 20 elements
-// (vertically adjacent 5 x 5 windows: v[0..19] the four common rows, a[0..4]
-// and b[0..4] the rows only one window has).  Forgetful selection as in
-// median25: the rounds that only see common elements (the first 14, then
-// v[14..19]) run once for both windows; the last four rounds and the final
-// median of three run per window.  Each result is the median of its window.
-__device__ __forceinline__ void median25_pair(const float v[20], const float a[5], const float b[5], float& ma,
-                                              float& mb)
-{
-    float t[14];
-#pragma unroll
-    for (int i = 0; i < 14; ++i) t[i] = v[i];
-#pragma unroll
-    for (int round = 0; round < 7; ++round) {
-        const int lo = round;
-#pragma unroll
-        for (int i = lo + 1; i < 14; ++i) cswap(t[lo], t[i]);
-#pragma unroll
-        for (int i = lo + 1; i < 13; ++i) cswap(t[i], t[13]);
-        t[13] = round < 6 ? v[14 + round] : 0.0f;
-    }
-    // round 6 dropped t[6] and t[13]; t[7..12] are the shared survivors
-    float ta[14], tb[14];
-#pragma unroll
-    for (int i = 7; i < 13; ++i) ta[i] = tb[i] = t[i];
-    ta[13] = a[0];
-    tb[13] = b[0];
-#pragma unroll
-    for (int round = 7; round < 11; ++round) {
-        const int lo = round;
-#pragma unroll
-        for (int i = lo + 1; i < 14; ++i) {
-            cswap(ta[lo], ta[i]);
-            cswap(tb[lo], tb[i]);
-        }
-#pragma unroll
-        for (int i = lo + 1; i < 13; ++i) {
-            cswap(ta[i], ta[13]);
-            cswap(tb[i], tb[13]);
-        }
-        ta[13] = a[round - 6];
-        tb[13] = b[round - 6];
-    }
-    cswap(ta[11], ta[12]);
-    cswap(ta[12], ta[13]);
-    cswap(ta[11], ta[12]);
-    cswap(tb[11], tb[12]);
-    cswap(tb[12], tb[13]);
-    cswap(tb[11], tb[12]);
-    ma = ta[12];
-    mb = tb[12];
 }
 
 __global__ void k_median_accum(const float* __restrict__ du, const float* __restrict__ dv, long long st_fs,
