@@ -1105,7 +1105,7 @@ __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* 
         }
         __syncthreads();
     }
-    const int x = x0 + tx, ya = y0 + 2 * ty, yb = ya + 1;
+    const int x = x0 + tx, ya = y0 + 2 * ty;
     if (x >= w || ya >= h) return;
     double m[2][2];  // [pixel a / b][du / dv]
     if (do_median) {
