@@ -182,7 +182,7 @@ def run_diff(args, dev):
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
 
 
-def run_uneven(args, dev):
+def run_uneven(args, dev, precision="fp32"):
     """Uneven-size batch: frames drawn uniformly from {256^2, 512^2, 796x512,
     1024^2} x {1, 2} channels, each size/channel pair a video of its own
     registered to the mean of its first 50 frames; one register() call for all
@@ -210,7 +210,7 @@ def run_uneven(args, dev):
             frames.append(preprocess_torch(vid.frame(t), ref_raw).contiguous())
     opts = dict(OPTIONS)
     opts.pop("min_level", None)
-    opts["precision"] = "fp32"
+    opts["precision"] = precision
     ub = UnevenBatch({k: v[2] for k, v in refs.items()}, graphs=True, **opts)
     ub.register(frames)  # plans, graph capture
     torch.cuda.synchronize()
@@ -225,7 +225,7 @@ def run_uneven(args, dev):
     ms = e0.elapsed_time(e1) / reps
     ub.close()
     counts = {f"{k[0]}x{k[1]}x{k[2]}": v for k, v in sorted(counters.items())}
-    return {"workload": f"{len(frames)} frames of mixed size and channels, one register() call", "precision": "fp32",
+    return {"workload": f"{len(frames)} frames of mixed size and channels, one register() call", "precision": precision,
             "frames_per_size": counts, "ms_per_batch": ms, "frames_per_s": len(frames) / (ms / 1e3),
             "graphs": True, "streams": 4}
 
@@ -326,7 +326,10 @@ def run_stream(args, dev):
     if n_epe:
         stream["vs_oracle"] = stream_epe(refp, host, kept, OPTIONS)
     del host
-    return stream, run_compensate(raw_u16, ref_raw_np, B, opts)
+    comp = run_compensate(raw_u16, ref_raw_np, B, opts)
+    # the same loop in float64 (the reference's precision) on the first 64 frames
+    comp["fp64"] = run_compensate(raw_u16[:min(N, 2 * B)], ref_raw_np, B, dict(opts, precision="fp64"))
+    return stream, comp
 
 
 def stream_epe(refp, host, kept, options):
@@ -798,6 +801,8 @@ def run_gb300(args):
         parity.pop("_oracle_flows", None)
     backward = run_diff(args, dev) if (rank == 0 and args.diff_frames > 0) else None
     uneven = run_uneven(args, dev) if (rank == 0 and args.uneven_frames > 0) else None
+    if uneven is not None:
+        uneven["fp64"] = run_uneven(args, dev, "fp64")
     stream_2048, compensate_2048 = run_stream(args, dev) if (rank == 0 and args.stream_frames > 0) else (None, None)
 
     if rank == 0:

@@ -60,7 +60,8 @@ class UnevenBatch:
         return out
 
     def register(self, frames: Sequence[torch.Tensor]) -> List[torch.Tensor]:
-        """flows (H, W, 2) float32 on the device, in the order of `frames`."""
+        """flows (H, W, 2) on the device (float64 with precision="fp64",
+        float32 otherwise), in the order of `frames`."""
         groups = self.groups(frames)
         results: List[Optional[torch.Tensor]] = [None] * len(frames)
         main = torch.cuda.current_stream()
@@ -87,7 +88,8 @@ class UnevenBatch:
         if entry is None:
             H, W, K = key
             static_in = torch.empty((n, H, W, K), dtype=torch.float32, device=group[0].device)
-            static_out = torch.empty((n, H, W, 2), dtype=torch.float32, device=group[0].device)
+            static_out = torch.empty((n, H, W, 2), dtype=torch.float64 if plan.fp64 else torch.float32,
+                                     device=group[0].device)
             static_in.copy_(torch.stack(group))
             plan.displacement(static_in, None, static_out, stream=st)  # warm-up outside the capture
             g = torch.cuda.CUDAGraph()

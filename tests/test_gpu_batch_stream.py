@@ -20,8 +20,8 @@ def _frames(key, n, seed):
     return preprocess_torch(ref_raw, ref_raw).contiguous(), preprocess_torch(raw[4:], ref_raw).contiguous()
 
 
-@pytest.mark.parametrize("graphs", [False, True])
-def test_uneven_batch_equals_per_group_calls(graphs):
+@pytest.mark.parametrize("graphs,precision", [(False, "fp32"), (True, "fp32"), (True, "fp64")])
+def test_uneven_batch_equals_per_group_calls(graphs, precision):
     from pyflowreg_gb300 import api
     from pyflowreg_gb300.batch import UnevenBatch
 
@@ -36,13 +36,13 @@ def test_uneven_batch_equals_per_group_calls(graphs):
     order = np.random.default_rng(0).permutation(len(frames))
     frames = [frames[i] for i in order]
     keys = [keys[i] for i in order]
-    ub = UnevenBatch(refs, graphs=graphs, **OPTS)
+    ub = UnevenBatch(refs, graphs=graphs, precision=precision, **OPTS)
     for _ in range(2):  # the second call replays the captured graphs
         got = ub.register(frames)
     torch.cuda.synchronize()
     for key in shapes:
         idx = [i for i, k in enumerate(keys) if k == key]
-        plan = api.Plan(api.make_params(K=key[2], **OPTS), *key, len(idx))
+        plan = api.Plan(api.make_params(K=key[2], precision=precision, **OPTS), *key, len(idx))
         plan.set_reference(refs[key])
         ref = plan.displacement(torch.stack([frames[i] for i in idx]))
         torch.cuda.synchronize()
