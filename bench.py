@@ -70,6 +70,10 @@ def parse():
                     help="frames of the differentiation workload (512x512x1); 0 skips it")
     ap.add_argument("--diff-modes", default="unrolled_store_sweeps,unrolled,implicit",
                     help="gradient modes timed in the differentiation workload")
+    ap.add_argument("--compensate-frames", type=int, default=800,
+                    help="frames of the 512x512x2 compensate loop in float64 (batches of 400); 0 skips it")
+    ap.add_argument("--no-config0", dest="config0", action="store_false",
+                    help="skip the single 256x256x1 pair through get_displacement")
     ap.add_argument("--uneven-frames", type=int, default=256,
                     help="frames of the uneven-size batch (sizes 256^2, 512^2, 796x512, 1024^2; 1-2 channels); 0 skips")
     ap.add_argument("--stream-epe-frames", type=int, default=0,
@@ -180,6 +184,73 @@ def run_diff(args, dev):
                         "level's fixed point with one SOR solve on the same operator: cheaper, but at "
                         "a_data = 0.45 it misses most of the exact derivative",
             "fwd_ms": head["fwd_ms"], "bwd_ms": head["bwd_ms"], "ratio": head["ratio"], "modes": modes}
+
+
+def frame_model_bytes(levels, K_, iterations, update_lag):
+    """Streaming-model bytes of one frame (float32 words): per level of N
+    padded pixels, I iterations of 36 B (five folded coefficients read, du, dv
+    read and written), floor(I / L) psi ticks of 24K + 28 B (J, du, dv read,
+    coefficients written) and 4 (13K + 12) B of level setup (resize, warp, J,
+    weight, flow upsample, median, accumulate)."""
+    per_px = iterations * 36 + (iterations // update_lag) * (24 * K_ + 28) + 4 * (13 * K_ + 12)
+    return float(sum((h + 2) * (w + 2) for (h, w, _, _) in levels) * per_px)
+
+
+def run_config0(args, dev):
+    """The plain method on one 256x256x1 pair with the default OFOptions (the
+    reference's CPU configuration): get_displacement with host arrays in and
+    out, then the compensation warp of the moving frame, per call."""
+    import torch
+
+    import pyflowreg_gb300 as G
+    from pyflowreg_gb300.synthetic import pair_256
+
+    fixed, moving, truth = pair_256(0)
+    opts = dict(OPTIONS)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        flow = G.get_displacement(fixed, moving, precision=prec, **opts)  # warm-up: plan, tables
+        G.imregister_wrapper(moving, flow[..., 0], flow[..., 1], fixed)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            flow = G.get_displacement(fixed, moving, precision=prec, **opts)
+            reg = G.imregister_wrapper(moving, flow[..., 0], flow[..., 1], fixed)
+            times.append(time.perf_counter() - t0)
+        d = flow - truth
+        res[prec] = {"ms_per_pair": 1e3 * statistics.median(times),
+                     "epe_vs_truth_px": float(np.sqrt((d ** 2).sum(-1)).mean()),
+                     "compensated_shape": list(reg.shape)}
+    return {"workload": "one 256x256x1 pair (40 blobs, sinusoid field of 4 px), default OFOptions, "
+                        "get_displacement (numpy in and out) + compensation warp, wall clock, median of 5",
+            **res}
+
+
+def run_compensate_512(args, dev):
+    """The 512x512x2 photon-count video as uint16 counts through the streamed
+    compensate loop in float64, batches of 400 (OFOptions.buffer_size):
+    preprocessing against the raw reference, the initial-field chain between
+    batches, flows, compensation warp and statistics on the device."""
+    import torch
+
+    from pyflowreg_gb300.synthetic import TorchVideo
+
+    N, B = args.compensate_frames, 400
+    vid = TorchVideo(seed=1, h=H, w=W, K=K, device=dev)
+    with torch.no_grad():
+        ref_raw = vid.frames(0, 50).mean(0).double().cpu().numpy()
+        raw = np.empty((N, H, W, K), np.uint16)
+        for t0 in range(0, N, 100):
+            n = min(100, N - t0)
+            raw[t0:t0 + n] = vid.frames(50 + t0, n).clamp(0, 65535).to(torch.int32).cpu().numpy().astype(np.uint16)
+    opts = dict(OPTIONS)
+    opts.pop("min_level", None)
+    out = run_compensate(raw, ref_raw, B, dict(opts, precision="fp64"))
+    out["workload"] = (f"{N} x 512x512x2 uint16 frames through the streamed compensate loop in float64, batches of "
+                       f"{B}: preprocess, initial-field chain, flows, compensation warp, statistics, registered "
+                       "frames and flows to the host")
+    return out
 
 
 def run_uneven(args, dev, precision="fp32"):
@@ -787,6 +858,14 @@ def run_gb300(args):
                              "kernel's DFMA x 2 + DADD + DMUL, fold included, profiles/dram_traffic.txt) x pixel "
                              "updates / SOR time, against cuBLAS DGEMM on the same GPU"}
 
+    # the whole frame against the float32 streaming model of bytes per frame
+    bpf = frame_model_bytes(plan.levels(), K, OPTIONS["iterations"], OPTIONS["update_lag"])
+    frame_model = {"bytes_per_frame": bpf, "GBps_at_value": bpf * value / world / 1e9,
+                   "frac_of_hbm": bpf * value / world / 1e9 / peak if peak else None,
+                   "note": "float32 streaming-model bytes per frame (every level's padded pixels x (50 x 36 + "
+                           "10 x (24K + 28) + 4 (13K + 12)) B) at the measured frames/s; the float64 path moves "
+                           "twice the words and is bound by the float64 pipe, not by HBM"}
+
     cpu = parity = None
     reference_gpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -800,6 +879,8 @@ def run_gb300(args):
     if parity is not None:
         parity.pop("_oracle_flows", None)
     backward = run_diff(args, dev) if (rank == 0 and args.diff_frames > 0) else None
+    config0 = run_config0(args, dev) if (rank == 0 and args.config0) else None
+    compensate_512 = run_compensate_512(args, dev) if (rank == 0 and args.compensate_frames > 0) else None
     uneven = run_uneven(args, dev) if (rank == 0 and args.uneven_frames > 0) else None
     if uneven is not None:
         uneven["fp64"] = run_uneven(args, dev, "fp64")
@@ -846,6 +927,9 @@ def run_gb300(args):
             "fp32_fast_path": fp32,
             "bwd_fwd_ratio": backward["ratio"] if backward else None,
             "backward": backward,
+            "frame_streaming_model": frame_model,
+            "config0_pair": config0,
+            "compensate_512": compensate_512,
             "uneven_batch": uneven,
             "stream_2048": stream_2048,
             "compensate_2048": compensate_2048,
@@ -915,8 +999,12 @@ def cpu_baseline(args, ref, frames, gpu_out, precision):
                 "vs_checker": flow_diff(fm, flows),
                 "note": "the analogue of numba's fastmath=True: faster, its flows move within the reference's "
                         "own rounding envelope"}
+    # how far the reference's red-black GPU variants' order alone moves the flow (oracle, float64)
+    rb = O.get_displacement_batch(fx, mv, n_threads=cores, weight=wt, variant="o3", order=O.ORDER_RED_BLACK,
+                                  **OPTIONS)
     parity = {"frames": n, "precision": precision, "timed_path": flow_diff(gpu_out[:n].cpu().numpy(), flows),
               "tolerance": {"max_abs_px": 1e-3, "mean_epe_px": 1e-4},
+              "red_black_order_vs_reference": flow_diff(rb, flows),
               "oracle": "fp64 lexicographic C restatement of pyflowreg's numba path, pinned to the reference's own "
                         "source by the golden fixtures",
               "_oracle_flows": flows}
