@@ -83,6 +83,8 @@ def parse():
                     help="run only the 2048x2048x2 streaming workloads; prints their JSON object")
     ap.add_argument("--stream-frames", type=int, default=128,
                     help="frames of the 2048x2048x2 streaming workload (batches of 32); 0 skips")
+    ap.add_argument("--autotune-levels", type=int, default=4,
+                    help="finest levels whose SOR launch shape the autotuner times on the workload")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default SOR launch shape instead of tuning it on the workload first")
     ap.add_argument("--only-diff", action="store_true",
@@ -747,7 +749,7 @@ def run_gb300(args):
     tuning = None
     if not args.no_autotune:
         # launch-shape tuning on the workload itself (outside the timed region; flows unchanged)
-        chosen = plan.autotune(frames, n_levels=4, reps=1)
+        chosen = plan.autotune(frames, n_levels=args.autotune_levels, reps=1)
         if fp64:
             tuning = {f"level {i} ({plan.level_tuning()[i][3]} rows)":
                       {"kernel": "k_sor_chain64", "rows_per_cta": t or "by batch size"}

@@ -659,8 +659,9 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
     for (int k = 0; k < channels; ++k) pl->a_data[k] = (float)params->a_data[k];
     pl->xpath = params->precision == FRG_FP64_REFERENCE || params->a_smooth != 1.0 ||
                 params->const_assumption == 2 || params->gnc_stages != 0;
-    pl->dpath = params->precision == FRG_FP64_REFERENCE && params->a_smooth == 1.0 &&
-                params->const_assumption != 2 && params->gnc_stages == 0;
+    // the float64 chained SOR serves every float64 level loop without ψ_s or GNC stages: the fp64
+    // precision, and census in either precision (the float32 API then rounds its flow)
+    pl->dpath = pl->xpath && params->a_smooth == 1.0 && params->gnc_stages == 0;
     const int n_passes = fill_passes(params->iterations, params->update_lag, kGMax, nullptr, 0);
     size_t max_dp64 = 0;
     {
@@ -1266,7 +1267,7 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
             // du, dv into the interiors of the padded xdu, xdv for the median
             const long long dp = (long long)L.g.D * L.g.P;
             const double wx = L.alpha_x / (L.h_col * L.h_col), wy = L.alpha_y / (L.h_row * L.h_row);
-            FRG_LAUNCH(launch_x_tensor_diag(L.ref64, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
+            FRG_LAUNCH(launch_x_tensor_diag(L.ref64, L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
                                             pl->p.const_assumption, pl->dJ, 6LL * K * dp, L.g, pl->xuv, pl->xuv + mn,
                                             uv_fs, wx, wy, pl->dlap, 2 * dp, st));
             Pass ps[kMaxChain];

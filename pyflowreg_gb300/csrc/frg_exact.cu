@@ -451,8 +451,9 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
     jo[5] = __fma_rn(rxy, fxt, dmul(ryy, fyt));
 }
 
-__global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__ f1, const float* __restrict__ f2,
-                                                      int K, int h, int w, TensConsts C, int f2_f32, int gray,
+__global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__ f1, const float* __restrict__ f1f,
+                                                      const float* __restrict__ f2, int K, int h, int w, TensConsts C,
+                                                      double hy, double hx, int f2_f32, int gray,
                                                       double* __restrict__ J, long long J_fs, DiagGeom g,
                                                       const double* __restrict__ u, const double* __restrict__ v,
                                                       long long uv_fs, double wx, double wy, double* __restrict__ lap,
@@ -472,7 +473,10 @@ __global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__
     double* Jf = J + f * J_fs;
     for (int k = 0; k < K; ++k) {
         double j[6];
-        tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
+        if (gray == 2)  // census: the reference-order arithmetic of kx_tensor
+            tensor_px64(f1f, f2, f, K, k, h, w, r + 1, c + 1, hy, hx, f2_f32, 2, j);
+        else
+            tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
         // the cross terms doubled (exact), as the solver's data residual uses them
 #pragma unroll
         for (int q = 0; q < 6; ++q) Jf[((long long)q * K + k) * plane + di] = q < 3 ? j[q] : dadd(j[q], j[q]);
@@ -498,8 +502,8 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_x_tensor_diag(const double* f1, const float* f2, int n_frames, int K, int h, int w, double hy,
-                                 double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
+cudaError_t launch_x_tensor_diag(const double* f1, const float* f1f, const float* f2, int n_frames, int K, int h, int w,
+                                 double hy, double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
                                  const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
                                  long long lap_fs, cudaStream_t st)
 {
@@ -516,8 +520,8 @@ cudaError_t launch_x_tensor_diag(const double* f1, const float* f2, int n_frames
     const long long warps = (long long)g.D * (g.P >> 5);
     if ((warps + 7) / 8 > 0x7fffffffLL || n_frames > 65535) return cudaErrorInvalidValue;
     dim3 grd((unsigned)((warps + 7) / 8), n_frames);
-    kx_tensor_diag<<<grd, 256, 0, st>>>(f1, f2, K, h, w, C, f2_f32, gray, J, J_fs, g, u, v, uv_fs, wx, wy, lap,
-                                        lap_fs);
+    kx_tensor_diag<<<grd, 256, 0, st>>>(f1, f1f, f2, K, h, w, C, hy, hx, f2_f32, gray, J, J_fs, g, u, v, uv_fs, wx,
+                                        wy, lap, lap_fs);
     return cudaGetLastError();
 }
 

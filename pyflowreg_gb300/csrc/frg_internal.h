@@ -168,11 +168,13 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
                             int f2_f32, int gray, double* J, cudaStream_t st);
 // The tensor diagonal-major (T, 6, K, D*P) with the smoothness constant
 // (T, 2, D*P) from the padded float64 u, v (frame stride uv_fs), for the
-// float64 chained SOR; f1 is the reference level in float64 (K, h, w).  The
-// planes hold J11, J22, J33, 2 J12, 2 J13, 2 J23: the cross terms doubled
-// (exact), as the solver's data residual uses them.
-cudaError_t launch_x_tensor_diag(const double* f1, const float* f2, int n_frames, int K, int h, int w, double hy,
-                                 double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
+// float64 chained SOR; f1 is the reference level in float64 (K, h, w), f1f the
+// same in float32 (the census data term, gray = 2, runs the reference-order
+// arithmetic of kx_tensor on it).  The planes hold J11, J22, J33, 2 J12, 2 J13,
+// 2 J23: the cross terms doubled (exact), as the solver's data residual uses
+// them.
+cudaError_t launch_x_tensor_diag(const double* f1, const float* f1f, const float* f2, int n_frames, int K, int h, int w,
+                                 double hy, double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
                                  const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
                                  long long lap_fs, cudaStream_t st);
 cudaError_t launch_x_to_double(const float* src, long long n, double* dst, cudaStream_t st);
