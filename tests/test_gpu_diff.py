@@ -303,3 +303,22 @@ def test_plan_rejects_out_of_order_backward():
     flow(torch.tensor(fixed, device=dev), torch.tensor(moving, device=dev), torch.tensor(1.5), plan)
     with pytest.raises(RuntimeError):
         y1.sum().backward()
+
+
+def test_auto_checkpoint_keeps_sweeps_when_they_fit():
+    """checkpoint="auto" keeps every half-sweep (the faster backward) when the
+    checkpoints fit in half the free device memory, which a small plan does;
+    its gradients are those of an explicit "sweeps" plan."""
+    from pyflowreg_gb300.diff import flow
+
+    K, h, w = 1, 40, 36
+    fixed, moving, _, _ = _frames([9], K, h, w)
+    dev = torch.device("cuda")
+    grads = {}
+    for ckpt in ("auto", "sweeps"):
+        plan = _plan(h, w, K, 1, torch.float64, iterations=12, checkpoint=ckpt)
+        assert plan.checkpoint == "sweeps"
+        m_t = torch.tensor(moving, device=dev, requires_grad=True)
+        flow(torch.tensor(fixed, device=dev), m_t, torch.tensor(1.5), plan).pow(2).sum().backward()
+        grads[ckpt] = m_t.grad.cpu()
+    assert torch.equal(grads["auto"], grads["sweeps"])
