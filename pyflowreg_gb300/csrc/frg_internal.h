@@ -43,6 +43,8 @@ __host__ __device__ inline long long diag_index(const DiagGeom& g, int r, int c)
 // device: this sets it once per (kernel, current device) pair, so a process that
 // launches on several GPUs gets it on each of them.  Thread-safe.
 cudaError_t ensure_max_dyn_smem(const void* kernel, int bytes);
+// Allows clusters of more than 8 CTAs for `kernel` on the current device (once).
+cudaError_t ensure_nonportable_clusters(const void* kernel);
 
 // Kernel launchers (frg_kernels.cu).  All enqueue on `st` and return the
 // launch status; none synchronises.

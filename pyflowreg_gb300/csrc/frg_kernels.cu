@@ -33,6 +33,21 @@ cudaError_t ensure_max_dyn_smem(const void* kernel, int bytes)
     return e;
 }
 
+cudaError_t ensure_nonportable_clusters(const void* kernel)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, bool> done;  // (kernel, device)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(kernel, dev);
+    if (done.count(key)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e == cudaSuccess) done[key] = true;
+    return e;
+}
+
 __constant__ float c_cubic[32 * 4];
 __constant__ float c_linear[32 * 2];
 

@@ -90,7 +90,8 @@ namespace {
 constexpr int kLane64 = 256;       // most rows (threads) per CTA
 constexpr int kG64 = kGMax;        // iterations pipelined per pass, as a template maximum
 constexpr int kSmem64 = 232448;    // 227 KB of dynamic shared memory per CTA
-constexpr int kMaxStrips64 = 8;    // portable cluster size
+constexpr int kMaxStrips64 = 16;   // cluster size (over 8: the non-portable opt-in)
+constexpr int kPortableStrips = 8;
 
 struct Sor64Args {
     const double* J;    // [6][K][D*P] per frame, order J11, J22, J33, J12, J13, J23
@@ -493,6 +494,10 @@ cudaError_t run_chain64_t(const Sor64Args& A, const Chain64Table& T, int n_frame
         k_sor_chain64<K, CO, false, NTM><<<n_frames, nt, smem, st>>>(A, T);
         return cudaGetLastError();
     } else {
+        if (A.nc > kPortableStrips) {
+            const cudaError_t e2 = ensure_nonportable_clusters((const void*)k_sor_chain64<K, CO, true, NTM>);
+            if (e2 != cudaSuccess) return e2;
+        }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(n_frames * A.nc));
         cfg.blockDim = dim3((unsigned)nt);
@@ -539,6 +544,9 @@ bool sor_chain64_rows_ok(const DiagGeom& g, int rows)
 
 int sor_chain64_default_rows(const DiagGeom& g, int n_frames, int n_sms)
 {
+    // levels over 512 rows: 128-row strips (three CTAs per SM) while the cluster
+    // stays within 16 CTAs
+    if (g.P > 512 && sor_chain64_rows_ok(g, 128)) return 128;
     // the tallest strips that still give every SM work; shorter strips where a
     // batch of few frames would leave SMs idle (one frame per call: 8 strips)
     for (int rows = kLane64; rows >= 64; rows /= 2) {
@@ -558,7 +566,8 @@ bool sor_chain64_supports(int K, const DiagGeom& g, int n_passes)
     split64(g, kLane64, &nc, &nt);
     // 32-bit offsets within a frame: the largest plane index read is (6K + 2) planes of D * P
     const long long plane = (long long)g.D * g.P;
-    return nc <= kMaxStrips64 && plane * (6 * K + 2) < 0x7fffffffLL && chain64_smem(nt) <= (size_t)kSmem64;
+    // the tallest strips must fit a portable cluster: the fallback of a refused larger cluster
+    return nc <= kPortableStrips && plane * (6 * K + 2) < 0x7fffffffLL && chain64_smem(nt) <= (size_t)kSmem64;
 }
 
 cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W, long long W_fs, const double* lap,
@@ -612,13 +621,24 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
         A.a_data[k] = k < K ? a_data[k] : 0.0;
         A.a_m1[k] = k < K ? a_data[k] - 1.0 : 0.0;
     }
-    A.nc = nc;
-    switch (K) {
-        case 1: return run_chain64<1>(A, T, co, n_frames, nt, st);
-        case 2: return run_chain64<2>(A, T, co, n_frames, nt, st);
-        case 3: return run_chain64<3>(A, T, co, n_frames, nt, st);
-        default: return run_chain64<4>(A, T, co, n_frames, nt, st);
+    auto launch = [&](int nc_, int nt_) {
+        A.nc = nc_;
+        switch (K) {
+            case 1: return run_chain64<1>(A, T, co, n_frames, nt_, st);
+            case 2: return run_chain64<2>(A, T, co, n_frames, nt_, st);
+            case 3: return run_chain64<3>(A, T, co, n_frames, nt_, st);
+            default: return run_chain64<4>(A, T, co, n_frames, nt_, st);
+        }
+    };
+    cudaError_t e = launch(nc, nt);
+    if (e != cudaSuccess && nc > kPortableStrips) {
+        // a device that cannot schedule a cluster this large refuses the launch (nothing ran, the
+        // error is not sticky): the tallest strips give the same bits with at most 8 CTAs
+        cudaGetLastError();
+        split64(g, kLane64, &nc, &nt);
+        e = launch(nc, nt);
     }
+    return e;
 }
 
 }  // namespace frg

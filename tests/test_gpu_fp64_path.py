@@ -1,7 +1,8 @@
 """The float64 path's launch choices do not change its results: every strip
 height of the float64 chained SOR (256, 128 or 64 rows per CTA, levels over
-the strip height as clusters of strips) gives the same bits, and the plan's
-automatic choice agrees with each explicit one."""
+the strip height as clusters of strips, up to 16 CTAs for levels over 1024
+rows in 128-row strips) gives the same bits, and the plan's automatic choice
+agrees with each explicit one."""
 import numpy as np
 import pytest
 import torch
@@ -20,7 +21,7 @@ def _frames(H, W, K, n, seed):
     return preprocess_torch(ref_raw, ref_raw).contiguous(), preprocess_torch(raw[4:], ref_raw).contiguous()
 
 
-@pytest.mark.parametrize("H,W,K", [(300, 96, 2), (160, 144, 1)])
+@pytest.mark.parametrize("H,W,K", [(300, 96, 2), (160, 144, 1), (1100, 48, 1), (1700, 40, 2)])
 def test_strip_heights_give_identical_flows(H, W, K):
     from pyflowreg_gb300 import api
 
