@@ -308,7 +308,8 @@ def test_plan_rejects_out_of_order_backward():
 def test_auto_checkpoint_keeps_sweeps_when_they_fit():
     """checkpoint="auto" keeps every half-sweep (the faster backward) when the
     checkpoints fit in half the free device memory, which a small plan does;
-    its gradients are those of an explicit "sweeps" plan."""
+    its gradients are those of an explicit "sweeps" plan (to the rounding of
+    the warp adjoint's atomic scatter, whose order varies from run to run)."""
     from pyflowreg_gb300.diff import flow
 
     K, h, w = 1, 40, 36
@@ -321,4 +322,5 @@ def test_auto_checkpoint_keeps_sweeps_when_they_fit():
         m_t = torch.tensor(moving, device=dev, requires_grad=True)
         flow(torch.tensor(fixed, device=dev), m_t, torch.tensor(1.5), plan).pow(2).sum().backward()
         grads[ckpt] = m_t.grad.cpu()
-    assert torch.equal(grads["auto"], grads["sweeps"])
+    scale = float(grads["sweeps"].abs().max())
+    assert float((grads["auto"] - grads["sweeps"]).abs().max()) <= 1e-12 * scale
