@@ -144,6 +144,11 @@ __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ 
                         const double* __restrict__ v, long long uv_fs, int K, int h, int w, double h_col,
                         double h_row, float* __restrict__ out)
 {
+    // the table is read per lane at the lane's own sub-pixel position: copied into shared
+    // memory first (constant memory serialises a warp's distinct addresses)
+    __shared__ float s_tab[32 * 4];
+    for (int i = threadIdx.x; i < 32 * 4; i += blockDim.x) s_tab[i] = cx_cubic[i];
+    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     const int f = blockIdx.z;
@@ -154,29 +159,38 @@ __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ 
     const float mx = (float)dadd((double)x, ddiv(u[f * uv_fs + o], h_col));
     const float my = (float)dadd((double)y, ddiv(v[f * uv_fs + o], h_row));
     const bool oob = (mx < 0.0f) || (mx >= (float)w) || (my < 0.0f) || (my >= (float)h);
+    if (oob) {
+        for (int k = 0; k < K; ++k)
+            out[((long long)f * K + k) * hw + (long long)y * w + x] = f1[(long long)k * hw + (long long)y * w + x];
+        return;
+    }
+    const float cx = fminf(fmaxf(mx, 0.0f), (float)(w - 1));
+    const float cy = fminf(fmaxf(my, 0.0f), (float)(h - 1));
+    const int X = __float2int_rn(cx * 32.0f), Y = __float2int_rn(cy * 32.0f);
+    const int ix = X >> 5, fx = X & 31, iy = Y >> 5, fy = Y & 31;
+    // the 16 weights (float products, exact in double) and the tap offsets, once for all channels
+    double w2[4][4];
+    long long ro[4];
+    int co[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float wyi = s_tab[fy * 4 + i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) w2[i][j] = f2d(__fmul_rn(wyi, s_tab[fx * 4 + j]));
+        ro[i] = (long long)xclamp(iy - 1 + i, 0, h - 1) * w;
+        co[i] = xclamp(ix - 1 + i, 0, w - 1);
+    }
     for (int k = 0; k < K; ++k) {
-        float* dst = out + ((long long)f * K + k) * hw + (long long)y * w + x;
-        if (oob) {
-            *dst = f1[(long long)k * hw + (long long)y * w + x];
-            continue;
-        }
-        const float cx = fminf(fmaxf(mx, 0.0f), (float)(w - 1));
-        const float cy = fminf(fmaxf(my, 0.0f), (float)(h - 1));
-        const int X = __float2int_rn(cx * 32.0f), Y = __float2int_rn(cy * 32.0f);
-        const int ix = X >> 5, fx = X & 31, iy = Y >> 5, fy = Y & 31;
         const float* src = f2 + ((long long)f * K + k) * hw;
         double acc = 0.0;
-        for (int i = 0; i < 4; ++i) {
-            const int yy = xclamp(iy - 1 + i, 0, h - 1);
-            for (int j = 0; j < 4; ++j) {
-                const int xx = xclamp(ix - 1 + j, 0, w - 1);
-                const float w2 = __fmul_rn(cx_cubic[fy * 4 + i], cx_cubic[fx * 4 + j]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
                 // the product of two floats is exact in double, so the fused form rounds as
                 // dadd(acc, dmul(...)) does
-                acc = __fma_rn(f2d(src[(long long)yy * w + xx]), f2d(w2), acc);
-            }
-        }
-        *dst = (float)acc;
+                acc = __fma_rn(f2d(src[ro[i] + co[j]]), w2[i][j], acc);
+        out[((long long)f * K + k) * hw + (long long)y * w + x] = (float)acc;
     }
 }
 

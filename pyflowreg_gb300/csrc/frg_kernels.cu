@@ -246,9 +246,16 @@ cudaError_t launch_resize_v(const float* src, int n_frames, int n_planes, int ih
 // 1/32-pixel grid of cv2.remap (round half to even) with Keys A = -0.75
 // bicubic or bilinear weights and replicated borders.
 // ---------------------------------------------------------------------------
+// The interpolation tables are read per lane at the lane's own sub-pixel
+// position, so they are copied into shared memory first (constant memory
+// serialises a warp's distinct addresses); the 4 x 4 weights of a pixel are
+// formed once for all channels.
 __global__ void k_warp(View f2, View f1, View u, View v, int K, int h, int w, float h_col, float h_row,
                        int cubic, ViewW out)
 {
+    __shared__ float s_tab[32 * 4];
+    for (int i = threadIdx.x; i < 32 * 4; i += blockDim.x) s_tab[i] = cubic ? c_cubic[i] : (i < 64 ? c_linear[i] : 0.0f);
+    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     const int f = blockIdx.z;
@@ -270,33 +277,46 @@ __global__ void k_warp(View f2, View f1, View u, View v, int K, int h, int w, fl
     const int Y = __float2int_rn(cy * 32.0f);
     const int ix = X >> 5, fx = X & 31;
     const int iy = Y >> 5, fy = Y & 31;
-    for (int k = 0; k < K; ++k) {
-        const float* src = f2.p + f * f2.fs + k * f2.ps;
-        float acc = 0.0f;
-        if (cubic) {
+    if (cubic) {
+        float w2[4][4];
+        long long ro[4], co[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float* row = src + (long long)clampi(iy - 1 + i, 0, h - 1) * f2.rs;
-                const float wyi = c_cubic[fy * 4 + i];
+        for (int i = 0; i < 4; ++i) {
+            const float wyi = s_tab[fy * 4 + i];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float w2 = __fmul_rn(wyi, c_cubic[fx * 4 + j]);
-                    acc = fmaf(row[(long long)clampi(ix - 1 + j, 0, w - 1) * f2.cs], w2, acc);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const float* row = src + (long long)clampi(iy + i, 0, h - 1) * f2.rs;
-                const float wyi = c_linear[fy * 2 + i];
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const float w2 = __fmul_rn(wyi, c_linear[fx * 2 + j]);
-                    acc = fmaf(row[(long long)clampi(ix + j, 0, w - 1) * f2.cs], w2, acc);
-                }
-            }
+            for (int j = 0; j < 4; ++j) w2[i][j] = __fmul_rn(wyi, s_tab[fx * 4 + j]);
+            ro[i] = (long long)clampi(iy - 1 + i, 0, h - 1) * f2.rs;
+            co[i] = (long long)clampi(ix - 1 + i, 0, w - 1) * f2.cs;
         }
-        out.p[f * out.fs + k * out.ps + (long long)y * out.rs + (long long)x * out.cs] = acc;
+        for (int k = 0; k < K; ++k) {
+            const float* src = f2.p + f * f2.fs + k * f2.ps;
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc = fmaf(src[ro[i] + co[j]], w2[i][j], acc);
+            out.p[f * out.fs + k * out.ps + (long long)y * out.rs + (long long)x * out.cs] = acc;
+        }
+    } else {
+        float w2[2][2];
+        long long ro[2], co[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const float wyi = s_tab[fy * 2 + i];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) w2[i][j] = __fmul_rn(wyi, s_tab[fx * 2 + j]);
+            ro[i] = (long long)clampi(iy + i, 0, h - 1) * f2.rs;
+            co[i] = (long long)clampi(ix + i, 0, w - 1) * f2.cs;
+        }
+        for (int k = 0; k < K; ++k) {
+            const float* src = f2.p + f * f2.fs + k * f2.ps;
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) acc = fmaf(src[ro[i] + co[j]], w2[i][j], acc);
+            out.p[f * out.fs + k * out.ps + (long long)y * out.rs + (long long)x * out.cs] = acc;
+        }
     }
 }
 
