@@ -620,10 +620,14 @@ __global__ void kx_sor(const double* __restrict__ J, const double* __restrict__ 
     const int nsteps = (h - 1) + (w - 1) + 2 * (iterations - 1) + 1;
     for (int s = 0; s < nsteps; ++s) {
         for (int r = threadIdx.x; r < h; r += blockDim.x) {
-            for (int t = 0; t < iterations; ++t) {
-                const int c = s - r - 2 * t;
-                if (c < 0) break;
-                if (c >= w) continue;
+            // the iterations whose column s - r - 2t lies in [0, w): t from ceil((s - r - w + 1) / 2)
+            // to floor((s - r) / 2), without visiting the others
+            const int sr = s - r;
+            if (sr < 0) continue;
+            const int t_lo = sr >= w ? (sr - w + 2) / 2 : 0;
+            const int t_hi = min(iterations - 1, sr / 2);
+            for (int t = t_lo; t <= t_hi; ++t) {
+                const int c = sr - 2 * t;
                 const long long o = (long long)(r + 1) * n + (c + 1);
                 const double duc = du[o], dvc = dv[o];
                 if (t == iterations - 1 && (r == 0 || r == h - 1 || c == 0 || c == w - 1))
@@ -836,10 +840,12 @@ __global__ void kx_sor_range(const double* __restrict__ J, const double* __restr
     const int nsteps = (h - 1) + (w - 1) + 2 * (nit - 1) + 1;
     for (int s = 0; s < nsteps; ++s) {
         for (int r = threadIdx.x; r < h; r += blockDim.x) {
-            for (int tl = 0; tl < nit; ++tl) {
-                const int c = s - r - 2 * tl;
-                if (c < 0) break;
-                if (c >= w) continue;
+            const int sr = s - r;
+            if (sr < 0) continue;
+            const int t_lo = sr >= w ? (sr - w + 2) / 2 : 0;
+            const int t_hi = min(nit - 1, sr / 2);
+            for (int tl = t_lo; tl <= t_hi; ++tl) {
+                const int c = sr - 2 * tl;
                 const long long o = (long long)(r + 1) * n + (c + 1);
                 const double duc = du[o], dvc = dv[o];
                 if (tl == nit - 1) {
