@@ -242,6 +242,21 @@ def test_many_channels_generic_path(oracle):
     assert mx <= 2 * env_max and ep <= 2 * env_epe, (mx, ep, env_max, env_epe)
 
 
+@pytest.mark.parametrize("K", [3, 4])
+def test_fp64_three_and_four_channels(oracle, K):
+    """K = 3 and 4 run the float64 chained SOR's largest instantiations (their
+    fold inputs spill a few registers): parity with the oracle, per-channel
+    weights included."""
+    rng = np.random.default_rng(10 + K)
+    fixed, moving, _ = pair_256(3 + K, h=70, w=58)
+    fk = np.stack([fixed * (1 + 0.2 * k) for k in range(K)], axis=2)
+    mk = (np.stack([moving * (1 + 0.2 * k) for k in range(K)], axis=2)
+          + 0.001 * rng.standard_normal((70, 58, K))).astype(np.float32)
+    weight = np.linspace(1.0, 2.0, K)
+    kw = dict(alpha=(1.5, 1.5), iterations=25, weight=weight)
+    assert_parity(G.get_displacement(fk, mk, precision="fp64", **kw), oracle.get_displacement(fk, mk, **kw))
+
+
 def test_deterministic():
     fixed, moving, _ = pair_256(6, h=128, w=128)
     a = G.get_displacement(fixed, moving, alpha=(1.5, 1.5))
