@@ -18,6 +18,7 @@ in one call.  There is no CPU fallback: without a CUDA device these raise.
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
 from typing import Optional
 
@@ -601,6 +602,37 @@ def _host_io(plan, key, H, W, K, frames, fp64, dev):
     return io
 
 
+_copy_pool = None
+_copy_pool_lock = threading.Lock()
+
+
+def _host_copy(dst: np.ndarray, src: np.ndarray) -> None:
+    """dst[...] = src for large frame stacks, split over host threads along the
+    first axis (numpy releases the GIL while it copies), so pinned staging
+    keeps up with the transfers."""
+    global _copy_pool
+    n = dst.shape[0]
+    if n < 8 or dst.nbytes < (64 << 20):
+        dst[...] = src
+        return
+    with _copy_pool_lock:
+        if _copy_pool is None:
+            from concurrent.futures import ThreadPoolExecutor
+
+            _copy_pool = ThreadPoolExecutor(max_workers=max(1, min(8, (os.cpu_count() or 1))))
+        pool = _copy_pool
+    parts = min(pool._max_workers, n)
+    step = -(-n // parts)
+
+    def part(i):
+        a, b = i * step, min(n, (i + 1) * step)
+        if a < b:
+            dst[a:b] = src[a:b]
+
+    for f in [pool.submit(part, i) for i in range(parts)]:
+        f.result()
+
+
 def _run_host(params, fixed, moving, weight, uv, max_frames=None):
     """Host arrays in, host array out.  The batch goes to the plan's lanes in
     contiguous parts; each part is copied into pinned memory, uploaded on a
@@ -643,7 +675,7 @@ def _run_host(params, fixed, moving, weight, uv, max_frames=None):
     def drain(li):
         io, a, b = pending.pop(li)
         io.down_done.synchronize()
-        out[a:b] = io.pin_out[:b - a].numpy()
+        _host_copy(out[a:b], io.pin_out[:b - a].numpy())
 
     for pi, (t0, t1) in enumerate(parts):
         li = pi % len(lanes)
@@ -653,7 +685,7 @@ def _run_host(params, fixed, moving, weight, uv, max_frames=None):
         if io.up_done is not None:
             io.up_done.synchronize()
         k = t1 - t0
-        io.pin_in[:k].numpy()[...] = mov[t0:t1]
+        _host_copy(io.pin_in[:k].numpy(), mov[t0:t1])
         ls = streams[li]
         with torch.cuda.stream(st_up):
             io.dev_in[:k].copy_(io.pin_in[:k], non_blocking=True)
