@@ -1008,35 +1008,105 @@ __device__ __forceinline__ void dswap(double& x, double& y)
     y = hi;
 }
 
-__device__ double median25d(double v[25])
+__device__ __forceinline__ void uswap(unsigned& x, unsigned& y)
 {
-    double t[14];
+    const unsigned lo = min(x, y), hi = max(x, y);
+    x = lo;
+    y = hi;
+}
+
+// The 13th smallest of 25 values: forgetful selection (keep 14 candidates,
+// repeatedly drop the minimum and the maximum and admit the next value; the
+// middle of the last three is the median).
+template <class T>
+__device__ __forceinline__ T median25_net(const T v[25])
+{
+    T t[14];
 #pragma unroll
     for (int i = 0; i < 14; ++i) t[i] = v[i];
 #pragma unroll
     for (int round = 0; round < 11; ++round) {
         const int lo = round;
 #pragma unroll
-        for (int i = lo + 1; i < 14; ++i) dswap(t[lo], t[i]);
+        for (int i = lo + 1; i < 14; ++i) {
+            if constexpr (sizeof(T) == 8) dswap(t[lo], t[i]);
+            else uswap(t[lo], t[i]);
+        }
 #pragma unroll
-        for (int i = lo + 1; i < 13; ++i) dswap(t[i], t[13]);
+        for (int i = lo + 1; i < 13; ++i) {
+            if constexpr (sizeof(T) == 8) dswap(t[i], t[13]);
+            else uswap(t[i], t[13]);
+        }
         t[13] = v[14 + round];
     }
-    dswap(t[11], t[12]);
-    dswap(t[12], t[13]);
-    dswap(t[11], t[12]);
+    if constexpr (sizeof(T) == 8) {
+        dswap(t[11], t[12]);
+        dswap(t[12], t[13]);
+        dswap(t[11], t[12]);
+    } else {
+        uswap(t[11], t[12]);
+        uswap(t[12], t[13]);
+        uswap(t[11], t[12]);
+    }
     return t[12];
 }
 
-// The same median with the comparisons on the float32 pipe.  The high word of
-// a double (sign, exponent, top 20 bits of the fraction), read as a float,
-// orders like the double itself as long as it is a finite float (|x| < 2^1017):
-// both are sign-magnitude encodings with the magnitude bits in significance
-// order.  The 13th smallest key is found by the selection network of
-// median25d on floats; if exactly one value carries it, that value is the
-// median.  When several values share the key (values equal in their top 20
-// fraction bits), or a key is not finite, median25d decides in float64.
+__device__ double median25d(double v[25]) { return median25_net<double>(v); }
+
+// The same median with the comparisons on the float32 and integer pipes.  The
+// high word of a double (sign, exponent, top 20 bits of the fraction), read as
+// a float, orders like the double itself as long as it is a finite float
+// (|x| < 2^1017): both are sign-magnitude encodings with the magnitude bits in
+// significance order.  The 13th smallest key km is found by the selection
+// network on floats; if exactly one value carries it, that value is the
+// median.  Several values carry km when they agree in their top 20 fraction
+// bits, which smooth flow fields make common; median25_tie then decides from
+// the low words.  A key that is not a finite float, or km = 0 (the keys of +0
+// and -0 compare equal with different high words), leaves the decision to
+// median25d on the doubles.
 __device__ __forceinline__ float hikey(double x) { return __int_as_float(__double2hiint(x)); }
+
+// The median of 25 doubles (get(i), i < 25) whose 13th smallest key km (finite,
+// non-zero) is carried by eq > 1 of them, nlt keys being smaller.  A finite
+// non-zero float equals only its own bit pattern, so the values that carry km
+// share their high word and with it their sign, and their low words order them:
+// ascending for a positive km, descending for a negative one.  With the low
+// word complemented for a negative km, the tie key t (0 below km, the low word
+// at km, ~0 above) is non-decreasing in the values' order, so the 13th smallest
+// t is the median's low word.  It is the smallest tied t when the median is the
+// first tied value in order (r = 12 - nlt = 0), the largest when it is the last
+// (r = eq - 1: every two-way tie is one of the two), and otherwise the 25-value
+// selection on the tie keys, on the integer pipe.
+template <class Get>
+__device__ __forceinline__ double median25_tie(Get get, float km, int nlt, int eq)
+{
+    const unsigned s = (__float_as_uint(km) >> 31) ? 0xffffffffu : 0u;
+    const int r = 12 - nlt;
+    unsigned tm;
+    if (r == 0 || r == eq - 1) {
+        unsigned tmin = 0xffffffffu, tmax = 0u;
+#pragma unroll
+        for (int i = 0; i < 25; ++i) {
+            const double x = get(i);
+            if (hikey(x) == km) {
+                const unsigned t = (unsigned)__double2loint(x) ^ s;
+                tmin = min(tmin, t);
+                tmax = max(tmax, t);
+            }
+        }
+        tm = r == 0 ? tmin : tmax;
+    } else {
+        unsigned t[25];
+#pragma unroll
+        for (int i = 0; i < 25; ++i) {
+            const double x = get(i);
+            const float k = hikey(x);
+            t[i] = k < km ? 0u : (k > km ? 0xffffffffu : (unsigned)__double2loint(x) ^ s);
+        }
+        tm = median25_net<unsigned>(t);
+    }
+    return __hiloint2double(__float_as_int(km), (int)(tm ^ s));
+}
 
 __device__ __forceinline__ void fswap(float& x, float& y)
 {
@@ -1068,27 +1138,32 @@ __device__ double median25_keys(double v[25])
     fswap(t[12], t[13]);
     fswap(t[11], t[12]);
     const float m = t[12];
-    int eq = 0;
+    int eq = 0, nlt = 0;
     double pick = 0.0;
 #pragma unroll
     for (int i = 0; i < 25; ++i) {
-        if (hikey(v[i]) == m) {
+        const float k = hikey(v[i]);
+        nlt += k < m;
+        if (k == m) {
             ++eq;
             pick = v[i];
         }
     }
     if (finite && eq == 1) return pick;
+    if (finite && m != 0.0f) return median25_tie([&](int i) { return v[i]; }, m, nlt, eq);
     return median25d(v);
 }
 
-// Median + accumulate on the padded float64 du, dv ((T, h + 2, w + 2) with
-// the level's edge ring), exact like median25_keys: a 32 x 16 output tile with
-// its mirrored 2-pixel halo is staged in shared memory as the doubles and
-// their float keys (high words); each thread takes two vertically adjacent
-// pixels, whose windows share four of their five rows, and median25_pair
-// finds both windows' 13th smallest keys on the float pipe.  A key carried by
-// exactly one value of its window names the median; when several values share
-// it, or a key is not a finite float, median25d decides from the doubles.
+// Median + accumulate on float64 du, dv (the interiors of the padded level
+// planes: du[y * s_rs + x], frames s_fs apart), exact like median25_keys: a
+// 32 x 16 output tile with its mirrored 2-pixel halo is staged in shared
+// memory as the doubles and their float keys (high words); each thread takes
+// two vertically adjacent pixels, whose windows share four of their five rows,
+// and median25_pair finds both windows' 13th smallest keys on the float pipe.
+// A key carried by exactly one value of its window names the median; several
+// values carrying it go to median25_tie (integer pipe), and a key that is not a
+// finite float, or a zero key, to median25d.  Writes u + median(du) (u, v the
+// padded planes, frames uv_fs apart), or the median itself when u is null.
 // Needs h, w >= 3 when do_median.
 constexpr int kXMedTx = 32, kXMedTy = 8, kXMedRows = 2 * kXMedTy;
 
@@ -1100,8 +1175,8 @@ __device__ __forceinline__ int mirror_x(int i, int n)
 }
 
 __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* __restrict__ du,
-                                                                 const double* __restrict__ dv,
-                                                                 const double* __restrict__ u,
+                                                                 const double* __restrict__ dv, long long s_fs,
+                                                                 long long s_rs, const double* __restrict__ u,
                                                                  const double* __restrict__ v, long long uv_fs, int h,
                                                                  int w, int do_median, double* ou, double* ov,
                                                                  long long o_fs, long long o_rs, long long o_cs)
@@ -1112,15 +1187,14 @@ __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* 
     const int x0 = blockIdx.x * kXMedTx, y0 = blockIdx.y * kXMedRows;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * kXMedTx + tx;
-    const long long n = w + 2, mn = (long long)(h + 2) * n;
-    const double* duf = du + (long long)f * mn;
-    const double* dvf = dv + (long long)f * mn;
+    const double* duf = du + (long long)f * s_fs;
+    const double* dvf = dv + (long long)f * s_fs;
     if (do_median) {
         for (int i = tid; i < (kXMedRows + 4) * (kXMedTx + 4); i += kXMedTx * kXMedTy) {
             const int r = i / (kXMedTx + 4), c = i - r * (kXMedTx + 4);
             const int yy = mirror_x(min(y0 - 2 + r, h + 1), h);
             const int xx = mirror_x(min(x0 - 2 + c, w + 1), w);
-            const long long o = (long long)(yy + 1) * n + xx + 1;
+            const long long o = (long long)yy * s_rs + xx;
             const double a = duf[o], b = dvf[o];
             sd[0][r][c] = a;
             sd[1][r][c] = b;
@@ -1150,7 +1224,7 @@ __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* 
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 const int r0 = 2 * ty + q;
-                int eq = 0;
+                int eq = 0, nlt = 0;
                 bool finite = true;
                 double pick = 0.0;
 #pragma unroll
@@ -1159,18 +1233,23 @@ __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* 
                     for (int dx = 0; dx < 5; ++dx) {
                         const float k = sk[pl][r0 + dy][tx + dx];
                         finite = finite && fabsf(k) <= 3.402823466e38f;
+                        nlt += k < km[q];
                         if (k == km[q]) {
                             ++eq;
                             pick = sd[pl][r0 + dy][tx + dx];
                         }
                     }
                 if (!(finite && eq == 1)) {
-                    double win[25];
+                    if (finite && km[q] != 0.0f) {
+                        pick = median25_tie([&](int i) { return sd[pl][r0 + i / 5][tx + i % 5]; }, km[q], nlt, eq);
+                    } else {
+                        double win[25];
 #pragma unroll
-                    for (int dy = 0; dy < 5; ++dy)
+                        for (int dy = 0; dy < 5; ++dy)
 #pragma unroll
-                        for (int dx = 0; dx < 5; ++dx) win[dy * 5 + dx] = sd[pl][r0 + dy][tx + dx];
-                    pick = median25d(win);
+                            for (int dx = 0; dx < 5; ++dx) win[dy * 5 + dx] = sd[pl][r0 + dy][tx + dx];
+                        pick = median25d(win);
+                    }
                 }
                 m[q][pl] = pick;
             }
@@ -1179,47 +1258,27 @@ __global__ void __launch_bounds__(kXMedTx * kXMedTy) kx_median_rm(const double* 
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const int y = ya + q < h ? ya + q : ya;
-            const long long o = (long long)(y + 1) * n + x + 1;
+            const long long o = (long long)y * s_rs + x;
             m[q][0] = duf[o];
             m[q][1] = dvf[o];
         }
     }
+    const long long n = w + 2;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int y = ya + q;
         if (y >= h) break;
         const long long oc = (long long)(y + 1) * n + x + 1;
-        ou[f * o_fs + y * o_rs + x * o_cs] = dadd(u[f * uv_fs + oc], m[q][0]);
-        ov[f * o_fs + y * o_rs + x * o_cs] = dadd(v[f * uv_fs + oc], m[q][1]);
+        ou[f * o_fs + y * o_rs + x * o_cs] = u ? dadd(u[f * uv_fs + oc], m[q][0]) : m[q][0];
+        ov[f * o_fs + y * o_rs + x * o_cs] = v ? dadd(v[f * uv_fs + oc], m[q][1]) : m[q][1];
     }
-}
-
-// 5x5 median (scipy "mirror") of one float64 plane (h, w), h, w >= 3.
-__global__ void kx_median5_plane(const double* __restrict__ src, int h, int w, double* __restrict__ dst)
-{
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
-    if (x >= w) return;
-    double a[25];
-    int q = 0;
-    for (int dy = -2; dy <= 2; ++dy) {
-        int yy = y + dy;
-        if (yy < 0) yy = -yy;
-        if (yy >= h) yy = 2 * (h - 1) - yy;
-        for (int dx = -2; dx <= 2; ++dx) {
-            int xx = x + dx;
-            if (xx < 0) xx = -xx;
-            if (xx >= w) xx = 2 * (w - 1) - xx;
-            a[q++] = src[(long long)yy * w + xx];
-        }
-    }
-    dst[(long long)y * w + x] = median25_keys(a);
 }
 
 cudaError_t launch_x_median5_plane(const double* src, int h, int w, double* dst, cudaStream_t st)
 {
-    dim3 blk(128), grd((w + 127) / 128, h);
-    kx_median5_plane<<<grd, blk, 0, st>>>(src, h, w, dst);
+    dim3 blk(kXMedTx, kXMedTy), grd((w + kXMedTx - 1) / kXMedTx, (h + kXMedRows - 1) / kXMedRows, 1);
+    const long long hw = (long long)h * w;
+    kx_median_rm<<<grd, blk, 0, st>>>(src, src, hw, w, nullptr, nullptr, 0, h, w, 1, dst, dst, hw, w, 1);
     return cudaGetLastError();
 }
 
@@ -1229,7 +1288,9 @@ cudaError_t launch_x_median_accum(const double* du, const double* dv, const doub
 {
     if (n_frames > 65535) return cudaErrorInvalidValue;
     dim3 blk(kXMedTx, kXMedTy), grd((w + kXMedTx - 1) / kXMedTx, (h + kXMedRows - 1) / kXMedRows, n_frames);
-    kx_median_rm<<<grd, blk, 0, st>>>(du, dv, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs, o_cs);
+    const long long n = w + 2, mn = (long long)(h + 2) * n;
+    kx_median_rm<<<grd, blk, 0, st>>>(du + n + 1, dv + n + 1, mn, n, u, v, uv_fs, h, w, do_median, ou, ov, o_fs, o_rs,
+                                      o_cs);
     return cudaGetLastError();
 }
 

@@ -206,8 +206,8 @@ cudaError_t launch_cubic_up(const T* src, int n_frames, int n_planes, int ih, in
 cudaError_t launch_x_median_accum(const double* du, const double* dv, const double* u, const double* v,
                                   long long uv_fs, int n_frames, int h, int w, int do_median, double* ou, double* ov,
                                   long long o_fs, long long o_rs, long long o_cs, cudaStream_t st);
-// 5x5 median (mirror) of one float64 plane (h, w), h, w >= 3 (the selection of
-// launch_x_median_accum).
+// 5x5 median (mirror) of one float64 plane (h, w), h, w >= 3, by the kernel of
+// launch_x_median_accum.
 cudaError_t launch_x_median5_plane(const double* src, int h, int w, double* dst, cudaStream_t st);
 // One GNC warping step's state update (two kernels, the second only when
 // write_ring): (ou, ov) = [median5](u + du) interiors, then the padded u, v

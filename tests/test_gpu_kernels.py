@@ -94,6 +94,14 @@ def test_median_f64_exact(h, w):
 
     rng = np.random.default_rng(h * 1000 + w)
     a = rng.standard_normal((h, w))
+    # a smooth ramp (values 1e-7 apart share their top 20 fraction bits, as in a
+    # smooth flow field), positive on the left half, negative on the right
+    yy, xx = np.mgrid[:h, :w]
+    ramp = 0.3 + 1e-7 * (yy * 3 + xx) + 2.0 ** -44 * rng.integers(0, 64, (h, w))
+    a[: h // 2 + 1] = np.where(xx < w // 2, ramp, -ramp)[: h // 2 + 1]
+    # blocks whose values all share one high word (every tie rank occurs)
+    a[-4:, : w // 3] = 1.7 * (1 + 2.0 ** -45 * rng.integers(-40, 40, a[-4:, : w // 3].shape))
+    a[-4:, -(w // 3):] = -1.7 * (1 + 2.0 ** -45 * rng.integers(-40, 40, a[-4:, -(w // 3):].shape))
     a[::3, ::2] = a[0, 0]                                   # exact ties
     a[1::4, 1::3] = a[1, 1] * (1 + 2.0 ** -40 * rng.integers(-3, 4, a[1::4, 1::3].shape))  # same top bits
     a[2::5, ::4] = 0.0
