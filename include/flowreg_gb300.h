@@ -255,6 +255,17 @@ int frg_median5_f64(int h, int w, const double* src, double* dst, void* stream);
  * own. */
 int frg_pow_f64(long long n, const double* x, double b, double* out, void* stream);
 
+/* Page-locks (cudaHostRegister, default flags) or releases host memory that
+ * asynchronous device-to-host copies of flows write into: the batch call's
+ * output array, so that the last parts of a batch are read back by one copy
+ * each instead of through a pinned staging buffer.  Host-side I/O of the batch
+ * form (motion_correction/parallelization/base.py:76-110 hands the executor
+ * host arrays); it replaces no reference function.  A refused registration
+ * returns FRG_ECUDA (frg_last_error says why) and leaves no pending CUDA error
+ * behind for later launches. */
+int frg_host_register(void* ptr, long long bytes);
+int frg_host_unregister(void* ptr);
+
 /* Preprocessing of frames before the flow, as compensate_recording does it
  * (motion_correction/compensate_recording.py:521-561, normalize and
  * apply_gaussian_filter in util/image_processing.py:12-165): out =

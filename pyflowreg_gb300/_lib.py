@@ -110,6 +110,8 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_median5", I, [I, I, P, P, P])
         _sig(lib, "frg_median5_f64", I, [I, I, P, P, P])
         _sig(lib, "frg_pow_f64", I, [ctypes.c_longlong, P, D, P, P])
+        _sig(lib, "frg_host_register", I, [P, ctypes.c_longlong])
+        _sig(lib, "frg_host_unregister", I, [P])
         _sig(lib, "frg_preprocess", I, [I, I, I, I, P, pD, pD, P, pI, P, pI, P, pI, I, I, P, P, P])
         _sig(lib, "frg_preprocess_f64", I, [I, I, I, I, P, pD, pD, P, pI, P, pI, P, pI, I, P, P, P])
         _sig(lib, "frg_flow_post_workspace", S, [I, I, I])

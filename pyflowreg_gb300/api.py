@@ -590,8 +590,7 @@ class _HostIO:
         self.dev_out = torch.empty((frames, H, W, 2), dtype=odt, device=dev)
         self.pin_in = torch.empty((frames, H, W, K), dtype=torch.float32).pin_memory()
         self.pin_out = torch.empty((frames, H, W, 2), dtype=odt).pin_memory()
-        self.up_done = None    # event: pin_in consumed by the upload
-        self.down_done = None  # event: pin_out filled by the read-back
+        self.up_done = None  # event: pin_in consumed by the upload
 
 
 def _host_io(plan, key, H, W, K, frames, fp64, dev):
@@ -606,14 +605,15 @@ _copy_pool = None
 _copy_pool_lock = threading.Lock()
 
 
-def _host_copy(dst: np.ndarray, src: np.ndarray) -> None:
+def _host_copy(dst: np.ndarray, src) -> None:
     """dst[...] = src for large frame stacks, split over host threads along the
     first axis (numpy releases the GIL while it copies), so pinned staging
-    keeps up with the transfers."""
+    keeps up with the transfers.  src = None writes zeros: it touches fresh
+    pages of dst ahead of a later copy."""
     global _copy_pool
     n = dst.shape[0]
     if n < 8 or dst.nbytes < (64 << 20):
-        dst[...] = src
+        dst[...] = 0 if src is None else src
         return
     with _copy_pool_lock:
         if _copy_pool is None:
@@ -627,7 +627,7 @@ def _host_copy(dst: np.ndarray, src: np.ndarray) -> None:
     def part(i):
         a, b = i * step, min(n, (i + 1) * step)
         if a < b:
-            dst[a:b] = src[a:b]
+            dst[a:b] = 0 if src is None else src[a:b]
 
     for f in [pool.submit(part, i) for i in range(parts)]:
         f.result()
@@ -636,9 +636,11 @@ def _host_copy(dst: np.ndarray, src: np.ndarray) -> None:
 def _run_host(params, fixed, moving, weight, uv, max_frames=None):
     """Host arrays in, host array out.  The batch goes to the plan's lanes in
     contiguous parts; each part is copied into pinned memory, uploaded on a
-    copy stream, registered on its lane's stream and read back on a second
-    copy stream, so the host copies and transfers of one part overlap the
-    device work of the others."""
+    copy stream and registered on its lane's stream, so the host copies and
+    transfers of one part overlap the device work of the others.  A part whose
+    lane takes another part is read back through pinned memory before the lane
+    moves on; the last part of every lane is read back straight into the output
+    array, which is page-locked for the copies while the lanes compute."""
     _require_cuda()
     T, m, n, K = moving.shape
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -673,8 +675,11 @@ def _run_host(params, fixed, moving, weight, uv, max_frames=None):
     mov = np.asarray(moving)
 
     def drain(li):
-        io, a, b = pending.pop(li)
-        io.down_done.synchronize()
+        io, a, b, done = pending.pop(li)
+        with torch.cuda.stream(st_down):
+            st_down.wait_event(done)
+            io.pin_out[:b - a].copy_(io.dev_out[:b - a], non_blocking=True)
+        st_down.synchronize()
         _host_copy(out[a:b], io.pin_out[:b - a].numpy())
 
     for pi, (t0, t1) in enumerate(parts):
@@ -696,15 +701,39 @@ def _run_host(params, fixed, moving, weight, uv, max_frames=None):
         lanes[li].displacement(io.dev_in[:k], uv_t, io.dev_out[:k], stream=ls)
         done = torch.cuda.Event()
         done.record(ls)
+        pending[li] = (io, t0, t1, done)
+    # the lanes' last parts: while they compute, the output rows they fill are first touched
+    # (page faults) and page-locked, so each is read back by one device-to-host copy
+    a0 = min(a for _, a, _, _ in pending.values())
+    tail = out[a0:]
+    _host_copy(tail, None)
+    locked = _page_lock(tail)
+    try:
         with torch.cuda.stream(st_down):
-            st_down.wait_event(done)
-            io.pin_out[:k].copy_(io.dev_out[:k], non_blocking=True)
-            io.down_done = torch.cuda.Event()
-            io.down_done.record(st_down)
-        pending[li] = (io, t0, t1)
-    for li in list(pending):
-        drain(li)
+            for io, a, b, done in pending.values():
+                st_down.wait_event(done)
+                if locked:
+                    torch.from_numpy(out[a:b]).copy_(io.dev_out[:b - a], non_blocking=True)
+                else:
+                    io.pin_out[:b - a].copy_(io.dev_out[:b - a], non_blocking=True)
+        st_down.synchronize()
+        if not locked:
+            for io, a, b, _ in pending.values():
+                _host_copy(out[a:b], io.pin_out[:b - a].numpy())
+    finally:
+        if locked:
+            _lib.check(_lib.load().frg_host_unregister(ctypes.c_void_p(tail.ctypes.data)), "frg_host_unregister")
+    pending.clear()
     return out
+
+
+def _page_lock(arr: np.ndarray) -> bool:
+    """Page-locks a host array of at least 64 MiB for asynchronous
+    device-to-host copies; False for a smaller array or when the runtime
+    refuses (the caller then copies through its pinned buffers)."""
+    if arr.nbytes < (64 << 20):
+        return False
+    return _lib.load().frg_host_register(ctypes.c_void_p(arr.ctypes.data), arr.nbytes) == 0
 
 
 def get_displacement_device(fixed_t, moving_t, uv_t=None, weight_t=None, out_t=None, stream=None,

@@ -1668,6 +1668,28 @@ int frg_median5(int h, int w, const float* src, float* dst, void* stream)
     return rc;
 }
 
+int frg_host_register(void* ptr, long long bytes)
+{
+    if (!ptr || bytes <= 0) return fail(FRG_EINVAL, "bad argument");
+    const cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // a refusal is reported here, not by the next launch
+        return fail(FRG_ECUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+    }
+    return FRG_OK;
+}
+
+int frg_host_unregister(void* ptr)
+{
+    if (!ptr) return fail(FRG_EINVAL, "bad argument");
+    const cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(FRG_ECUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
+    }
+    return FRG_OK;
+}
+
 int frg_median5_f64(int h, int w, const double* src, double* dst, void* stream)
 {
     if (!src || !dst || h < 3 || w < 3) return fail(FRG_EINVAL, "bad argument");

@@ -179,3 +179,24 @@ def test_lane_plan_equals_one_plan(T):
     assert torch.equal(lanes.displacement(fr), want)
     assert torch.equal(lanes.displacement(fr[:7]), want[:7])
     lanes.close()
+
+
+def test_host_batch_read_back_paths_equal_device_call():
+    """The host-array batch call reads a part back through pinned memory when its
+    lane takes another part, and the lanes' last parts (over 64 MiB here)
+    straight into the page-locked output array: both give the flows of the
+    device-resident call."""
+    import pyflowreg_gb300 as G
+    from pyflowreg_gb300 import api
+
+    key = (256, 256, 2)
+    ref, fr = _frames(key, 300, 21)
+    wt = np.full(key, 0.5)
+    want = G.get_displacement_device(ref, fr, None, torch.full(key, 0.5, device="cuda"), **OPTS).cpu().numpy()
+    api.clear_plans()
+    # a 128-frame plan runs two lanes of 64 frames: parts 0-2 are read back while
+    # their lane moves on, parts 3 and 4 (frames 192-299) into the locked output
+    got = G.get_displacement_batch(ref.cpu().numpy(), fr.cpu().numpy(), weight=wt, max_frames=128, **OPTS)
+    assert got.dtype == np.float64 and got[192:].nbytes >= 64 << 20
+    np.testing.assert_array_equal(got, want)
+    api.clear_plans()
