@@ -274,7 +274,7 @@ struct LevelPlan {
     float* ref = nullptr;    // (K, h, w) reference level
     float* wdiag = nullptr;  // (K, D*P) weight level, diagonal-major
     double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
-    double* wdiag64 = nullptr;  // (K, D*P) the same, diagonal-major, for the float64 chained SOR
+    double* wdiag64 = nullptr;  // (2, K, D*P) the same and times a_data, diagonal-major, for the float64 chained SOR
     double* ref64 = nullptr;    // (K, h, w) reference level in float64, for its tensor
     bool chain64 = false;       // fp64 plan: this level runs the float64 chained SOR
     int rows64 = 0;             // its rows per CTA strip (64, 128, 256); 0: chosen per call from the batch size
@@ -724,7 +724,7 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         if (rc) { frg_plan_destroy(pl); return rc; }
         L.chain64 = pl->dpath && sor_chain64_supports(channels, L.g, n_passes);
         if (L.chain64) {
-            if ((rc = dev_alloc(pl, &L.wdiag64, (size_t)channels * L.g.D * L.g.P)) ||
+            if ((rc = dev_alloc(pl, &L.wdiag64, (size_t)2 * channels * L.g.D * L.g.P)) ||
                 (rc = dev_alloc(pl, &L.ref64, (size_t)channels * L.h * L.w))) {
                 frg_plan_destroy(pl);
                 return rc;
@@ -993,7 +993,7 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
             FRG_LAUNCH(launch_x_resize_v_d(pl->tmp, 1, K, H, L.w, L.wpad64, 0, mn, L.w + 2, L.h, 2, L.img.iy,
                                            L.img.wy, L.img.P, st));
             if (L.chain64) {
-                FRG_LAUNCH(launch_x_pad_to_diag(L.wpad64, K, L.h, L.w, L.g, L.wdiag64, st));
+                FRG_LAUNCH(launch_x_pad_to_diag(L.wpad64, K, L.h, L.w, L.g, L.wdiag64, st, pl->a_data64));
                 FRG_LAUNCH(launch_x_to_double(L.ref, (long long)K * hw, L.ref64, st));
             }
         }

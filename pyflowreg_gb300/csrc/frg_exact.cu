@@ -491,9 +491,11 @@ __global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__
             tensor_px64(f1f, f2, f, K, k, h, w, r + 1, c + 1, hy, hx, f2_f32, 2, j);
         else
             tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
-        // the cross terms doubled (exact), as the solver's data residual uses them
+        // the cross terms doubled (exact), as the solver's data residual uses them, and
+        // J33 with the residual's offset 1e-5 added
 #pragma unroll
-        for (int q = 0; q < 6; ++q) Jf[((long long)q * K + k) * plane + di] = q < 3 ? j[q] : dadd(j[q], j[q]);
+        for (int q = 0; q < 6; ++q)
+            Jf[((long long)q * K + k) * plane + di] = q < 2 ? j[q] : (q == 2 ? dadd(j[2], 0.00001) : dadd(j[q], j[q]));
     }
     const long long n = w + 2;
     const double* uf = u + f * uv_fs;
@@ -951,21 +953,35 @@ cudaError_t launch_x_to_double(const float* src, long long n, double* dst, cudaS
     return cudaGetLastError();
 }
 
-// Padded (K, m*n) planes (the interior at (1, 1)) to diagonal-major (K, D*P).
-__global__ void kx_pad_to_diag(const double* __restrict__ src, int K, int h, int w, DiagGeom g, double* __restrict__ dst)
+// Padded (K, m*n) planes (the interior at (1, 1)) to diagonal-major (K, D*P);
+// with scale set, also the planes times scale[k] at dst + K*D*P.
+struct ChannelScale {
+    double s[kMaxK];
+};
+
+__global__ void kx_pad_to_diag(const double* __restrict__ src, int K, int h, int w, DiagGeom g, double* __restrict__ dst,
+                               ChannelScale sc, int scaled)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y;
     const int k = blockIdx.z;
     if (c >= w || k >= K) return;
     const long long n = w + 2, mn = (long long)(h + 2) * n;
-    dst[(long long)k * g.D * g.P + diag_index(g, r, c)] = src[k * mn + (long long)(r + 1) * n + c + 1];
+    const long long plane = (long long)g.D * g.P, di = diag_index(g, r, c);
+    const double v = src[k * mn + (long long)(r + 1) * n + c + 1];
+    dst[k * plane + di] = v;
+    if (scaled) dst[(K + k) * plane + di] = dmul(v, sc.s[k]);
 }
 
-cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st)
+cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st,
+                                 const double* scale)
 {
+    if (K < 1 || K > kMaxK) return cudaErrorInvalidValue;
+    ChannelScale sc = {};
+    if (scale)
+        for (int k = 0; k < K; ++k) sc.s[k] = scale[k];
     dim3 blk(128), grd((w + 127) / 128, h, K);
-    kx_pad_to_diag<<<grd, blk, 0, st>>>(src, K, h, w, g, dst);
+    kx_pad_to_diag<<<grd, blk, 0, st>>>(src, K, h, w, g, dst, sc, scale ? 1 : 0);
     return cudaGetLastError();
 }
 

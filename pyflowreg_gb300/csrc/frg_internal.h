@@ -123,8 +123,9 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
                              float* out_du = nullptr, float* out_dv = nullptr, long long out_fs = 0);
 // The chained SOR in float64 (frg_sor64.cu, k_sor_chain64): the schedule of
 // launch_sor_chain with float64 state, coefficients and arithmetic (the parity
-// precision).  J [6][K][D*P], W [K][D*P], lap [2][D*P], coef [5][D*P] and the
-// state du, dv [D*P] are diagonal-major doubles; the final pass writes du, dv
+// precision).  J [6][K][D*P] (J11, J22, J33 + 1e-5, 2 J12, 2 J13, 2 J23), W
+// [2][K][D*P] (W, then W * a_data), lap [2][D*P], coef [5][D*P] and the state
+// du, dv [D*P] are diagonal-major doubles; the final pass writes du, dv
 // at out + r * out_rs + c.  Levels of at most 2048 (padded) rows (over 256 as
 // clusters of row strips), K <= 4, w >= 3, at most kMaxChain passes of G <= kGMax.
 // rows: the most rows per CTA (64, 128 or 256; 0 = 256), the level split into at
@@ -172,9 +173,9 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
 // (T, 2, D*P) from the padded float64 u, v (frame stride uv_fs), for the
 // float64 chained SOR; f1 is the reference level in float64 (K, h, w), f1f the
 // same in float32 (the census data term, gray = 2, runs the reference-order
-// arithmetic of kx_tensor on it).  The planes hold J11, J22, J33, 2 J12, 2 J13,
-// 2 J23: the cross terms doubled (exact), as the solver's data residual uses
-// them.
+// arithmetic of kx_tensor on it).  The planes hold J11, J22, J33 + 1e-5, 2 J12,
+// 2 J13, 2 J23: the cross terms doubled (exact) and the offset of psi's argument
+// (E + 1e-5) added to J33, as the solver's data residual uses them.
 cudaError_t launch_x_tensor_diag(const double* f1, const float* f1f, const float* f2, int n_frames, int K, int h, int w,
                                  double hy, double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
                                  const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
@@ -195,7 +196,11 @@ cudaError_t launch_x_sor_smooth(const double* J, const double* W, const double* 
                                 cudaStream_t st, long long* launches);
 cudaError_t launch_x_to_float(const double* src, long long n, float* dst, cudaStream_t st);
 // Padded (K, (h+2)*(w+2)) float64 planes to diagonal-major (K, D*P).
-cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st);
+// Padded (K, h + 2, w + 2) float64 planes to diagonal-major (K, D*P) at dst;
+// with scale (K host values), also each plane times scale[k] at dst + K*D*P
+// (the float64 chained SOR's weights W and W * a_data).
+cudaError_t launch_x_pad_to_diag(const double* src, int K, int h, int w, DiagGeom g, double* dst, cudaStream_t st,
+                                 const double* scale = nullptr);
 cudaError_t launch_x_hwk_to_planes(const double* src, int n_arrays, long long mn, int K, double* dst, cudaStream_t st);
 // cv2.resize INTER_CUBIC of planar planes (n_frames * n_planes, ih, iw) to
 // (oh, ow): width pass into tmp, height pass into the strided dst view.

@@ -94,9 +94,9 @@ constexpr int kMaxStrips64 = 16;   // cluster size (over 8: the non-portable opt
 constexpr int kPortableStrips = 8;
 
 struct Sor64Args {
-    const double* J;    // [6][K][D*P] per frame, order J11, J22, J33, J12, J13, J23
+    const double* J;    // [6][K][D*P] per frame: J11, J22, J33 + 1e-5, 2 J12, 2 J13, 2 J23
     long long J_fs;
-    const double* W;    // [K][D*P] per frame (W_fs 0: shared by all frames)
+    const double* W;    // [2][K][D*P] per frame, W then W * a_data (W_fs 0: shared by all frames)
     long long W_fs;
     const double* lap;  // [2][D*P]: the u- and v-parts of the smoothness numerator from u, v
     long long lap_fs;
@@ -113,7 +113,6 @@ struct Sor64Args {
     double wa, wb;      // smoothness weights of the row neighbours (y) and the column neighbours (x)
     double wsum;        // ((wx + wx) + wy) + wy, the reference's order
     double omega, one_m_omega;
-    double a_data[kMaxK];
     double a_m1[kMaxK];  // a_data - 1
     int nc;              // row strips (CTAs) per frame
 };
@@ -176,7 +175,8 @@ __device__ __forceinline__ double omega_over(double omega, double den)
 // Coefficients of one pixel for a pass (core/level_solver.py:229-255, 309-364):
 // with psi at a tick from the pixel's pass-start du, dv (E in nested fused
 // multiply-adds; the reference adds J23 dv twice, hence 2 J23), psi = 1 on the
-// first pass, or the stored coefficients of the group's first pass.
+// first pass, or the stored coefficients of the group's first pass.  On a tick
+// W psi = (W a) (E + 1e-5)^(a - 1), with W a and J33 + 1e-5 stored per pixel.
 //   A12 = sum_k W psi J12,  BU = lap_u - sum_k W psi J13,  BV = lap_v - sum_k W psi J23,
 //   iDu = omega / (wsum + sum_k W psi J11) (0 when the denominator is 0), iDv likewise
 //   (omega times the reciprocal: within an ulp or two of the quotient).
@@ -201,16 +201,18 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldI
     for (int k = 0; k < K; ++k) {
         const double j11 = r.j[0 * K + k], j22 = r.j[1 * K + k], j33 = r.j[2 * K + k];
         const double j12 = r.j[3 * K + k], j13 = r.j[4 * K + k], j23 = r.j[5 * K + k];
-        double wp = r.w[k];
+        double wp = r.w[k];  // W, or W * a_data on a tick pass
         if (tick) {
             const double a = du, b = dv;
-            // E = a (J11 a + 2 J12 b + 2 J13) + b (J22 b + 2 J23) + J33: 5 float64 operations
+            // E + 1e-5 = a (J11 a + 2 J12 b + 2 J13) + b (J22 b + 2 J23) + (J33 + 1e-5):
+            // 5 float64 operations; max(E, 0) + 1e-5 as max(E + 1e-5, 1e-5), compared as
+            // 64-bit integers (the order of non-negative doubles; negative ones are below)
             double t = __fma_rn(j11, a, j13);
             t = __fma_rn(j12, b, t);
             const double q = __fma_rn(j22, b, j23);
             double E = __fma_rn(t, a, __fma_rn(q, b, j33));
-            if (__double2hiint(E) < 0) E = 0.0;  // max(E, 0) on the sign bit
-            wp = __dmul_rn(wp, __dmul_rn(A.a_data[k], dpow_tab(__dadd_rn(E, 0.00001), A.a_m1[k])));
+            if (__double_as_longlong(E) < __double_as_longlong(0.00001)) E = 0.00001;
+            wp = __dmul_rn(wp, dpow_tab(E, A.a_m1[k]));
         }
         den_u = __fma_rn(wp, j11, den_u);
         den_v = __fma_rn(wp, j22, den_v);
@@ -321,8 +323,9 @@ __global__ void __launch_bounds__(NTM, StripBounds<NTM>::blocks) k_sor_chain64(S
             } else {
 #pragma unroll
                 for (int q = 0; q < 6 * K; ++q) f.j[q] = Jr[q * pl + o];
+                const double* wsrc = (pk & kPkTick) ? Wr + K * pl : Wr;  // W * a_data on a tick
 #pragma unroll
-                for (int k = 0; k < K; ++k) f.w[k] = Wr[k * pl + o];
+                for (int k = 0; k < K; ++k) f.w[k] = wsrc[k * pl + o];
                 f.lu = lapr[o];
                 f.lv = lapr[pl + o];
             }
@@ -617,10 +620,7 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
     A.wsum = ((wx + wx) + wy) + wy;
     A.omega = omega;
     A.one_m_omega = 1.0 - omega;
-    for (int k = 0; k < kMaxK; ++k) {
-        A.a_data[k] = k < K ? a_data[k] : 0.0;
-        A.a_m1[k] = k < K ? a_data[k] - 1.0 : 0.0;
-    }
+    for (int k = 0; k < kMaxK; ++k) A.a_m1[k] = k < K ? a_data[k] - 1.0 : 0.0;
     auto launch = [&](int nc_, int nt_) {
         A.nc = nc_;
         switch (K) {
