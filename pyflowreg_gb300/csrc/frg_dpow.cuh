@@ -1,5 +1,5 @@
 // Float64 power x^b for the data-term nonlinearity of the float64 solver,
-// psi = a (E + 1e-5)^(a - 1) (core/level_solver.py:247), in 18 float64
+// psi = a (E + 1e-5)^(a - 1) (core/level_solver.py:247), in 15 float64
 // operations instead of the ~100 the general pow costs on a float64 pipe that
 // runs at 1/64 of the float32 rate.
 //
@@ -14,7 +14,8 @@
 //   log2 x = e - log2(inv_j) + log2(1 + r), log2(1 + r) by its Taylor series
 //     to r^5 (truncation below 2^-56, a tenth of an ulp of the result);
 //     -log2(inv_j) is tabulated as Lhi + Llo with Lhi a multiple of 2^-42, so
-//     e + Lhi is exact;
+//     e + Lhi is exact (and formed by integer operations from the fixed-point
+//     sum, as is the double of k below);
 //   y = b log2 x = yh + yl: yh = b (e + Lhi) rounded, yl its rounding error
 //     (an fma) plus b (Llo + log2(1 + r)), so |yl| <= |b| 2^-8.5;
 //   k = round(256 yh), f = yh - k / 256 + yl, |f| <= 2^-9 + |b| 2^-8.5;
@@ -41,7 +42,7 @@
 
 namespace frg {
 
-constexpr int kDpowLogN = 256;   // log table entries: (inv_j, Lhi - 1023, Llo)
+constexpr int kDpowLogN = 256;   // log table entries: (inv_j, Lhi 2^42 as a 64-bit integer, Llo)
 constexpr int kDpowExpN = 256;   // exp table entries: 2^(i / 256)
 
 // The tables (device memory of this translation unit; the library is built
@@ -106,8 +107,14 @@ __device__ __forceinline__ double dpow_tab(double x, double b)
     double p = __fma_rn(r, kL3, kL2);
     p = __fma_rn(r, p, kL1);
     p = __fma_rn(r, p, dpow_tail(r, (float)kL4, (float)kL5));
-    const double ed = __dsub_rn(__hiloint2double(0x43300000, eb), 4503599627370496.0);  // eb as a double
-    const double lh = __dadd_rn(ed, __ldg(lt + 1));                                     // e + Lhi, exact
+    // e + Lhi, exact: the fixed-point integer N = (eb - 1023) 2^42 + Lhi 2^42
+    // (0 < |N| < 2^52) written as a double by integer operations
+    const long long N = ((long long)(eb - 1023) << 42) + __double_as_longlong(__ldg(lt + 1));
+    const unsigned long long aN = (unsigned long long)(N < 0 ? -N : N);
+    const int pN = 63 - __clzll((long long)aN);
+    const double lh = __longlong_as_double((long long)(((unsigned long long)(N < 0) << 63) |
+                                                       ((unsigned long long)(981 + pN) << 52) |
+                                                       ((aN << (52 - pN)) & 0xFFFFFFFFFFFFFull)));
     const double ll = __dadd_rn(__ldg(lt + 2), p);
     const double yh = __dmul_rn(b, lh);
     double yl = __fma_rn(b, lh, -yh);
@@ -115,7 +122,12 @@ __device__ __forceinline__ double dpow_tab(double x, double b)
     if ((__double2hiint(yh) & 0x7fffffff) >= 0x40800000) return pow(x, b);  // |yh| >= 512, or NaN
     const double t = __fma_rn(yh, 256.0, 6755399441055744.0);  // 1.5 * 2^52: round(256 yh) in the low word
     const int k = __double2loint(t);
-    const double kd = __dsub_rn(t, 6755399441055744.0);
+    // k as a double (|k| <= 2^17) by integer operations
+    const unsigned ak = (unsigned)(k < 0 ? -k : k);
+    const int pk = 31 - __clz((int)ak);
+    const double kd = ak == 0u ? 0.0
+                               : __hiloint2double((int)(((unsigned)(k < 0) << 31) | ((unsigned)(1023 + pk) << 20) |
+                                                        ((ak << (20 - pk)) & 0xfffffu)), 0);
     double f = __fma_rn(kd, -0.00390625, yh);
     f = __dadd_rn(f, yl);
     double q = __fma_rn(f, kE3, kE2);

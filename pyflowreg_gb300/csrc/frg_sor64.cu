@@ -32,6 +32,7 @@
 #include <cooperative_groups.h>
 
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <set>
 
@@ -56,8 +57,9 @@ cudaError_t upload_dpow_tables()
         const long double L = -log2l((long double)inv);   // in [0, 1)
         const double Lhi = (double)(nearbyintl(L * two42) / two42);
         const double Llo = (double)(L - (long double)Lhi);
+        const long long L42 = (long long)nearbyintl(L * two42);  // Lhi 2^42, below 2^42
         lt[3 * j] = inv;
-        lt[3 * j + 1] = Lhi - 1023.0;  // exact: a multiple of 2^-42 below 1024 in magnitude
+        std::memcpy(&lt[3 * j + 1], &L42, sizeof(L42));
         lt[3 * j + 2] = Llo;
     }
     for (int i = 0; i < kDpowExpN; ++i) et[i] = (double)exp2l((long double)i / (long double)kDpowExpN);
