@@ -382,6 +382,7 @@ struct frg_plan {
     double* xuv = nullptr;    // (T, 2, m*n)
     double* xacc[2] = {nullptr, nullptr};  // (T, 2, h*w)
     double a_data64[kMaxK] = {0};
+    PowTab64 pow64[kMaxK];  // the float64 chained SOR's power table per channel (shared by equal exponents)
     // final cubic upsampling when min_level > 0 (tables per output column / row)
     int32_t* up_sx = nullptr;
     float* up_wx = nullptr;
@@ -416,6 +417,32 @@ int dev_alloc(frg_plan* pl, T** out, size_t count)
     pl->allocs.push_back(p);
     pl->bytes += b;
     *out = (T*)p;
+    return FRG_OK;
+}
+
+// The float64 chained SOR's power tables: one per distinct exponent a_data[k] - 1
+// with |a_data[k] - 1| <= 1 (others keep a null table: the general power).
+int make_pow_tables(frg_plan* pl, int channels)
+{
+    std::vector<double2> tab(kPowTabN);
+    for (int k = 0; k < channels; ++k) {
+        const double b = pl->a_data64[k] - 1.0;
+        int same = -1;
+        for (int q = 0; q < k && same < 0; ++q)
+            if (pl->a_data64[q] - 1.0 == b) same = q;
+        if (same >= 0) {
+            pl->pow64[k] = pl->pow64[same];
+            continue;
+        }
+        PowTab64 pt;
+        if (!make_pow_table(b, tab.data(), &pt)) continue;
+        double2* dt = nullptr;
+        if (int rc = dev_alloc(pl, &dt, (size_t)kPowTabN)) return rc;
+        const cudaError_t e = cudaMemcpy(dt, tab.data(), sizeof(double2) * kPowTabN, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(FRG_ECUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        pt.t = dt;
+        pl->pow64[k] = pt;
+    }
     return FRG_OK;
 }
 
@@ -791,6 +818,10 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
             return rc;
         }
         for (int k = 0; k < channels; ++k) pl->a_data64[k] = params->a_data[k];
+        if (max_dp64 > 0 && (rc = make_pow_tables(pl, channels))) {
+            frg_plan_destroy(pl);
+            return rc;
+        }
         if (max_dp64 > 0 &&
             ((rc = dev_alloc(pl, &pl->dJ, T * 6 * K * max_dp64)) || (rc = dev_alloc(pl, &pl->dlap, T * 2 * max_dp64)) ||
              (rc = dev_alloc(pl, &pl->dcoef, T * 5 * max_dp64)) || (rc = dev_alloc(pl, &pl->ddu, T * max_dp64)) ||
@@ -1282,7 +1313,8 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
             const int rows = L.rows64 ? L.rows64 : sor_chain64_default_rows(L.g, T, pl->n_sms);
             FRG_LAUNCH(launch_sor_chain64(pl->dJ, 6LL * K * dp, L.wdiag64, 0, pl->dlap, 2 * dp, pl->dcoef, 5 * dp,
                                           pl->ddu, pl->ddv, dp, T, K, L.g, cp, np, pl->a_data64, wx, wy, pl->p.omega,
-                                          st, pl->xdu + (w + 2) + 1, pl->xdv + (w + 2) + 1, mn, w + 2, rows));
+                                          st, pl->xdu + (w + 2) + 1, pl->xdv + (w + 2) + 1, mn, w + 2, rows,
+                                          pl->pow64));
             if (timed) {
                 int rc = record_event(&pl->prof, st);
                 if (rc) return rc;

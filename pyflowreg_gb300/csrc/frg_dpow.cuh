@@ -40,6 +40,8 @@
 
 #include <cuda_runtime.h>
 
+#include "frg_internal.h"
+
 namespace frg {
 
 constexpr int kDpowLogN = 256;   // log table entries: (inv_j, Lhi 2^42 as a 64-bit integer, Llo)
@@ -136,6 +138,33 @@ __device__ __forceinline__ double dpow_tab(double x, double b)
     const double E = __ldg(g_dpow_exp + (k & 255));
     const double res = __fma_rn(E, q, E);
     return __hiloint2double(__double2hiint(res) + (k >> 8) * 0x100000, __double2loint(res));
+}
+
+// x^b for |b| <= 1 from the exponent's own table (PowTab64, built on the host by
+// make_pow_table): with x = 2^e m, j the top 8 bits of m's fraction and
+// r = m inv_j - 1 as in dpow_tab,
+//   x^b = [2^(e b) (1 / inv_j)^b] (1 + r)^b,
+// the bracket a tabulated double-double T.x + T.y (64 exponents x 256 j, from
+// the host's long double), (1 + r)^b - 1 = s by its binomial series to r^6
+// (|r| <= 2^-9 and |b| <= 1: the r^7 term is below 2^-63), the terms to r^3
+// in float64 and r^4 to r^6 in float32 (below 2^-36), and the result
+// T.x + fma(T.x, s, T.y): one rounding of a value within 2^-60 of x^b, so
+// within about half an ulp.  6 float64 operations.  x outside [2^-17, 2^47)
+// (or not a positive normal number) and a null table take dpow_tab.
+__device__ __forceinline__ double dpow_b(double x, double b, const PowTab64& P)
+{
+    const int hi = __double2hiint(x);
+    const unsigned idx = (unsigned)((hi >> 12) - ((1023 + kPowEMin) << 8));
+    if (P.t == nullptr || idx >= (unsigned)kPowTabN) return dpow_tab(x, b);
+    const int j = (hi >> 12) & 0xff;
+    const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, __double2loint(x));
+    const double r = __fma_rn(m, __ldg(g_dpow_log + 3 * j), -1.0);
+    const float rf = dpow_tail_f(r);
+    const float r2 = __fmul_rn(rf, rf);
+    const float tail = __fmul_rn(__fmul_rn(r2, r2), __fadd_rn(P.c4, __fmul_rn(rf, __fadd_rn(P.c5, __fmul_rn(rf, P.c6)))));
+    const double s = __fma_rn(r, __fma_rn(r, __fma_rn(r, P.c3, P.c2), b), dpow_tail_d(tail));
+    const double2 T = __ldg(P.t + idx);
+    return __dadd_rn(T.x, __fma_rn(T.x, s, T.y));
 }
 
 // Host: fills the tables on the current device (once per device).

@@ -121,6 +121,20 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
                              int n_frames, int K, DiagGeom g, const ChainPass* passes, int n_passes,
                              const float* a_data, float wx, float wy, float omega, cudaStream_t st,
                              float* out_du = nullptr, float* out_dv = nullptr, long long out_fs = 0);
+// The float64 solver's power x^b for one exponent b with |b| <= 1 (frg_dpow.cuh,
+// dpow_b): a table of 2^(e b) (1 / inv_j)^b as double-double over the top 20
+// bits of a positive x (unbiased exponent e in [-17, 46], the top 8 fraction
+// bits j), and the binomial series (1 + r)^b - 1 = b r + c2 r^2 + ... + c6 r^6.
+constexpr int kPowEMin = -17;
+constexpr int kPowTabN = 64 * 256;
+struct PowTab64 {
+    const double2* t = nullptr;  // kPowTabN entries on the device; null: the general power
+    double c2 = 0.0, c3 = 0.0;
+    float c4 = 0.0f, c5 = 0.0f, c6 = 0.0f;
+};
+// Host: fills tab (kPowTabN entries) and the series constants of *pt for
+// exponent b (pt->t untouched); false, with nothing written, when |b| > 1.
+bool make_pow_table(double b, double2* tab, PowTab64* pt);
 // The chained SOR in float64 (frg_sor64.cu, k_sor_chain64): the schedule of
 // launch_sor_chain with float64 state, coefficients and arithmetic (the parity
 // precision).  J [6][K][D*P] (J11, J22, J33 + 1e-5, 2 J12, 2 J13, 2 J23), W
@@ -129,7 +143,9 @@ cudaError_t launch_sor_chain(const float* J, long long J_fs, const float* W, lon
 // at out + r * out_rs + c.  Levels of at most 2048 (padded) rows (over 256 as
 // clusters of row strips), K <= 4, w >= 3, at most kMaxChain passes of G <= kGMax.
 // rows: the most rows per CTA (64, 128 or 256; 0 = 256), the level split into at
-// most 8 strips; every split gives the same bits.
+// most 8 strips; every split gives the same bits.  pows: the power table of
+// each channel's exponent a_data[k] - 1 (null, or a null table: the general
+// power).
 bool sor_chain64_supports(int K, const DiagGeom& g, int n_passes);
 bool sor_chain64_rows_ok(const DiagGeom& g, int rows);
 int sor_chain64_default_rows(const DiagGeom& g, int n_frames, int n_sms);
@@ -138,9 +154,9 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
                                long long st_fs, int n_frames, int K, DiagGeom g, const ChainPass* passes,
                                int n_passes, const double* a_data, double wx, double wy, double omega,
                                cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs,
-                               int rows = 0);
-// x^b elementwise by the float64 solver's table-driven power (frg_dpow.cuh);
-// upload_dpow_tables must have run on the current device.
+                               int rows = 0, const PowTab64* pows = nullptr);
+// x^b elementwise by the float64 solver's power (frg_dpow.cuh), with the table
+// path for |b| <= 1; upload_dpow_tables must have run on the current device.
 cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cudaStream_t st);
 cudaError_t upload_dpow_tables();
 // 5x5 median (mirror) of row-major du, dv (T, h, w) plus accumulation into u, v.

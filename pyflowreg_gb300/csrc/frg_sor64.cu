@@ -35,6 +35,7 @@
 #include <cstring>
 #include <mutex>
 #include <set>
+#include <vector>
 
 namespace frg {
 
@@ -69,12 +70,44 @@ cudaError_t upload_dpow_tables()
     return cudaSuccess;
 }
 
+// dpow_b's table for exponent b: T(e, j) = 2^(e b) (1 / inv_j)^b in long double,
+// split into a double and the double of the remainder; inv_j as the device's
+// log table holds it.
+bool make_pow_table(double b, double2* tab, PowTab64* pt)
+{
+    if (!(b >= -1.0 && b <= 1.0)) return false;
+    const long double lb = b;
+    long double B[256];
+    for (int j = 0; j < 256; ++j) {
+        const double c = 1.0 + (2.0 * j + 1.0) / 512.0;  // exact
+        const double inv = 1.0 / c;
+        B[j] = exp2l(-lb * log2l((long double)inv));
+    }
+    for (int e = 0; e < kPowTabN / 256; ++e) {
+        const long double A = exp2l((long double)(e + kPowEMin) * lb);
+        for (int j = 0; j < 256; ++j) {
+            const long double v = A * B[j];
+            const double hi = (double)v;
+            tab[e * 256 + j] = make_double2(hi, (double)(v - (long double)hi));
+        }
+    }
+    // binomial coefficients C(b, n) = C(b, n - 1) (b - n + 1) / n
+    long double c = lb, cn[7];
+    for (int n = 2; n <= 6; ++n) cn[n] = c = c * (lb - (n - 1)) / n;
+    pt->c2 = (double)cn[2];
+    pt->c3 = (double)cn[3];
+    pt->c4 = (float)cn[4];
+    pt->c5 = (float)cn[5];
+    pt->c6 = (float)cn[6];
+    return true;
+}
+
 namespace {
 
-__global__ void k_pow64(long long n, const double* __restrict__ x, double b, double* __restrict__ out)
+__global__ void k_pow64(long long n, const double* __restrict__ x, double b, PowTab64 P, double* __restrict__ out)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = dpow_tab(x[i], b);
+    if (i < n) out[i] = dpow_b(x[i], b, P);
 }
 
 }  // namespace
@@ -83,8 +116,25 @@ cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cu
 {
     if (n <= 0) return cudaSuccess;
     if ((n + 255) / 256 > 0x7fffffffLL) return cudaErrorInvalidValue;
-    k_pow64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, b, out);
-    return cudaGetLastError();
+    PowTab64 P;
+    std::vector<double2> tab(kPowTabN);
+    double2* dt = nullptr;
+    if (make_pow_table(b, tab.data(), &P)) {
+        cudaError_t e = cudaMalloc((void**)&dt, sizeof(double2) * kPowTabN);
+        if (e == cudaSuccess) e = cudaMemcpy(dt, tab.data(), sizeof(double2) * kPowTabN, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (dt) cudaFree(dt);
+            return e;
+        }
+        P.t = dt;
+    }
+    k_pow64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, b, P, out);
+    cudaError_t e = cudaGetLastError();
+    if (dt) {
+        const cudaError_t f = cudaFreeAsync(dt, st);
+        if (e == cudaSuccess) e = f;
+    }
+    return e;
 }
 
 namespace {
@@ -116,6 +166,7 @@ struct Sor64Args {
     double wsum;        // ((wx + wx) + wy) + wy, the reference's order
     double omega, one_m_omega;
     double a_m1[kMaxK];  // a_data - 1
+    PowTab64 pw[kMaxK];  // the power's table per channel (null table: the general power)
     int nc;              // row strips (CTAs) per frame
 };
 
@@ -214,7 +265,7 @@ __device__ __forceinline__ Coef64 fold64(const Sor64Args& A, int pk, const FoldI
             const double q = __fma_rn(j22, b, j23);
             double E = __fma_rn(t, a, __fma_rn(q, b, j33));
             if (__double_as_longlong(E) < __double_as_longlong(0.00001)) E = 0.00001;
-            wp = __dmul_rn(wp, dpow_tab(E, A.a_m1[k]));
+            wp = __dmul_rn(wp, dpow_b(E, A.a_m1[k], A.pw[k]));
         }
         den_u = __fma_rn(wp, j11, den_u);
         den_v = __fma_rn(wp, j22, den_v);
@@ -580,7 +631,7 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
                                long long st_fs, int n_frames, int K, DiagGeom g, const ChainPass* passes,
                                int n_passes, const double* a_data, double wx, double wy, double omega,
                                cudaStream_t st, double* out_du, double* out_dv, long long out_fs, int out_rs,
-                               int rows)
+                               int rows, const PowTab64* pows)
 {
     if (!sor_chain64_supports(K, g, n_passes) || n_frames < 1) return cudaErrorInvalidValue;
     if (rows == 0) rows = kLane64;
@@ -622,7 +673,10 @@ cudaError_t launch_sor_chain64(const double* J, long long J_fs, const double* W,
     A.wsum = ((wx + wx) + wy) + wy;
     A.omega = omega;
     A.one_m_omega = 1.0 - omega;
-    for (int k = 0; k < kMaxK; ++k) A.a_m1[k] = k < K ? a_data[k] - 1.0 : 0.0;
+    for (int k = 0; k < kMaxK; ++k) {
+        A.a_m1[k] = k < K ? a_data[k] - 1.0 : 0.0;
+        A.pw[k] = pows && k < K ? pows[k] : PowTab64();
+    }
     auto launch = [&](int nc_, int nt_) {
         A.nc = nc_;
         switch (K) {
