@@ -276,6 +276,7 @@ struct LevelPlan {
     double* wpad64 = nullptr;  // (K, (h+2)*(w+2)) weight level with zero ring (fp64 mode)
     double* wdiag64 = nullptr;  // (2, K, D*P) the same and times a_data, diagonal-major, for the float64 chained SOR
     double* ref64 = nullptr;    // (K, h, w) reference level in float64, for its tensor
+    double* refd64 = nullptr;   // (4, K, h, w) its derivatives gx1, gy1, fxx1, fyy1 (launch_x_ref_derivs)
     bool chain64 = false;       // fp64 plan: this level runs the float64 chained SOR
     int rows64 = 0;             // its rows per CTA strip (64, 128, 256); 0: chosen per call from the batch size
     int sor_G = 0;        // fused SOR iterations per pass (0: the most the ring allows)
@@ -752,7 +753,8 @@ int frg_plan_create(const frg_params* params, int height, int width, int channel
         L.chain64 = pl->dpath && sor_chain64_supports(channels, L.g, n_passes);
         if (L.chain64) {
             if ((rc = dev_alloc(pl, &L.wdiag64, (size_t)2 * channels * L.g.D * L.g.P)) ||
-                (rc = dev_alloc(pl, &L.ref64, (size_t)channels * L.h * L.w))) {
+                (rc = dev_alloc(pl, &L.ref64, (size_t)channels * L.h * L.w)) ||
+                (rc = dev_alloc(pl, &L.refd64, (size_t)4 * channels * L.h * L.w))) {
                 frg_plan_destroy(pl);
                 return rc;
             }
@@ -1026,6 +1028,7 @@ int frg_set_reference(frg_plan* pl, const float* fixed, const float* weight, voi
             if (L.chain64) {
                 FRG_LAUNCH(launch_x_pad_to_diag(L.wpad64, K, L.h, L.w, L.g, L.wdiag64, st, pl->a_data64));
                 FRG_LAUNCH(launch_x_to_double(L.ref, (long long)K * hw, L.ref64, st));
+                FRG_LAUNCH(launch_x_ref_derivs(L.ref64, K, L.h, L.w, L.h_row, L.h_col, L.refd64, st));
             }
         }
         pl->has_ref = true;
@@ -1298,9 +1301,9 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
             // du, dv into the interiors of the padded xdu, xdv for the median
             const long long dp = (long long)L.g.D * L.g.P;
             const double wx = L.alpha_x / (L.h_col * L.h_col), wy = L.alpha_y / (L.h_row * L.h_row);
-            FRG_LAUNCH(launch_x_tensor_diag(L.ref64, L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
-                                            pl->p.const_assumption, pl->dJ, 6LL * K * dp, L.g, pl->xuv, pl->xuv + mn,
-                                            uv_fs, wx, wy, pl->dlap, 2 * dp, st));
+            FRG_LAUNCH(launch_x_tensor_diag(L.ref64, L.refd64, L.ref, img2, T, K, h, w, L.h_row, L.h_col,
+                                            L.top ? 0 : 1, pl->p.const_assumption, pl->dJ, 6LL * K * dp, L.g, pl->xuv,
+                                            pl->xuv + mn, uv_fs, wx, wy, pl->dlap, 2 * dp, st));
             Pass ps[kMaxChain];
             ChainPass cp[kMaxChain];
             const int np = fill_passes(pl->p.iterations, pl->p.update_lag, kGMax, ps, kMaxChain);

@@ -140,9 +140,16 @@ cudaError_t upload_cubic_table_x(const float* tab128)
     return cudaMemcpyToSymbol(cx_cubic, tab128, sizeof(float) * 128);
 }
 
+// The flow over the spacing: a product with the reciprocal where the spacing is a
+// power of two (the finest level's 1), which rounds like the quotient.
+struct WarpScale {
+    double h_col, h_row, i_col, i_row;
+    int pow2_col, pow2_row;
+};
+
 __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ f1, const double* __restrict__ u,
-                        const double* __restrict__ v, long long uv_fs, int K, int h, int w, double h_col,
-                        double h_row, float* __restrict__ out)
+                        const double* __restrict__ v, long long uv_fs, int K, int h, int w, WarpScale S,
+                        float* __restrict__ out)
 {
     // the table is read per lane at the lane's own sub-pixel position: copied into shared
     // memory first (constant memory serialises a warp's distinct addresses)
@@ -156,8 +163,9 @@ __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ 
     const long long n = w + 2;
     const long long hw = (long long)h * w;
     const long long o = (long long)(y + 1) * n + (x + 1);
-    const float mx = (float)dadd((double)x, ddiv(u[f * uv_fs + o], h_col));
-    const float my = (float)dadd((double)y, ddiv(v[f * uv_fs + o], h_row));
+    const double uu = u[f * uv_fs + o], vv = v[f * uv_fs + o];
+    const float mx = (float)dadd((double)x, S.pow2_col ? dmul(uu, S.i_col) : ddiv(uu, S.h_col));
+    const float my = (float)dadd((double)y, S.pow2_row ? dmul(vv, S.i_row) : ddiv(vv, S.h_row));
     const bool oob = (mx < 0.0f) || (mx >= (float)w) || (my < 0.0f) || (my >= (float)h);
     if (oob) {
         for (int k = 0; k < K; ++k)
@@ -197,8 +205,16 @@ __global__ void kx_warp(const float* __restrict__ f2, const float* __restrict__ 
 cudaError_t launch_x_warp(const float* f2, const float* f1, const double* u, const double* v, long long uv_fs,
                           int n_frames, int K, int h, int w, double h_col, double h_row, float* out, cudaStream_t st)
 {
+    WarpScale S;
+    S.h_col = h_col;
+    S.h_row = h_row;
+    int ex = 0;
+    S.pow2_col = frexp(h_col, &ex) == 0.5 ? 1 : 0;
+    S.pow2_row = frexp(h_row, &ex) == 0.5 ? 1 : 0;
+    S.i_col = 1.0 / h_col;
+    S.i_row = 1.0 / h_row;
     dim3 blk(128), grd((w + 127) / 128, h, n_frames);
-    kx_warp<<<grd, blk, 0, st>>>(f2, f1, u, v, uv_fs, K, h, w, h_col, h_row, out);
+    kx_warp<<<grd, blk, 0, st>>>(f2, f1, u, v, uv_fs, K, h, w, S, out);
     return cudaGetLastError();
 }
 
@@ -381,8 +397,25 @@ __global__ void kx_tensor(const float* __restrict__ f1, const float* __restrict_
 // one contiguous run; the stencil reads go through L1.
 struct TensConsts {
     double ihx2, ihy2, ihxx, ihyy;  // 1 / (2 hx), 1 / (2 hy), 1 / hx^2, 1 / hy^2
+    double ihy4;                    // 1 / (4 hy) = ihy2 / 2, exact
     float h2x_f, h2y_f, hxx_f, hyy_f;
 };
+
+TensConsts tens_consts(double hy, double hx)
+{
+    TensConsts C;
+    const double h2x = 2.0 * hx, h2y = 2.0 * hy, hxx = hx * hx, hyy = hy * hy;
+    C.ihx2 = 1.0 / h2x;
+    C.ihy2 = 1.0 / h2y;
+    C.ihxx = 1.0 / hxx;
+    C.ihyy = 1.0 / hyy;
+    C.ihy4 = 0.5 * C.ihy2;
+    C.h2x_f = (float)h2x;
+    C.h2y_f = (float)h2y;
+    C.hxx_f = (float)hxx;
+    C.hyy_f = (float)hyy;
+    return C;
+}
 
 __device__ __forceinline__ double drcp(double x)
 {
@@ -394,12 +427,35 @@ __device__ __forceinline__ double drcp(double x)
     return __fma_rn(y, e, y);
 }
 
-__device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, const float* __restrict__ b, int h, int w,
-                                              int yo, int xo, const TensConsts& C, int f2_f32, int gray, double* jo)
+// The reference level's own derivatives, the same for every frame: planes
+// (4, K, h, w) of gx1 = (f1[x+1] - f1[x-1]) / (2 hx), gy1 likewise,
+// fxx1 = (f1[x-1] - 2 f1 + f1[x+1]) / hx^2 and fyy1, at every pixel with the
+// level's clamped neighbours, computed once per reference by kx_ref_derivs.
+constexpr int kRefGx = 0, kRefGy = 1, kRefFxx = 2, kRefFyy = 3;
+
+__device__ __forceinline__ void ref_derivs64(const double* __restrict__ a, int h, int w, int yy, int xx,
+                                             const TensConsts& C, double* o)
 {
     // unpadded reads at padded (yy, xx), clamped into the level
-    auto A = [&](int yy, int xx) { return a[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
-    auto Bf = [&](int yy, int xx) { return b[(long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1)]; };
+    auto A = [&](int y, int x) { return a[(long long)xclamp(y - 1, 0, h - 1) * w + xclamp(x - 1, 0, w - 1)]; };
+    const double a0 = A(yy, xx);
+    o[kRefGx] = dmul(dsub(A(yy, xx + 1), A(yy, xx - 1)), C.ihx2);
+    o[kRefGy] = dmul(dsub(A(yy + 1, xx), A(yy - 1, xx)), C.ihy2);
+    o[kRefFxx] = dmul(dadd(dsub(A(yy, xx - 1), dadd(a0, a0)), A(yy, xx + 1)), C.ihxx);
+    o[kRefFyy] = dmul(dadd(dsub(A(yy - 1, xx), dadd(a0, a0)), A(yy + 1, xx)), C.ihyy);
+}
+
+// a: the reference level (h, w) of channel k in float64; rd: its derivative
+// planes (plane q at rd + q * rd_ps, row-major h x w).
+__device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, const double* __restrict__ rd,
+                                              long long rd_ps, const float* __restrict__ b, int h, int w, int yo,
+                                              int xo, const TensConsts& C, int f2_f32, int gray, double* jo)
+{
+    // unpadded reads at padded (yy, xx), clamped into the level
+    auto at = [&](int yy, int xx) { return (long long)xclamp(yy - 1, 0, h - 1) * w + xclamp(xx - 1, 0, w - 1); };
+    auto A = [&](int yy, int xx) { return a[at(yy, xx)]; };
+    auto Bf = [&](int yy, int xx) { return b[at(yy, xx)]; };
+    auto R = [&](int q, int yy, int xx) { return rd[q * rd_ps + at(yy, xx)]; };
     auto gx2 = [&](int yy, int xx) {
         if (f2_f32) return f2d(__fdiv_rn(__fsub_rn(Bf(yy, xx + 1), Bf(yy, xx - 1)), C.h2x_f));
         return dmul(dsub(f2d(Bf(yy, xx + 1)), f2d(Bf(yy, xx - 1))), C.ihx2);
@@ -408,15 +464,17 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
         if (f2_f32) return f2d(__fdiv_rn(__fsub_rn(Bf(yy + 1, xx), Bf(yy - 1, xx)), C.h2y_f));
         return dmul(dsub(f2d(Bf(yy + 1, xx)), f2d(Bf(yy - 1, xx))), C.ihy2);
     };
-    auto FX = [&](int yy, int xx) {
+    // twice fx, fy (gx1 + gx2) at a position clamped into [1, h] x [1, w]: the halving is
+    // exact, so it moves into the spacing factor of the derivative taken from them
+    auto FX2 = [&](int yy, int xx) {
         yy = xclamp(yy, 1, h);
         xx = xclamp(xx, 1, w);
-        return dmul(0.5, dadd(dmul(dsub(A(yy, xx + 1), A(yy, xx - 1)), C.ihx2), gx2(yy, xx)));
+        return dadd(R(kRefGx, yy, xx), gx2(yy, xx));
     };
-    auto FY = [&](int yy, int xx) {
+    auto FY2 = [&](int yy, int xx) {
         yy = xclamp(yy, 1, h);
         xx = xclamp(xx, 1, w);
-        return dmul(0.5, dadd(dmul(dsub(A(yy + 1, xx), A(yy - 1, xx)), C.ihy2), gy2(yy, xx)));
+        return dadd(R(kRefGy, yy, xx), gy2(yy, xx));
     };
     auto FT = [&](int yy, int xx) {
         yy = xclamp(yy, 1, h);
@@ -424,7 +482,7 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
         return dsub(f2d(Bf(yy, xx)), A(yy, xx));
     };
     if (gray) {
-        const double fxv = FX(yo, xo), fyv = FY(yo, xo), ftv = FT(yo, xo);
+        const double fxv = dmul(0.5, FX2(yo, xo)), fyv = dmul(0.5, FY2(yo, xo)), ftv = FT(yo, xo);
         jo[0] = dmul(fxv, fxv);
         jo[1] = dmul(fyv, fyv);
         jo[2] = dmul(ftv, ftv);
@@ -433,12 +491,11 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
         jo[5] = dmul(fyv, ftv);
         return;
     }
-    const double fxy = dmul(dsub(FX(yo + 1, xo), FX(yo - 1, xo)), C.ihy2);
+    const double fxy = dmul(dsub(FX2(yo + 1, xo), FX2(yo - 1, xo)), C.ihy4);
     const double fxt = dmul(dsub(FT(yo, xo + 1), FT(yo, xo - 1)), C.ihx2);
     const double fyt = dmul(dsub(FT(yo + 1, xo), FT(yo - 1, xo)), C.ihy2);
-    const double a0 = A(yo, xo);
-    const double fxx1 = dmul(dadd(dsub(A(yo, xo - 1), dadd(a0, a0)), A(yo, xo + 1)), C.ihxx);
-    const double fyy1 = dmul(dadd(dsub(A(yo - 1, xo), dadd(a0, a0)), A(yo + 1, xo)), C.ihyy);
+    const double fxx1 = R(kRefFxx, yo, xo);
+    const double fyy1 = R(kRefFyy, yo, xo);
     double fxx2, fyy2;
     if (f2_f32) {
         fxx2 = f2d(__fdiv_rn(__fadd_rn(__fsub_rn(Bf(yo, xo - 1), __fmul_rn(2.0f, Bf(yo, xo))), Bf(yo, xo + 1)),
@@ -465,7 +522,29 @@ __device__ __forceinline__ void tensor_fast64(const double* __restrict__ a, cons
     jo[5] = __fma_rn(rxy, fxt, dmul(ryy, fyt));
 }
 
-__global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__ f1, const float* __restrict__ f1f,
+__global__ void kx_ref_derivs(const double* __restrict__ f1, int K, int h, int w, TensConsts C, double* __restrict__ rd)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    const int k = blockIdx.z;
+    if (c >= w) return;
+    const long long hw = (long long)h * w;
+    double o[4];
+    ref_derivs64(f1 + k * hw, h, w, r + 1, c + 1, C, o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rd[((long long)q * K + k) * hw + (long long)r * w + c] = o[q];
+}
+
+cudaError_t launch_x_ref_derivs(const double* f1, int K, int h, int w, double hy, double hx, double* rd,
+                                cudaStream_t st)
+{
+    dim3 blk(128), grd((w + 127) / 128, h, K);
+    kx_ref_derivs<<<grd, blk, 0, st>>>(f1, K, h, w, tens_consts(hy, hx), rd);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__ f1, const double* __restrict__ rd,
+                                                      const float* __restrict__ f1f,
                                                       const float* __restrict__ f2, int K, int h, int w, TensConsts C,
                                                       double hy, double hx, int f2_f32, int gray,
                                                       double* __restrict__ J, long long J_fs, DiagGeom g,
@@ -490,7 +569,8 @@ __global__ void __launch_bounds__(256) kx_tensor_diag(const double* __restrict__
         if (gray == 2)  // census: the reference-order arithmetic of kx_tensor
             tensor_px64(f1f, f2, f, K, k, h, w, r + 1, c + 1, hy, hx, f2_f32, 2, j);
         else
-            tensor_fast64(f1 + k * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C, f2_f32, gray, j);
+            tensor_fast64(f1 + k * hw, rd + k * hw, K * hw, f2 + ((long long)f * K + k) * hw, h, w, r + 1, c + 1, C,
+                          f2_f32, gray, j);
         // the cross terms doubled (exact), as the solver's data residual uses them, and
         // J33 with the residual's offset 1e-5 added
 #pragma unroll
@@ -518,26 +598,17 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_x_tensor_diag(const double* f1, const float* f1f, const float* f2, int n_frames, int K, int h, int w,
-                                 double hy, double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
-                                 const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
-                                 long long lap_fs, cudaStream_t st)
+cudaError_t launch_x_tensor_diag(const double* f1, const double* rd, const float* f1f, const float* f2, int n_frames,
+                                 int K, int h, int w, double hy, double hx, int f2_f32, int gray, double* J,
+                                 long long J_fs, DiagGeom g, const double* u, const double* v, long long uv_fs,
+                                 double wx, double wy, double* lap, long long lap_fs, cudaStream_t st)
 {
-    TensConsts C;
-    const double h2x = 2.0 * hx, h2y = 2.0 * hy, hxx = hx * hx, hyy = hy * hy;
-    C.ihx2 = 1.0 / h2x;
-    C.ihy2 = 1.0 / h2y;
-    C.ihxx = 1.0 / hxx;
-    C.ihyy = 1.0 / hyy;
-    C.h2x_f = (float)h2x;
-    C.h2y_f = (float)h2y;
-    C.hxx_f = (float)hxx;
-    C.hyy_f = (float)hyy;
+    const TensConsts C = tens_consts(hy, hx);
     const long long warps = (long long)g.D * (g.P >> 5);
     if ((warps + 7) / 8 > 0x7fffffffLL || n_frames > 65535) return cudaErrorInvalidValue;
     dim3 grd((unsigned)((warps + 7) / 8), n_frames);
-    kx_tensor_diag<<<grd, 256, 0, st>>>(f1, f1f, f2, K, h, w, C, hy, hx, f2_f32, gray, J, J_fs, g, u, v, uv_fs, wx,
-                                        wy, lap, lap_fs);
+    kx_tensor_diag<<<grd, 256, 0, st>>>(f1, rd, f1f, f2, K, h, w, C, hy, hx, f2_f32, gray, J, J_fs, g, u, v, uv_fs,
+                                        wx, wy, lap, lap_fs);
     return cudaGetLastError();
 }
 

@@ -187,15 +187,21 @@ cudaError_t launch_x_tensor(const float* f1, const float* f2, int n_frames, int 
                             int f2_f32, int gray, double* J, cudaStream_t st);
 // The tensor diagonal-major (T, 6, K, D*P) with the smoothness constant
 // (T, 2, D*P) from the padded float64 u, v (frame stride uv_fs), for the
-// float64 chained SOR; f1 is the reference level in float64 (K, h, w), f1f the
-// same in float32 (the census data term, gray = 2, runs the reference-order
+// float64 chained SOR; f1 is the reference level in float64 (K, h, w) and rd
+// its derivatives (launch_x_ref_derivs), f1f the same level in float32 (the
+// census data term, gray = 2, runs the reference-order
 // arithmetic of kx_tensor on it).  The planes hold J11, J22, J33 + 1e-5, 2 J12,
 // 2 J13, 2 J23: the cross terms doubled (exact) and the offset of psi's argument
 // (E + 1e-5) added to J33, as the solver's data residual uses them.
-cudaError_t launch_x_tensor_diag(const double* f1, const float* f1f, const float* f2, int n_frames, int K, int h, int w,
-                                 double hy, double hx, int f2_f32, int gray, double* J, long long J_fs, DiagGeom g,
-                                 const double* u, const double* v, long long uv_fs, double wx, double wy, double* lap,
-                                 long long lap_fs, cudaStream_t st);
+cudaError_t launch_x_tensor_diag(const double* f1, const double* rd, const float* f1f, const float* f2, int n_frames,
+                                 int K, int h, int w, double hy, double hx, int f2_f32, int gray, double* J,
+                                 long long J_fs, DiagGeom g, const double* u, const double* v, long long uv_fs,
+                                 double wx, double wy, double* lap, long long lap_fs, cudaStream_t st);
+// The reference level's derivatives that kx_tensor_diag reads (rd: planes
+// (4, K, h, w) of gx1, gy1, fxx1, fyy1 of f1 (K, h, w) in float64, the same
+// arithmetic as the tensor's), once per reference and level.
+cudaError_t launch_x_ref_derivs(const double* f1, int K, int h, int w, double hy, double hx, double* rd,
+                                cudaStream_t st);
 cudaError_t launch_x_to_double(const float* src, long long n, double* dst, cudaStream_t st);
 cudaError_t launch_x_sor(const double* J, const double* W, const double* u, const double* v, long long uv_fs,
                          double* du, double* dv, double* wp, int n_frames, int K, int h, int w, double alpha_x,
