@@ -189,7 +189,8 @@ def test_registration_loss_gradient_matches_oracle_fp64():
     Lo = D.loss(fo, mo, torch.tensor(truth[0]), torch.tensor(w_true[0]), torch.stack([ao, ao]), np.full(K, 1.0),
                 **opts)
     Lo.backward()
-    assert abs(float(L) - float(Lo)) <= 1e-8 * abs(float(Lo)), (float(L), float(Lo))
+    Lv, Lov = float(L.detach()), float(Lo.detach())
+    assert abs(Lv - Lov) <= 1e-8 * abs(Lov), (Lv, Lov)
     for got, ref in ((m_t.grad[0].cpu(), mo.grad), (f_t.grad[0].cpu(), fo.grad), (a_t.grad.cpu(), ao.grad)):
         scale = float(ref.abs().max())
         err = float((got - ref).abs().max())
