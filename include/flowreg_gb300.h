@@ -249,10 +249,11 @@ int frg_median5_f64(int h, int w, const double* src, double* dst, void* stream);
 
 /* out[i] = x[i]^b (n doubles, device memory) by the power function of the
  * float64 solver's data-term nonlinearity psi = a (E + 1e-5)^(a - 1)
- * (core/level_solver.py:247, `(val + 0.00001) ** (a_data[k] - 1.0)`): a
- * table-driven log2 / exp2 within a few ulp of the correctly rounded power
- * for positive normal x.  Exported so that its accuracy can be tested on its
- * own. */
+ * (core/level_solver.py:247, `(val + 0.00001) ** (a_data[k] - 1.0)`): for
+ * |b| <= 1 a table of 2^(e b) c^b built for b (on the host, per call) with a
+ * binomial series, else a table-driven log2 / exp2; within a few ulp of the
+ * correctly rounded power for positive normal x, pow's results elsewhere.
+ * Exported so that its accuracy can be tested on its own. */
 int frg_pow_f64(long long n, const double* x, double b, double* out, void* stream);
 
 /* Page-locks (cudaHostRegister, default flags) or releases host memory that

@@ -120,10 +120,12 @@ cudaError_t launch_pow64(long long n, const double* x, double b, double* out, cu
     std::vector<double2> tab(kPowTabN);
     double2* dt = nullptr;
     if (make_pow_table(b, tab.data(), &P)) {
-        cudaError_t e = cudaMalloc((void**)&dt, sizeof(double2) * kPowTabN);
-        if (e == cudaSuccess) e = cudaMemcpy(dt, tab.data(), sizeof(double2) * kPowTabN, cudaMemcpyHostToDevice);
+        // stream-ordered: the copy from pageable memory returns once the table is staged
+        cudaError_t e = cudaMallocAsync((void**)&dt, sizeof(double2) * kPowTabN, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dt, tab.data(), sizeof(double2) * kPowTabN, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) {
-            if (dt) cudaFree(dt);
+            if (dt) cudaFreeAsync(dt, st);
             return e;
         }
         P.t = dt;
