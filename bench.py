@@ -917,8 +917,9 @@ def run_gb300(args):
                     "d2h_bytes_per_step": T * H * W * 2 * (8 if fp64 else 4),
                     "api": "pyflowreg_gb300.get_displacement_batch(fixed, moving, weight=..., **options): numpy "
                            "arrays in, numpy flows out (the reference-facing batch call behind the gb300 executor)",
-                    "copies": "pageable numpy -> pinned staging -> device per lane part, read-back into pinned "
-                              "memory and numpy; copies of one part overlap the other parts' compute",
+                    "copies": "pageable numpy -> pinned staging -> device per lane part (copies of one part "
+                              "overlap the other parts' compute); each lane's last part read back by one copy "
+                              "into the output array, page-locked while the lanes compute",
                     "timing": "wall clock around the calls after a warm-up call",
                     "flows_equal_device_resident_run": e2e_equal},
             "gpu_launches": int(launches),
