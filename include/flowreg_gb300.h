@@ -38,6 +38,7 @@ extern "C" {
 #define FRG_ENOMEM 2          /* device or host allocation failed */
 #define FRG_ECUDA 3           /* a CUDA call failed */
 #define FRG_EUNSUPPORTED 4    /* option not implemented by this backend */
+#define FRG_ECALLBACK 5       /* a host callback reported failure */
 
 #define FRG_MAX_CHANNELS 8
 #define FRG_MAX_GNC_STAGES 16
@@ -142,6 +143,23 @@ int frg_plan_level_tuning(const frg_plan* plan, int level, int* sor_G, int* sor_
  * does not).  Both give the same bits.  n_variants: how many serve the level
  * (0 when it does not use a fused kernel). */
 int frg_plan_set_level_variant(frg_plan* plan, int level, int variant);
+
+/* A host level solver that the float64 path calls in place of its own SOR:
+ * the `level_solver_backend` of get_displacement (core/optical_flow.py:579-606).
+ * It is called once per pyramid level and frame, on the thread inside
+ * frg_get_displacement_f64, after the stream has finished the level's motion
+ * tensor.  m = h + 2 and n = w + 2 (the padded level); J (6, K, m*n: J11, J22,
+ * J33, J12, J13, J23 with a zero ring), W (K, m*n, zero ring), u, v (m*n, edge
+ * ring) and du, dv (m*n) are float64 device pointers; alpha_x, alpha_y are the
+ * level's smoothness weights and hx, hy its column and row spacings.  The
+ * callback writes du, dv (complete on the device when it returns) and returns
+ * 0, or nonzero to end the call with FRG_ECALLBACK. */
+typedef int (*frg_level_solver_fn)(void* user, int level, int frame, int m, int n, int K, const double* J,
+                                   const double* W, const double* u, const double* v, double alpha_x,
+                                   double alpha_y, double hx, double hy, double* du, double* dv);
+/* Installs (fn non-null) or removes (fn null) the host level solver of a
+ * float64 plan without GNC stages; FRG_EUNSUPPORTED for other plans. */
+int frg_plan_set_level_solver(frg_plan* plan, frg_level_solver_fn fn, void* user);
 int frg_plan_level_variant(const frg_plan* plan, int level, int* variant, int* n_variants);
 
 /* Reference (fixed) frame (height, width, channels) float32 and the per-pixel

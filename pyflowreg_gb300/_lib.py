@@ -18,6 +18,7 @@ FRG_EINVAL = 1
 FRG_ENOMEM = 2
 FRG_ECUDA = 3
 FRG_EUNSUPPORTED = 4
+FRG_ECALLBACK = 5
 FRG_MAX_CHANNELS = 8
 FRG_MAX_GNC_STAGES = 16
 
@@ -47,6 +48,13 @@ class FrgParams(ctypes.Structure):
 
 FRG_FP32 = 0
 FRG_FP64_REFERENCE = 1
+
+
+# frg_level_solver_fn: (user, level, frame, m, n, K, J, W, u, v, alpha_x, alpha_y, hx, hy, du, dv) -> int
+LEVEL_SOLVER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p)
 
 
 class FrgError(RuntimeError):
@@ -93,6 +101,7 @@ def load(build_if_missing: bool = True):
         _sig(lib, "frg_plan_set_level_tuning", I, [P, I, I, I])
         _sig(lib, "frg_plan_level_tuning", I, [P, I, pI, pI, pI, pI])
         _sig(lib, "frg_plan_set_level_variant", I, [P, I, I])
+        _sig(lib, "frg_plan_set_level_solver", I, [P, LEVEL_SOLVER_FN, P])
         _sig(lib, "frg_plan_level_variant", I, [P, I, pI, pI])
         _sig(lib, "frg_launch_count", ctypes.c_longlong, [])
         _sig(lib, "frg_plan_set_profiling", I, [P, I])

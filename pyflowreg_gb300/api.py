@@ -530,7 +530,12 @@ def _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations, min_l
              const_assumption, gnc_schedule, warping_steps, level_solver_backend, precision="fp64"):
     const = resolve_const_assumption(const_assumption)
     if level_solver_backend is not None:
-        raise NotImplementedError("the GB300 backend runs its own level solver; level_solver_backend must be None")
+        if not callable(level_solver_backend):
+            raise TypeError("level_solver_backend must be callable")
+        if precision != "fp64":
+            raise NotImplementedError("a caller-supplied level solver runs on the float64 path (precision='fp64')")
+        if gnc_schedule is not None:
+            raise NotImplementedError("a caller-supplied level solver is supported without a GNC schedule")
     fixed = np.asarray(fixed)
     moving = np.asarray(moving)
     K = fixed.shape[2] if fixed.ndim == 3 else 1
@@ -560,8 +565,78 @@ def get_displacement(fixed, moving, alpha=(2, 2), update_lag=5, iterations=50, m
     fixed, moving, w, params, m, n, K = _prepare(fixed, moving, weight, a_data, alpha, update_lag, iterations,
                                                  min_level, levels, eta, a_smooth, const_assumption, gnc_schedule,
                                                  warping_steps, level_solver_backend, precision)
+    if level_solver_backend is not None:
+        return _run_with_solver(level_solver_backend, params, fixed.reshape(m, n, K), moving.reshape(1, m, n, K), w,
+                                uv, normalize_a_data(a_data, K), float(a_smooth), int(iterations), int(update_lag))
     flow = _run_host(params, fixed.reshape(m, n, K), moving.reshape(1, m, n, K), w, uv)
     return flow[0].astype(np.float64)
+
+
+class _DeviceF64:
+    """A float64 device buffer given by pointer and shape, viewed by torch
+    through the CUDA array interface (no copy)."""
+
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(int(s) for s in shape), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 3, "strides": None}
+
+
+def _device_f64(ptr, shape):
+    return torch.as_tensor(_DeviceF64(ptr, shape), device=torch.device("cuda", torch.cuda.current_device()))
+
+
+def _run_with_solver(solver, params, fixed, moving, weight, uv, a_data, a_smooth, iterations, update_lag):
+    """get_displacement with the caller's level solver (core/optical_flow.py:579-606):
+    the float64 path computes each level's pyramid, warp and motion tensor on
+    the device and, in place of its own SOR, hands the solver the arrays the
+    reference passes (J11..J23 and the weight as padded (m, n, K) float64, u, v
+    as padded (m, n), alpha, iterations, update_lag, verbose 0, a_data,
+    a_smooth, hx, hy, gnc_beta None); the returned du, dv go through the
+    median and accumulation on the device."""
+    _require_cuda()
+    m, n, K = fixed.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    errors = []
+
+    def call(user, level, frame, mm, nn, kk, J, W, u, v, ax, ay, hx, hy, du, dv):
+        try:
+            Jh = _device_f64(J, (6, kk, mm, nn)).cpu().numpy()
+            Wh = _device_f64(W, (kk, mm, nn)).cpu().numpy()
+            uh = _device_f64(u, (mm, nn)).cpu().numpy()
+            vh = _device_f64(v, (mm, nn)).cpu().numpy()
+            planes = [np.ascontiguousarray(Jh[q].transpose(1, 2, 0)) for q in range(6)]
+            d_u, d_v = solver(*planes, np.ascontiguousarray(Wh.transpose(1, 2, 0)), uh, vh, [ax, ay], iterations,
+                              update_lag, 0, a_data.copy(), a_smooth, hx, hy, None)
+            for ptr, arr in ((du, d_u), (dv, d_v)):
+                a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64))
+                if a.shape != (mm, nn):
+                    raise ValueError(f"the level solver returned shape {a.shape}, expected {(mm, nn)}")
+                _device_f64(ptr, (mm, nn)).copy_(torch.from_numpy(a))
+            torch.cuda.synchronize()
+            return 0
+        except BaseException as e:  # reported after the call returns
+            errors.append(e)
+            return 1
+
+    fn = _lib.LEVEL_SOLVER_FN(call)
+    plan = Plan(params, m, n, K, 1)
+    try:
+        _lib.check(plan.lib.frg_plan_set_level_solver(plan.handle, fn, None), "frg_plan_set_level_solver")
+        plan.set_reference(torch.from_numpy(np.ascontiguousarray(fixed, dtype=np.float32)).to(dev),
+                           torch.from_numpy(np.ascontiguousarray(weight, dtype=np.float32)).to(dev))
+        uv_t = None
+        if uv is not None:
+            uv_t = torch.from_numpy(np.ascontiguousarray(np.asarray(uv)[:, :, :2], dtype=np.float32)).to(dev)
+        try:
+            flow = plan.displacement(torch.from_numpy(np.ascontiguousarray(moving, dtype=np.float32)).to(dev), uv_t)
+        except _lib.FrgError:
+            if errors:
+                raise errors[0]
+            raise
+        torch.cuda.synchronize()
+        return flow[0].cpu().numpy().astype(np.float64)
+    finally:
+        plan.close()
 
 
 def get_displacement_batch(fixed, moving_frames, alpha=(2, 2), update_lag=5, iterations=50, min_level=0,

@@ -354,6 +354,8 @@ struct SorProfile {
 
 struct frg_plan {
     frg_params p{};
+    frg_level_solver_fn solver_fn = nullptr;  // host level solver in place of the float64 SOR
+    void* solver_user = nullptr;
     int H = 0, W = 0, K = 0, max_T = 0;
     int min_level = 0;
     std::vector<LevelPlan> levels;
@@ -1296,7 +1298,20 @@ int run_xpath(frg_plan* pl, int T, const float* moving, const float* uv_init, do
                                      pl->warped, st));
             img2 = pl->warped;
         }
-        if (L.chain64) {
+        if (pl->solver_fn) {
+            // the caller's level solver in place of the SOR (core/optical_flow.py:579-606): the
+            // tensor in the padded plane layout, then one call per frame once the stream has it
+            FRG_LAUNCH(launch_x_tensor(L.ref, img2, T, K, h, w, L.h_row, L.h_col, L.top ? 0 : 1,
+                                       pl->p.const_assumption, pl->xJ, st));
+            FRG_CUDA(cudaStreamSynchronize(st));
+            for (int f = 0; f < T; ++f) {
+                const int rc = pl->solver_fn(pl->solver_user, (int)li, f, h + 2, w + 2, K,
+                                             pl->xJ + (long long)f * 6 * K * mn, L.wpad64, pl->xuv + f * uv_fs,
+                                             pl->xuv + mn + f * uv_fs, L.alpha_x, L.alpha_y, L.h_col, L.h_row,
+                                             pl->xdu + (long long)f * mn, pl->xdv + (long long)f * mn);
+                if (rc != 0) return fail(FRG_ECALLBACK, "the level solver callback failed");
+            }
+        } else if (L.chain64) {
             // float64 chained SOR on diagonal-major buffers; the level's last pass writes
             // du, dv into the interiors of the padded xdu, xdv for the median
             const long long dp = (long long)L.g.D * L.g.P;
@@ -1722,6 +1737,16 @@ int frg_host_unregister(void* ptr)
         cudaGetLastError();
         return fail(FRG_ECUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
     }
+    return FRG_OK;
+}
+
+int frg_plan_set_level_solver(frg_plan* pl, frg_level_solver_fn fn, void* user)
+{
+    if (!pl) return fail(FRG_EINVAL, "NULL plan");
+    if (!pl->xpath || pl->p.gnc_stages > 0)
+        return fail(FRG_EUNSUPPORTED, "a host level solver needs a float64 plan without GNC stages");
+    pl->solver_fn = fn;
+    pl->solver_user = fn ? user : nullptr;
     return FRG_OK;
 }
 

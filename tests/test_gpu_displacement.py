@@ -264,10 +264,42 @@ def test_deterministic():
     np.testing.assert_array_equal(a, b)
 
 
+def test_caller_level_solver_matches_the_oracle(oracle):
+    """get_displacement with a caller-supplied level_solver_backend
+    (core/optical_flow.py:579-606): the device pyramid, warp and tensor hand
+    the solver the arrays the reference passes -- here the oracle's
+    restatement of compute_flow behind the reference's signature -- and the
+    flow matches the oracle's own get_displacement.  A solver's exception
+    reaches the caller."""
+    f1, m1, _ = pair_256(5, h=48, w=56)
+    f2, m2, _ = pair_256(6, h=48, w=56)
+    fixed, moving = np.stack([f1, f2 * 0.9], axis=2), np.stack([m1, m2 * 0.9], axis=2)
+    kw = dict(alpha=(1.5, 2.0), iterations=20)
+    shapes = []
+
+    def solver(J11, J22, J33, J12, J13, J23, weight, u, v, alpha, iterations, update_lag, verbose, a_data,
+               a_smooth, hx, hy, gnc_beta=None):
+        shapes.append((J11.shape, weight.shape, u.shape))
+        out = oracle.compute_flow(J11, J22, J33, J12, J13, J23, weight, u, v, alpha[0], alpha[1], iterations,
+                                  update_lag, a_data, a_smooth, hx, hy, gnc_beta=gnc_beta)
+        return out[..., 0], out[..., 1]
+
+    got = G.get_displacement(fixed, moving, level_solver_backend=solver, **kw)
+    want = oracle.get_displacement(fixed, moving, **kw)
+    assert shapes and all(j[2] == 2 and w[2] == 2 and len(u) == 2 and j[:2] == u for j, w, u in shapes)
+    assert_parity(got, want)
+
+    def bad(*args, **kwargs):
+        raise KeyError("solver failed")
+
+    with pytest.raises(KeyError):
+        G.get_displacement(fixed, moving, level_solver_backend=bad, **kw)
+
+
 def test_unsupported_options_raise():
     fixed, moving, _ = pair_256(4, h=32, w=32)
     with pytest.raises(NotImplementedError):
-        G.get_displacement(fixed, moving, level_solver_backend=lambda *a, **k: None)
+        G.get_displacement(fixed, moving, level_solver_backend=lambda *a, **k: None, precision="fp32")
     with pytest.raises(ValueError):
         G.get_displacement(fixed, moving, const_assumption="nope")
     with pytest.raises(ValueError):
